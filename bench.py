@@ -1,0 +1,386 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 path-trace pass: Mrays/s on the large procedural scene.
+
+Workload (one step): the whole 1920x1080 image of the ~2.1M-triangle
+procedural scene (1024x512-quad heightfield, 2000 boxes, 200 icospheres,
+64 emissive triangles, 1024x512 sky), 64 samples per pixel, max_bounces 8,
+traced through pt_trace in calls of at most 16 samples exactly as the
+reference's headless loop does (one tile covering the image).  A ray is every
+extend or shadow traversal.  The scene (BVH 134 MB + triangles 75 MB +
+attributes 235 MB) is larger than the 129 MB L2, so no L2 flush is needed
+between steps.
+
+Contract: python bench.py [--gpus N --steps K --warmup W] prints one JSON line.
+`--impl reference` times the CPU restatement of the reference's trace pass
+(oracle/, the reference itself cannot run here) on host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path[:0] = [str(ROOT), str(ROOT / "path-tracer_gb300")]
+
+import numpy as np  # noqa: E402
+
+WIDTH, HEIGHT, SPP, MAX_BOUNCES = 1920, 1080, 64, 8
+METRIC = "Mrays/s"
+KERNEL_NAMES = {"wavefront": 0, "plain": 1}
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--kernel", choices=list(KERNEL_NAMES), default="plain")
+    p.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
+    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--spp", type=int, default=SPP, help="samples per pixel of one step")
+    p.add_argument("--profile-run", action="store_true",
+                   help="only the timed steps (no counting pass, e2e or CPU baseline): for ncu captures")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+def workload_config(world, kernel: str) -> dict:
+    return {
+        "workload": "procedural scene (1024x512-quad heightfield + 2000 boxes + 200 icospheres s4 + 64 emissive "
+                    "triangles, 1024x512 sky), 1920x1080, 64 spp, max_bounces 8, one image per step",
+        "triangles": int(world.triangle_count()),
+        "bvh_nodes": int(world.node_count()),
+        "image": [WIDTH, HEIGHT],
+        "spp": SPP,
+        "max_bounces": MAX_BOUNCES,
+        "kernel": kernel,
+        "l2": "inputs larger than L2 (scene buffers ~440 MB vs 129 MB L2), no flush",
+        "seed": 1,
+    }
+
+
+def build_world():
+    import pathtracer as pt
+    world = pt.World.procedural()
+    world.set_aspect_ratio(WIDTH / HEIGHT)
+    return world, world.take_updates()
+
+
+def algorithmic_bytes(t: dict, emissive: int, paths: int) -> int:
+    """Bytes a ray batch must read or write at least once (roofline numerator):
+    per ray 32 (root) + 64 per interior node (both children) + 36 per
+    triangle test; per hit 112 attribute + 224 material + 36 hit triangle;
+    per triangle-light sample 16 * (2 + ceil(log2 E)) alias entries; per sky
+    sample 2 * 12; per escaped ray 64 (bilinear sky); per path 48
+    (accumulation read + write, storage texture write)."""
+    rays = t["extend_rays"] + t["shadow_rays"]
+    alias = 16 * (2 + math.ceil(math.log2(max(emissive, 1))))
+    return int(32 * rays + 64 * t["interior_visits"] + 36 * t["triangle_tests"] + 372 * t["hits"]
+               + alias * t["light_samples"] + 24 * t["sky_light_samples"] + 64 * t["sky_misses"] + 48 * paths)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = [line.split(",") for line in Path(self.file.name).read_text().splitlines() if line.strip()]
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.file.name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def pinned_updates(updates):
+    """A full WorldUpdates whose buffers live in pinned host memory (for the end-to-end timing)."""
+    import torch
+
+    from pathtracer import abi
+    keep = []
+
+    def pin(ptr, nbytes):
+        t = torch.empty(max(nbytes, 1), dtype=torch.uint8, pin_memory=True)
+        if nbytes:
+            C.memmove(t.data_ptr(), ptr, nbytes)
+        keep.append(t)
+        return t.data_ptr(), nbytes
+
+    s = updates.scene.contents
+    k = updates.skybox.contents
+    scene = abi.SceneUpload.from_buffer_copy(s)
+    h2d = 0
+    for field, ctype, count in (("geometries", abi.TriangleGeometry, s.triangle_count),
+                                ("attributes", abi.TriangleAttribute, s.triangle_count),
+                                ("materials", abi.Material, s.material_count),
+                                ("bvh_nodes", abi.BvhNode, s.node_count)):
+        p, n = pin(getattr(s, field), C.sizeof(ctype) * count)
+        setattr(scene, field, C.cast(p, C.POINTER(ctype)))
+        h2d += n
+    sky = abi.SkyboxUpload.from_buffer_copy(k)
+    p, n = pin(k.rgba, 16 * k.uniforms.width * k.uniforms.height)
+    sky.rgba = C.cast(p, C.POINTER(C.c_float))
+    h2d += n
+    if k.alias_count:
+        p, n = pin(k.alias_table, 12 * k.alias_count)
+        sky.alias_table = C.cast(p, C.POINTER(abi.SkyboxAliasEntry))
+        h2d += n
+    u = abi.WorldUpdates.from_buffer_copy(updates)
+    u.scene = C.pointer(scene)
+    u.skybox = C.pointer(sky)
+    h2d += 16 * updates.scene_alias_count + 64 + 16 + 16
+    keep.extend([scene, sky])
+    return u, keep, h2d
+
+
+def oracle_sample(updates, seconds: float, threads: int = 0):
+    """Time the oracle's FP32 restatement on a strided pixel subset of the same workload,
+    sized to take about `seconds`; returns (Mrays/s, threads, description)."""
+    import oracle
+    ow = oracle.world_from_updates(updates)
+    threads = threads or oracle.max_threads()
+
+    def run(stride_px: int, spp: int):
+        ys, xs = np.mgrid[0:HEIGHT:stride_px, 0:WIDTH:stride_px]
+        px = np.stack([xs.ravel(), ys.ravel()], axis=1).astype(np.uint32)
+        t0 = time.perf_counter()
+        _, rec = oracle.trace_paths(ow, (WIDTH, HEIGHT), MAX_BOUNCES, px, 1, spp, threads=threads, records=True)
+        dt = time.perf_counter() - t0
+        rays = int(rec["extend_rays"].sum() + rec["shadow_rays"].sum())
+        return rays, dt, px.shape[0]
+
+    rays, dt, _ = run(64, 4)  # calibration
+    rate = rays / max(dt, 1e-6)
+    want_rays = rate * seconds
+    rays_per_px = rays / max(1, (HEIGHT // 64 + 1) * (WIDTH // 64 + 1) * 4) * SPP
+    n_px = max(64, int(want_rays / max(rays_per_px, 1.0)))
+    stride = max(1, int(math.sqrt(WIDTH * HEIGHT / n_px)))
+    rays, dt, npx = run(stride, SPP)
+    desc = f"every {stride}th pixel in x and y ({npx} pixels) x {SPP} spp of the 1920x1080 image, {threads} threads"
+    return rays / dt / 1e6, threads, desc, dt
+
+
+def run_reference(args):
+    rank, _, world_size = dist_env()
+    if rank != 0:
+        return
+    world, updates = build_world()
+    import oracle
+    threads = oracle.max_threads()
+    per_step = max(2.0, min(args.cpu_seconds, 20.0))
+    values = []
+    for i in range(args.warmup + args.steps):
+        v, threads, desc, dt = oracle_sample(updates, per_step if i >= args.warmup else 1.0)
+        if i >= args.warmup:
+            values.append((v, dt))
+    value = float(np.mean([v for v, _ in values]))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean([d for _, d in values]) * 1e3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(world, "cpu"),
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's own trace pass (Rust + WGSL via wgpu) cannot run on this box; this is the "
+                "oracle's C++ restatement of src/render/trace.slang, OpenMP over paths",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    import pathtracer as pt
+    from pathtracer import abi
+
+    rank, local_rank, world_size = dist_env()
+    torch.cuda.set_device(local_rank)
+    pg = None
+    if world_size > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+
+    world, updates = build_world()
+    emissive = updates.scene_uniforms.contents.emissive_triangles_count
+    tracer = pt.PathTracer(updates, (WIDTH, HEIGHT), device=local_rank)
+    tracer.set_kernel(KERNEL_NAMES[args.kernel])
+    tracer.set_max_bounces(MAX_BOUNCES)
+
+    spp = args.spp
+
+    def step():
+        tracer.set_tile((WIDTH, HEIGHT), (0, 0), (WIDTH, HEIGHT))
+        remaining = spp
+        while remaining > 0:
+            remaining -= tracer.trace(remaining)
+
+    if args.profile_run:
+        for _ in range(args.steps):
+            step()
+        tracer.synchronize()
+        tracer.close()
+        print(json.dumps({"profile_run": True, "kernel": args.kernel, "spp": spp, "steps": args.steps}))
+        return
+
+    # counting pass over the identical (deterministic) workload
+    tracer.set_tile((WIDTH, HEIGHT), (0, 0), (WIDTH, HEIGHT))
+    totals, remaining = None, spp
+    while remaining > 0:
+        n, totals = tracer.trace_counted(remaining, totals)
+        remaining -= n
+    rays_per_step = totals["extend_rays"] + totals["shadow_rays"]
+    paths_per_step = WIDTH * HEIGHT * spp
+    bytes_per_step = algorithmic_bytes(totals, emissive, paths_per_step)
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    tracer.synchronize()
+
+    stream = torch.cuda.ExternalStream(tracer.stream())
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    tracer.synchronize()
+    tracer.reset_kernel_times()
+    tracer.set_profiling(True)
+    launches0 = tracer.launch_count()
+    with ClockSampler(local_rank) as clocks:
+        start.record(stream)
+        for _ in range(args.steps):
+            step()
+        stop.record(stream)
+        tracer.synchronize()
+        torch.cuda.synchronize()
+    elapsed_ms = start.elapsed_time(stop)
+    launches = tracer.launch_count() - launches0
+    times = tracer.kernel_times()
+    tracer.set_profiling(False)
+    if pg:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+        pg.barrier()
+    value = rays_per_step * args.steps * world_size / (elapsed_ms / 1e3) / 1e6
+
+    # dominant kernel and its roofline
+    cls = max(times.milliseconds, key=lambda k: times.milliseconds[k])
+    cls_launches = max(1, times.launches[cls])
+    avg_launch_s = times.milliseconds[cls] / cls_launches / 1e3
+    launches_per_step = cls_launches / args.steps
+    bytes_per_launch = bytes_per_step / launches_per_step
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = bytes_per_launch / avg_launch_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": cls, "bytes_per_launch": bytes_per_launch,
+                "avg_launch_ms": avg_launch_s * 1e3,
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback 6.8 TB/s"}
+
+    # end to end through the C ABI: world upload from pinned host memory, the
+    # render, and the RGBA8 result read back, every step
+    pinned, keep, h2d = pinned_updates(updates)
+    tracer.apply_updates(pinned)
+    step()
+    tracer.display_tile()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, args.e2e_steps)
+    for _ in range(e2e_steps):
+        tracer.apply_updates(pinned)
+        step()
+        tracer.display_tile()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = rays_per_step * e2e_steps / e2e_s / 1e6
+    if pg:
+        t = torch.tensor([e2e_s], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_value = rays_per_step * e2e_steps * world_size / float(t.item()) / 1e6
+
+    cpu = None
+    if rank == 0 and world_size == 1 and not args.no_cpu_baseline:
+        v, threads, desc, _ = oracle_sample(updates, args.cpu_seconds)
+        cpu = {"value": v, "unit": METRIC, "cores": threads, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world_size, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": dict(workload_config(world, args.kernel), parallelism=f"replicas x{world_size}"),
+            "rays_per_step": rays_per_step, "samples_per_s": paths_per_step * args.steps * world_size / (elapsed_ms / 1e3),
+            "roofline": roofline, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": WIDTH * HEIGHT * 4},
+            "gpu_launches": launches, "clocks": clocks.summary(),
+            "kernel_ms": {k: v for k, v in times.milliseconds.items() if times.launches[k]},
+        }
+        print(json.dumps(line), flush=True)
+    tracer.close()
+    del keep
+    if pg:
+        pg.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,573 @@
+// pt_device.cuh - device-side building blocks of the path-trace pass.
+//
+// Each function restates the trace.slang function named in its comment.
+// Everything here is compiled with -fmad=false -prec-div=true
+// -prec-sqrt=true -ftz=false, so +, -, *, / and sqrt round exactly like IEEE
+// binary32; fma appears only where the shader writes fma.  Vector helpers fix
+// one evaluation order (dot = (x*x' + y*y') + z*z', normalize = v * (1 /
+// sqrt(dot)), mix(a, b, t) = a*(1-t) + b*t, reflect(i, n) = i - (2 dot(n,i)) n,
+// fract(x) = x - floor(x)), and min/max drop NaN operands; the CPU oracle uses
+// the same definitions, which is what makes per-ray results bit-identical.
+#pragma once
+
+#include <stdint.h>
+
+#include "../../include/pt.h"
+#include "pt_fmath.h"
+
+namespace ptd {
+
+#define PTD __device__ __forceinline__
+
+constexpr float kPi = 3.14159265359f;
+constexpr float kInvPi = 0.31830988618f;
+constexpr float kInv2Pi = 0.15915494309189535f;
+constexpr float kTwoPi = 2.0f * 3.14159265359f;
+constexpr float kExposure = 0.00002604166f;
+constexpr float kFltMax = 0x1.fffffep+127f;
+constexpr uint64_t kFnvBasis = 0xcbf29ce484222325ull;
+constexpr uint64_t kFnvPrime = 0x100000001b3ull;
+
+struct f2 {
+    float x, y;
+};
+struct f3 {
+    float x, y, z;
+};
+
+PTD f3 mk(float x, float y, float z) { return f3{x, y, z}; }
+PTD f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+PTD f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+PTD f3 operator-(f3 a) { return {-a.x, -a.y, -a.z}; }
+PTD f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+PTD f3 operator/(f3 a, f3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
+PTD f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+PTD f3 operator*(float s, f3 a) { return {s * a.x, s * a.y, s * a.z}; }
+PTD f3 operator/(f3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+PTD f3 operator/(float s, f3 a) { return {s / a.x, s / a.y, s / a.z}; }
+PTD f3 operator+(f3 a, float s) { return {a.x + s, a.y + s, a.z + s}; }
+PTD f3 operator-(float s, f3 a) { return {s - a.x, s - a.y, s - a.z}; }
+PTD f3 operator-(f3 a, float s) { return {a.x - s, a.y - s, a.z - s}; }
+PTD float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+PTD f3 cross(f3 a, f3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+PTD float rsqrt_(float x) { return 1.0f / sqrtf(x); }
+PTD float length(f3 v) { return sqrtf(dot(v, v)); }
+PTD f3 normalize(f3 v) { return v * rsqrt_(dot(v, v)); }
+PTD float mix(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+PTD f3 mix(f3 a, f3 b, float t) { return {mix(a.x, b.x, t), mix(a.y, b.y, t), mix(a.z, b.z, t)}; }
+PTD float saturate(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+PTD f3 saturate(f3 v) { return {saturate(v.x), saturate(v.y), saturate(v.z)}; }
+PTD float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+PTD float fract(float x) { return x - floorf(x); }
+PTD float signf(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+PTD f3 reflect(f3 i, f3 n) { return i - (2.0f * dot(n, i)) * n; }
+PTD bool any_positive(f3 v) { return v.x > 0.0f || v.y > 0.0f || v.z > 0.0f; }
+PTD float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+PTD float comp(f3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+
+// WGSL u32(f32): truncation, saturating, NaN -> 0
+PTD uint32_t to_u32(float x) { return __float2uint_rz(x); }
+
+// rand(), trace.slang:195-202
+PTD float rand_next(uint32_t& s) {
+    s = s * 747796405u + 2891336453u;
+    const uint32_t word = ((s >> ((s >> 28u) + 4u)) ^ s) * 277803737u;
+    return __uint_as_float(0x3f800000u | (((word >> 22u) ^ word) >> 9u)) - 1.0f;
+}
+
+// seed of compute_main, trace.slang:736-737 (global_id.z is always 0)
+PTD uint32_t seed(uint32_t px, uint32_t py, uint32_t sample_count) {
+    uint32_t s = (px * 0x9E3779B9u) ^ (py * 0x85EBCA6Bu) ^ (sample_count * 0x27D4EB2Du) ^ 0xA511E9B3u;
+    return s | 1u;
+}
+
+// the world bind group (trace.slang:163-190) as device pointers
+struct World {
+    const pt_triangle_geometry* geo;
+    const pt_triangle_attribute* attr;
+    const pt_material* mat;
+    const pt_bvh_node* nodes;
+    const uint8_t* srgb;
+    const uint8_t* linear;
+    uint32_t srgb_count;
+    uint32_t linear_count;
+    const float4* sky;
+    const pt_skybox_alias_entry* sky_alias;
+    const pt_scene_alias_entry* scene_alias;
+    pt_skybox_uniforms sky_u;
+    pt_scene_uniforms scene;
+    pt_camera camera;
+    const float* srgb_lut;  // sRGB EOTF per byte (Rgba8UnormSrgb decode), 256 floats
+    int any_alpha;          // some material is not opaque
+};
+
+// per-path instrumentation (pt_path_record) kept in registers while tracing
+struct Counters {
+    uint64_t visit_hash;
+    uint32_t extend_rays, shadow_rays, interior_visits, leaf_visits, triangle_tests, rand_draws;
+    uint32_t hits, sky_misses, light_samples, sky_light_samples;
+};
+
+// add one path's counters into device totals (one atomic per field per warp;
+// __reduce_add_sync sums over exactly the lanes in the active mask)
+PTD void add_totals(unsigned long long* totals, const Counters& c) {
+    const uint32_t v[PT_COUNT_FIELDS] = {c.extend_rays, c.shadow_rays, c.interior_visits, c.leaf_visits,
+                                         c.triangle_tests, c.rand_draws, c.hits, c.sky_misses,
+                                         c.light_samples, c.sky_light_samples};
+    const unsigned mask = __activemask();
+    unsigned lane;
+    asm volatile("mov.u32 %0, %%laneid;" : "=r"(lane));
+    const unsigned leader = (unsigned)(__ffs(mask) - 1);
+#pragma unroll
+    for (int f = 0; f < PT_COUNT_FIELDS; ++f) {
+        const unsigned sum = __reduce_add_sync(mask, v[f]);
+        if (lane == leader) atomicAdd(totals + f, (unsigned long long)sum);
+    }
+}
+
+template <bool kRec>
+struct Rec {
+    PTD void visit(uint32_t) {}
+    PTD void interior() {}
+    PTD void leaf() {}
+    PTD void tri() {}
+    PTD void draw() {}
+};
+template <>
+struct Rec<true> {
+    Counters* c;
+    PTD void visit(uint32_t i) { c->visit_hash = (c->visit_hash ^ i) * kFnvPrime; }
+    PTD void interior() { c->interior_visits += 1; }
+    PTD void leaf() { c->leaf_visits += 1; }
+    PTD void tri() { c->triangle_tests += 1; }
+    PTD void draw() { c->rand_draws += 1; }
+};
+
+template <bool kRec>
+struct Rng {
+    uint32_t s;
+    Rec<kRec> rec;
+    PTD float operator()() {
+        rec.draw();
+        return rand_next(s);
+    }
+};
+
+PTD f3 vert(const World& w, uint32_t tri, int k) {
+    const float* v = w.geo[tri].v0 + 3 * k;
+    return mk(__ldg(v), __ldg(v + 1), __ldg(v + 2));
+}
+
+struct Tri {
+    f3 v0, v1, v2;
+};
+PTD Tri load_tri(const World& w, uint32_t tri) {
+    const float* p = w.geo[tri].v0;
+    Tri t;
+    t.v0 = mk(__ldg(p + 0), __ldg(p + 1), __ldg(p + 2));
+    t.v1 = mk(__ldg(p + 3), __ldg(p + 4), __ldg(p + 5));
+    t.v2 = mk(__ldg(p + 6), __ldg(p + 7), __ldg(p + 8));
+    return t;
+}
+
+// nearest + clamp-to-edge atlas fetch (default sampler, world_resources.rs:447-450)
+PTD float4 atlas(const World& w, bool srgb, int32_t layer, f2 uv) {
+    const uint32_t count = srgb ? w.srgb_count : w.linear_count;
+    const uint8_t* base = srgb ? w.srgb : w.linear;
+    if (count == 0u) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const uint32_t l = layer < 0 ? 0u : ((uint32_t)layer >= count ? count - 1u : (uint32_t)layer);
+    const float fx = floorf(uv.x * 8192.0f), fy = floorf(uv.y * 8192.0f);
+    const uint32_t ix = fx >= 8191.0f ? 8191u : to_u32(fx);
+    const uint32_t iy = fy >= 8191.0f ? 8191u : to_u32(fy);
+    const uchar4 p = __ldg(reinterpret_cast<const uchar4*>(base) + ((uint64_t)l * PT_ATLAS_SIZE + iy) * PT_ATLAS_SIZE + ix);
+    if (srgb)
+        return make_float4(__ldg(w.srgb_lut + p.x), __ldg(w.srgb_lut + p.y), __ldg(w.srgb_lut + p.z), (float)p.w / 255.0f);
+    return make_float4((float)p.x / 255.0f, (float)p.y / 255.0f, (float)p.z / 255.0f, (float)p.w / 255.0f);
+}
+
+PTD f2 atlas_uv(f2 uv, const float* os) { return {fma_(uv.x, os[2], os[0]), fma_(uv.y, os[3], os[1])}; }
+
+// bilinear + clamp-to-edge skybox fetch (skybox sampler, world_resources.rs:451-456)
+PTD uint32_t sky_index(float f, uint32_t n, int off) {
+    if (!(f == f)) return 0u;
+    int64_t i = f < -1e9f ? -1000000000ll : (f > 1e9f ? 1000000000ll : (int64_t)f);
+    i += off;
+    if (i < 0) i = 0;
+    if (i > (int64_t)n - 1) i = (int64_t)n - 1;
+    return (uint32_t)i;
+}
+PTD f3 sky_px(const World& w, uint32_t ix, uint32_t iy) {
+    const float4 p = __ldg(w.sky + (uint64_t)iy * w.sky_u.width + ix);
+    return mk(p.x, p.y, p.z);
+}
+PTD f3 skybox_bilinear(const World& w, f2 uv) {
+    const uint32_t W = w.sky_u.width, H = w.sky_u.height;
+    const float x = uv.x * (float)W - 0.5f, y = uv.y * (float)H - 0.5f;
+    const float x0 = floorf(x), y0 = floorf(y);
+    const float fx = x - x0, fy = y - y0;
+    const uint32_t ix0 = sky_index(x0, W, 0), ix1 = sky_index(x0, W, 1);
+    const uint32_t iy0 = sky_index(y0, H, 0), iy1 = sky_index(y0, H, 1);
+    const f3 top = mix(sky_px(w, ix0, iy0), sky_px(w, ix1, iy0), fx);
+    const f3 bottom = mix(sky_px(w, ix0, iy1), sky_px(w, ix1, iy1), fx);
+    return mix(top, bottom, fy);
+}
+
+// orthonormal_tangent, trace.slang:207-218
+PTD f3 orthonormal_tangent(f3 tangent, f3 normal) {
+    const f3 projected = tangent - dot(normal, tangent) * normal;
+    const float ls = dot(projected, projected);
+    if (ls > 1e-12f) return projected * rsqrt_(ls);
+    const float s = normal.z >= 0.0f ? 1.0f : -1.0f;
+    const float a = -1.0f / (s + normal.z);
+    return mk(fma_(s * normal.x * normal.x, a, 1.0f), s * normal.x * normal.y * a, -s * normal.x);
+}
+
+PTD float fifth_power(float x) { return x * x * x * x * x; }
+
+// fresnel_exact, trace.slang:330-341
+PTD float fresnel_exact(float ior, float cos_i) {
+    const float s = fma_(-cos_i, cos_i, 1.0f) / (ior * ior);
+    if (s >= 1.0f) return 1.0f;
+    const float cos_t = sqrtf(1.0f - s);
+    const float rs = fma_(-ior, cos_t, cos_i) / fma_(ior, cos_t, cos_i);
+    const float rp = fma_(-ior, cos_i, cos_t) / fma_(ior, cos_i, cos_t);
+    return 0.5f * (rs * rs + rp * rp);
+}
+
+// ggx_lambda, trace.slang:347-352
+PTD float ggx_lambda(f3 v, f2 a) {
+    return fma_(0.5f, sqrtf(1.0f + (a.x * a.x * v.x * v.x + a.y * a.y * v.y * v.y) / (v.z * v.z)), -0.5f);
+}
+
+// sample_VNDF, trace.slang:356-364
+PTD f3 sample_vndf(f3 wo, f2 a, float r, float two_pi_r) {
+    const f3 ww = normalize(mk(wo.x * a.x, wo.y * a.y, wo.z));
+    const float z = fma_(1.0f - r, 1.0f + ww.z, -ww.z);
+    const float sin_theta = sqrtf(saturate(fma_(-z, z, 1.0f)));
+    const float x = sin_theta * ptm::cosf_(two_pi_r);
+    const float y = sin_theta * ptm::sinf_(two_pi_r);
+    const f3 h = mk(x, y, z) + ww;
+    return normalize(mk(h.x * a.x, h.y * a.y, h.z));
+}
+
+// alpha_anisotropic, trace.slang:369-375
+PTD f2 alpha_anisotropic(float roughness, float anisotropy) {
+    const float iso = 1.0f - anisotropy;
+    const float at = roughness * roughness * 1.41421356237f * rsqrt_(fma_(iso, iso, 1.0f));
+    return {fmaxf(at, 1e-4f), fmaxf(at * iso, 1e-4f)};
+}
+
+// specular_ior_modulated, trace.slang:379-391
+PTD float specular_ior_modulated(float ior, float weight) {
+    const float num = ior - 1.0f;
+    const float den = ior + 1.0f;
+    const float f0 = num * num / (den * den);
+    const float f0s = signf(ior - 1.0f) * sqrtf(fminf(weight * f0, __uint_as_float(0x3f800000u - 1u)));
+    return (1.0f + f0s) / (1.0f - f0s);
+}
+
+// power_heuristic, trace.slang:416-424
+PTD float power_heuristic(float pdf, float other) {
+    const float scale = fmaxf(pdf, other);
+    if (scale <= 0.0f) return 0.0f;
+    const float p = pdf / scale;
+    const float q = other / scale;
+    return p * p / (p * p + q * q);
+}
+
+PTD f2 interp_uv(const pt_triangle_attribute& a, float u, float v, float w2) {
+    return {fract(u * a.uv0[0] + v * a.uv1[0] + w2 * a.uv2[0]), fract(u * a.uv0[1] + v * a.uv1[1] + w2 * a.uv2[1])};
+}
+
+// coverage, trace.slang:426-443
+PTD float coverage(const World& w, const pt_material& m, f2 uv) {
+    if (m.alpha_mode == PT_ALPHA_MODE_OPAQUE) return 1.0f;
+    float alpha = m.base_color[3];
+    if (m.base_color_tex_layer >= 0) alpha *= atlas(w, true, m.base_color_tex_layer, atlas_uv(uv, m.base_color_uv)).w;
+    if (m.alpha_mode == PT_ALPHA_MODE_MASK) return alpha >= m.alpha_cutoff ? 1.0f : 0.0f;
+    return alpha;
+}
+
+// passes_through, trace.slang:446-454
+template <bool kRec>
+PTD bool passes_through(const World& w, uint32_t tri, float v, float w2, Rng<kRec>& rng) {
+    const pt_triangle_attribute& attr = w.attr[tri];
+    const pt_material& m = w.mat[attr.material_index];
+    if (m.alpha_mode == PT_ALPHA_MODE_OPAQUE) return false;
+    const f2 uv = interp_uv(attr, 1.0f - v - w2, v, w2);
+    return coverage(w, m, uv) <= rng();
+}
+
+// evaluate_emission, trace.slang:455-466
+PTD f3 evaluate_emission(const World& w, const pt_material& m, f2 uv) {
+    f3 color = mk(m.emission_color_and_luminance[0], m.emission_color_and_luminance[1], m.emission_color_and_luminance[2]);
+    if (m.emission_tex_layer >= 0) {
+        const float4 t = atlas(w, true, m.emission_tex_layer, atlas_uv(uv, m.emission_uv));
+        color = color * mk(t.x, t.y, t.z);
+    }
+    return m.emission_weight * m.emission_color_and_luminance[3] * color;
+}
+
+// skybox_uv, trace.slang:467-472
+PTD f2 skybox_uv(f3 d) {
+    return {fract(fma_(ptm::atan2f_(d.z, d.x), kInv2Pi, 0.5f)), ptm::atan2f_(sqrtf(d.x * d.x + d.z * d.z), d.y) * kInvPi};
+}
+
+// evaluate_skybox, trace.slang:473-475
+PTD f3 evaluate_skybox(const World& w, f3 d) { return skybox_bilinear(w, skybox_uv(d)) * w.sky_u.average_luminance; }
+
+// skybox_texel_solid_angle, trace.slang:476-481
+PTD float skybox_texel_solid_angle(const World& w, uint32_t row) {
+    const float step = kPi / (float)w.sky_u.height;
+    const uint32_t other = w.sky_u.height - 1u - row;
+    const uint32_t pole_row = row < other ? row : other;
+    return (kTwoPi / (float)w.sky_u.width) * 2.0f * ptm::sinf_(((float)pole_row + 0.5f) * step) * ptm::sinf_(0.5f * step);
+}
+
+// skybox_light_pdf, trace.slang:482-489
+PTD float skybox_light_pdf(const World& w, f3 d, float prob) {
+    if (prob <= 0.0f) return 0.0f;
+    const f2 uv = skybox_uv(d);
+    uint32_t px = to_u32(uv.x * (float)w.sky_u.width);
+    uint32_t py = to_u32(uv.y * (float)w.sky_u.height);
+    if (px > w.sky_u.width - 1u) px = w.sky_u.width - 1u;
+    if (py > w.sky_u.height - 1u) py = w.sky_u.height - 1u;
+    return prob * __ldg(&w.sky_alias[(uint64_t)py * w.sky_u.width + px].selection_probability) /
+           skybox_texel_solid_angle(w, py);
+}
+
+// triangle_selection_probability, trace.slang:490-507
+PTD float triangle_selection_probability(const World& w, uint32_t tri) {
+    uint32_t first = 0u, end = w.scene.emissive_triangles_count;
+    while (first < end) {
+        const uint32_t middle = first + (end - first) / 2u;
+        const uint32_t ti = __ldg(&w.scene_alias[middle].triangle_index);
+        if (ti < tri) first = middle + 1u;
+        else if (ti > tri) end = middle;
+        else return __ldg(&w.scene_alias[middle].selection_probability);
+    }
+    return 0.0f;
+}
+
+// triangle_light_pdf, trace.slang:508-523
+PTD float triangle_light_pdf(const World& w, uint32_t tri, f3 d, float dist2, float prob) {
+    if (prob <= 0.0f) return 0.0f;
+    const Tri t = load_tri(w, tri);
+    const float area = 0.5f * fabsf(dot(cross(t.v1 - t.v0, t.v2 - t.v0), d));
+    if (area <= 0.0f) return 0.0f;
+    return prob * dist2 / area;
+}
+
+struct LightSample {
+    f3 direction;
+    float distance;
+    f3 emission;
+    float pdf;
+    int32_t triangle_index;
+};
+
+// sample_light, trace.slang:531-592
+template <bool kRec>
+PTD LightSample sample_light(const World& w, f3 origin, Rng<kRec>& rng, Counters* c) {
+    LightSample r;
+    r.direction = mk(0.0f, 0.0f, 0.0f);
+    r.distance = 0.0f;
+    r.emission = mk(0.0f, 0.0f, 0.0f);
+    r.pdf = 0.0f;
+    r.triangle_index = -1;
+    const float p0 = w.scene.light_probabilities[0], p1 = w.scene.light_probabilities[1];
+    if (p0 + p1 <= 0.0f) return r;
+    if (rng() < p0) {
+        if (kRec) c->light_samples += 1;
+        const uint32_t count = w.scene.emissive_triangles_count;
+        uint32_t slot = to_u32(rng() * (float)count);
+        if (slot > count - 1u) slot = count - 1u;
+        const pt_scene_alias_entry cand = w.scene_alias[slot];
+        const pt_scene_alias_entry entry = w.scene_alias[rng() < cand.threshold ? slot : cand.alias_index];
+        const Tri t = load_tri(w, entry.triangle_index);
+        const float root = sqrtf(rng());
+        const float u = 1.0f - root;
+        const float v = root * (1.0f - rng());
+        const float wb = 1.0f - u - v;
+        const f3 delta = u * t.v0 + v * t.v1 + wb * t.v2 - origin;
+        const float d2 = dot(delta, delta);
+        if (d2 <= 0.0f) return r;
+        r.distance = sqrtf(d2);
+        r.direction = delta / r.distance;
+        r.triangle_index = (int32_t)entry.triangle_index;
+        r.pdf = triangle_light_pdf(w, entry.triangle_index, r.direction, d2, p0 * entry.selection_probability);
+        const pt_triangle_attribute& attr = w.attr[entry.triangle_index];
+        const f2 uv = interp_uv(attr, u, v, wb);
+        const pt_material& m = w.mat[attr.material_index];
+        r.emission = coverage(w, m, uv) * evaluate_emission(w, m, uv);
+    } else {
+        if (kRec) c->sky_light_samples += 1;
+        const uint32_t W = w.sky_u.width, H = w.sky_u.height;
+        const uint32_t count = W * H;
+        uint32_t slot = to_u32(rng() * (float)count);
+        if (slot > count - 1u) slot = count - 1u;
+        const pt_skybox_alias_entry cand = w.sky_alias[slot];
+        const uint32_t index = rng() < cand.threshold ? slot : cand.alias_index;
+        const uint32_t row = index / W, column = index % W;
+        const float phi = (((float)column + rng()) / (float)W - 0.5f) * kTwoPi;
+        const bool north = row < H / 2u;
+        const uint32_t pole_row = north ? row : H - 1u - row;
+        const float half_step = 0.5f * kPi / (float)H;
+        const float a = ptm::sinf_((float)pole_row * half_step);
+        const float b = ptm::sinf_((float)(pole_row + 1u) * half_step);
+        const float shs = mix(a * a, b * b, rng());
+        const float cos_theta = 1.0f - 2.0f * shs;
+        const float sin_theta = 2.0f * sqrtf(fmaxf(0.0f, shs * (1.0f - shs)));
+        r.direction = mk(sin_theta * ptm::cosf_(phi), north ? cos_theta : -cos_theta, sin_theta * ptm::sinf_(phi));
+        r.distance = kFltMax;
+        r.pdf = skybox_light_pdf(w, r.direction, p1);
+        r.emission = evaluate_skybox(w, r.direction);
+    }
+    return r;
+}
+
+// intersect_aabb, trace.slang:597-609, on a node's bounds
+PTD float intersect_aabb(const float* bmin, const float* bmax, f3 nod, f3 rcp, float hit_t) {
+    const float t0x = fma_(bmin[0], rcp.x, nod.x), t0y = fma_(bmin[1], rcp.y, nod.y), t0z = fma_(bmin[2], rcp.z, nod.z);
+    const float t1x = fma_(bmax[0], rcp.x, nod.x), t1y = fma_(bmax[1], rcp.y, nod.y), t1z = fma_(bmax[2], rcp.z, nod.z);
+    const float t_near = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
+    const float t_far = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+    return (t_near <= t_far && t_far > 0.0f && t_near < hit_t) ? fmaxf(0.0f, t_near) : -1.0f;
+}
+
+// watertight shear setup, trace.slang:769-783
+struct Shear {
+    int kx, ky, kz;
+    float sx, sy, sz;
+};
+PTD Shear make_shear(f3 d, f3 rcp) {
+    const float adx = fabsf(d.x), ady = fabsf(d.y), adz = fabsf(d.z);
+    const int kxy = adx > ady ? 0 : 1;
+    const int kz = (kxy == 0 ? adx : ady) > adz ? kxy : 2;
+    const int kx_val = kz == 2 ? 0 : kz + 1;
+    const int ky_val = kx_val == 2 ? 0 : kx_val + 1;
+    const bool is_neg = comp(d, kz) < 0.0f;
+    Shear s;
+    s.kz = kz;
+    s.kx = is_neg ? ky_val : kx_val;
+    s.ky = is_neg ? kx_val : ky_val;
+    s.sz = comp(rcp, kz);
+    s.sx = -comp(d, s.kx) * s.sz;
+    s.sy = -comp(d, s.ky) * s.sz;
+    return s;
+}
+
+// watertight ray-triangle test, trace.slang:807-834 (false = rejected)
+PTD bool triangle_test(const Tri& t, f3 o, const Shear& s, float* t_out, float* v_out, float* w_out) {
+    const f3 A = t.v0 - o, B = t.v1 - o, C = t.v2 - o;
+    const float akz = comp(A, s.kz), bkz = comp(B, s.kz), ckz = comp(C, s.kz);
+    const float ax = fma_(s.sx, akz, comp(A, s.kx));
+    const float ay = fma_(s.sy, akz, comp(A, s.ky));
+    const float bx = fma_(s.sx, bkz, comp(B, s.kx));
+    const float by = fma_(s.sy, bkz, comp(B, s.ky));
+    const float cx = fma_(s.sx, ckz, comp(C, s.kx));
+    const float cy = fma_(s.sy, ckz, comp(C, s.ky));
+    const float U = fma_(cx, by, -cy * bx);
+    const float V = fma_(ax, cy, -ay * cx);
+    const float W = fma_(bx, ay, -by * ax);
+    if (fminf(U, fminf(V, W)) < 0.0f && fmaxf(U, fmaxf(V, W)) > 0.0f) return false;
+    const float det = U + V + W;
+    if (det == 0.0f) return false;
+    const float inv_det = 1.0f / det;
+    *t_out = s.sz * fma_(U, akz, fma_(V, bkz, W * ckz)) * inv_det;
+    *v_out = V * inv_det;
+    *w_out = W * inv_det;
+    return true;
+}
+
+// E_FON_exact, trace.slang:318-323
+PTD float e_fon_exact(float mu, float r) {
+    const float af = 1.0f / fma_(0.28779340921f, r, 1.0f);
+    const float si = sqrtf(fma_(-mu, mu, 1.0f));
+    const float g = si * (ptm::acosf_(mu) - si * mu) + 0x1.555556p-1f * ((si / mu) * (1.0f - (si * si * si)) - si);
+    return af + r * af * kInvPi * g;
+}
+
+// state of one shading point shared by both lobe evaluations (trace.slang:1097-1181)
+struct Bsdf {
+    float p_ggx, p_diffuse;
+    f3 base_color;
+    float base_weight, base_metalness, base_diffuse_roughness;
+    f3 specular_color;
+    float specular_weight, ior_m;
+    f2 alpha;
+    float opl;
+    f3 f0;
+    f3 e_dielectric;
+    float la, lb, lc, ld;  // ltc_coefficients
+    f3 bx, by;             // rows 0 and 1 of orthonormal_basis_ltc_wo (row 2 = z axis)
+    float p_u, p_c;
+};
+
+struct Lobes {
+    f3 f;
+    float pdf;
+};
+
+// evaluate_lobes, trace.slang:229-315
+PTD Lobes evaluate_lobes(f3 wo, f3 wi, const Bsdf& b) {
+    const f3 h = normalize(wo + wi);
+    const float hdotw = dot(h, wo);
+    const float g1 = 1.0f / b.opl;
+    const float g2 = 1.0f / (b.opl + ggx_lambda(wi, b.alpha));
+    const float dh = (h.x * h.x) / (b.alpha.x * b.alpha.x) + (h.y * h.y) / (b.alpha.y * b.alpha.y) + h.z * h.z;
+    const float D = kInvPi / (b.alpha.x * b.alpha.y * dh * dh);
+    const float ts = D * g2 / (4.0f * wi.z * wo.z);
+    const float omh = 1.0f - hdotw;
+    const float p5 = fifth_power(omh);
+    const f3 fa = (0.00105024005f * hdotw * omh) * (1.0f - b.specular_color);
+    const f3 fb = 9031.0f * b.f0 + 7776.0f;
+    const f3 fc = b.f0 - 1.0f;
+    const f3 fm = mk(fma_(fa.x, fb.x, fc.x), fma_(fa.y, fb.y, fc.y), fma_(fa.z, fb.z, fc.z));
+    const f3 f82 = b.f0 - p5 * fm;
+    const f3 f_conductor = saturate(b.specular_weight * f82) * ts;
+    const f3 f_dielectric = b.specular_color * fresnel_exact(b.ior_m, hdotw) * ts;
+    const f3 rho = b.base_color;
+    const float r = b.base_diffuse_roughness;
+    const float s_f = wi.x * wo.x + wi.y * wo.y;
+    const float sovert_f = s_f > 0.0f ? s_f / fmaxf(wo.z, wi.z) : s_f;
+    const float af = 1.0f / fma_(0.28779340921f, r, 1.0f);
+    const f3 f_ss = rho * kInvPi * af * fma_(r, sovert_f, 1.0f);
+    const float efo = e_fon_exact(wo.z, r);
+    const float efi = e_fon_exact(wi.z, r);
+    const float avg_ef = af * fma_(0.07248821245f, r, 1.0f);
+    const f3 rho_ms = rho * rho * avg_ef / (1.0f - rho * (1.0f - avg_ef));
+    const f3 f_ms = (rho_ms * kInvPi) * fmaxf(1.0e-7f, 1.0f - efo) * fmaxf(1.0e-7f, 1.0f - efi) / fmaxf(1.0e-7f, 1.0f - avg_ef);
+    const f3 f_diffuse = b.base_weight * (f_ss + f_ms);
+    const f3 f_glossy_diffuse = f_dielectric + (1.0f - b.e_dielectric) * f_diffuse;
+    const f3 f_total = mix(f_glossy_diffuse, f_conductor, b.base_metalness);
+    const float pdf_ggx = D * g1 / (4.0f * wo.z);
+    const f3 wl = mk(dot(b.bx, wi), dot(b.by, wi), dot(mk(0.0f, 0.0f, 1.0f), wi));
+    const float a = b.la, bb = b.lb, c = b.lc, d = b.ld;
+    const float det_m = c * fma_(-bb, d, a);
+    const f3 wh = mk(c * (wl.x - bb * wl.z), (a - bb * d) * wl.y, -c * (d * wl.x - a * wl.z));
+    const float len_sqr = dot(wh, wh);
+    const float s_pdf = fma_(0.5f, rsqrt_(fma_(d, d, 1.0f)), 0.5f);
+    const float pdf_c = (det_m * det_m) / (len_sqr * len_sqr) * fmaxf(wh.z, 0.0f) / (kPi * s_pdf);
+    const float pdf_eon = b.p_u * 0.15915494309f + b.p_c * pdf_c;
+    return {f_total, b.p_ggx * pdf_ggx + b.p_diffuse * pdf_eon};
+}
+
+// estimate_e_dielectric, trace.slang:396-411
+template <bool kRec>
+PTD f3 estimate_e_dielectric(f3 wo, float opl, f2 alpha, float ior_m, f3 spec_color, Rng<kRec>& rng) {
+    float sum = 0.0f;
+#pragma unroll 1
+    for (int i = 0; i < 16; ++i) {
+        const float r1 = rng();
+        const float tpr = kTwoPi * rng();
+        const f3 h = sample_vndf(wo, alpha, r1, tpr);
+        const f3 wi = reflect(-wo, h);
+        if (wi.z <= 0.0f) continue;
+        const float f = fresnel_exact(ior_m, dot(h, wo));
+        sum += f * opl / (opl + ggx_lambda(wi, alpha));
+    }
+    return spec_color * sum / 16.0f;
+}
+
+}  // namespace ptd

@@ -1,0 +1,44 @@
+// pt_layout_check.cpp - compile-time proof that the C ABI structs match the
+// byte layouts of the reference's bytemuck GPU structs (world.rs:139-537,
+// path_tracer.rs:45-57) and the shader's structs (trace.slang:48-152).
+#include <cstddef>
+
+#include "../../include/pt.h"
+
+#define CHECK_SIZE(T, n) static_assert(sizeof(T) == (n), #T " size")
+#define CHECK_OFF(T, f, n) static_assert(offsetof(T, f) == (n), #T "." #f " offset")
+
+CHECK_SIZE(pt_triangle_geometry, 36);
+CHECK_SIZE(pt_triangle_attribute, 112);
+CHECK_OFF(pt_triangle_attribute, n0, 4);
+CHECK_OFF(pt_triangle_attribute, uv0, 40);
+CHECK_OFF(pt_triangle_attribute, t0, 64);
+CHECK_OFF(pt_triangle_attribute, t2, 96);
+CHECK_SIZE(pt_bvh_node, 32);
+CHECK_OFF(pt_bvh_node, left_first, 12);
+CHECK_OFF(pt_bvh_node, aabb_max, 16);
+CHECK_OFF(pt_bvh_node, tri_count, 28);
+CHECK_SIZE(pt_material, 224);
+CHECK_OFF(pt_material, base_weight, 16);
+CHECK_OFF(pt_material, emission_weight, 28);
+CHECK_OFF(pt_material, emission_color_and_luminance, 32);
+CHECK_OFF(pt_material, specular_color_and_weight, 48);
+CHECK_OFF(pt_material, specular_roughness, 64);
+CHECK_OFF(pt_material, specular_ior, 80);
+CHECK_OFF(pt_material, normal_scale, 88);
+CHECK_OFF(pt_material, alpha_mode, 92);
+CHECK_OFF(pt_material, alpha_cutoff, 96);
+CHECK_OFF(pt_material, base_color_tex_layer, 104);
+CHECK_OFF(pt_material, specular_weight_tex_layer, 124);
+CHECK_OFF(pt_material, base_color_uv, 128);
+CHECK_OFF(pt_material, specular_color_uv, 192);
+CHECK_OFF(pt_material, specular_weight_uv, 208);
+CHECK_SIZE(pt_camera, 64);
+CHECK_SIZE(pt_scene_uniforms, 16);
+CHECK_SIZE(pt_scene_alias_entry, 16);
+CHECK_SIZE(pt_skybox_uniforms, 16);
+CHECK_SIZE(pt_skybox_alias_entry, 12);
+CHECK_SIZE(pt_trace_parameters, 32);
+CHECK_SIZE(pt_path_record, 128);
+
+extern "C" int pt_layout_checked(void) { return 1; }

@@ -1,0 +1,638 @@
+// trace_wavefront.cu - wavefront kernels of the trace pass (see pt_wavefront.h).
+//
+// Layout in HBM
+//   ray queues (ping-pong, slot order):  o = (origin xyz, path id bits)
+//                                        d = (direction xyz, rng state bits)
+//                                        T = (throughput xyz, previous BSDF pdf)
+//   hit per slot:                        (t, triangle bits, v, w)
+//   colour per path id:                  (final_color xyz, unused)
+//   shadow queue (slot order):           (origin xyz, path id), (direction xyz, distance),
+//                                        (contribution xyz, light triangle bits)
+//   BVH nodes copied 32 bytes past a 256-byte boundary, so the two children
+//   of every interior node (indices 2k+1, 2k+2) fill one aligned 64-byte
+//   block read with four 16-byte loads; triangles padded to 3 x float4.
+// Every path runs exactly the arithmetic of the plain kernel (pt_path.cuh),
+// in the same order, so results are bit-identical.
+#include <vector>
+
+#include "pt_path.cuh"
+#include "pt_wavefront.h"
+
+namespace ptd {
+
+struct Fast {
+    const float4* pairs;  // node i at pairs[2i], pairs[2i+1]
+    const float4* tri4;   // triangle i at tri4[3i .. 3i+2]
+};
+
+struct Queues {
+    float4* o[2];
+    float4* d[2];
+    float4* T[2];
+    float4* hit;
+    float4* color;
+    float4* so;
+    float4* sd;
+    float4* sc;
+    uint32_t* cnt;  // [0], [1] ray queue lengths, [2] shadow length, [3] extend fetch, [4] shadow fetch
+    Counters* rec;  // per path (recording variants)
+    int32_t* rec_hits;
+};
+
+constexpr int kExtendThreads = 128;
+constexpr int kShadeThreads = 128;
+
+PTD Tri load_tri4(const Fast& f, uint32_t tri) {
+    const float4* p = f.tri4 + 3 * (size_t)tri;
+    const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+    Tri t;
+    t.v0 = mk(a.x, a.y, a.z);
+    t.v1 = mk(b.x, b.y, b.z);
+    t.v2 = mk(c.x, c.y, c.z);
+    return t;
+}
+
+PTD float box_test(float4 lo, float4 hi, f3 nod, f3 rcp, float hit_t) {
+    const float bmin[3] = {lo.x, lo.y, lo.z}, bmax[3] = {hi.x, hi.y, hi.z};
+    return intersect_aabb(bmin, bmax, nod, rcp, hit_t);
+}
+
+// closest-hit traversal (trace.slang:764-884) on the aligned child-pair
+// layout; the deferred stack holds the (left_first, tri_count) of each node
+// so a pop needs no memory access; visit order is the reference's.
+template <bool kRec, bool kAlpha>
+PTD void closest_hit_wf(const World& w, const Fast& f, f3 o, f3 d, Rng<kRec>& rng, Counters* c, float& hit_t,
+                        int32_t& hit, float& hv, float& hw) {
+    Rec<kRec> rec{};
+    if constexpr (kRec) {
+        rec.c = c;
+        c->extend_rays += 1;
+    }
+    const f3 rcp = 1.0f / d;
+    const Shear s = make_shear(d, rcp);
+    const f3 nod = -o * rcp;
+    uint2 stack[64];
+    uint32_t istack[kRec ? 64 : 1];
+    uint32_t idx = 0u, sp = 0u;
+    uint32_t lf = __float_as_uint(__ldg(&f.pairs[0].w)), tc = __float_as_uint(__ldg(&f.pairs[1].w));
+    for (;;) {
+        rec.visit(idx);
+        if (tc > 0u) {
+            rec.leaf();
+            for (uint32_t i = 0; i < tc; ++i) {
+                const uint32_t tri = lf + i;
+                rec.tri();
+                float t, v, wb;
+                if (!triangle_test(load_tri4(f, tri), o, s, &t, &v, &wb)) continue;
+                if (t > 0.0f && t < hit_t) {
+                    if constexpr (kAlpha) {
+                        if (passes_through(w, tri, v, wb, rng)) continue;
+                    }
+                    hit_t = t;
+                    hit = (int32_t)tri;
+                    hv = v;
+                    hw = wb;
+                }
+            }
+        } else {
+            rec.interior();
+            const float4* p = f.pairs + 2 * (size_t)lf;
+            const float4 l0 = __ldg(p), l1 = __ldg(p + 1), r0 = __ldg(p + 2), r1 = __ldg(p + 3);
+            const float dl = box_test(l0, l1, nod, rcp, hit_t);
+            const float dr = box_test(r0, r1, nod, rcp, hit_t);
+            const bool hl = dl >= 0.0f, hr = dr >= 0.0f;
+            if (hl || hr) {
+                const bool go_left = hl && (!hr || dl < dr);
+                const float4 n0 = go_left ? l0 : r0, n1 = go_left ? l1 : r1;
+                if (hl && hr) {
+                    const float4 f0 = go_left ? r0 : l0, f1 = go_left ? r1 : l1;
+                    stack[sp & 63u] = make_uint2(__float_as_uint(f0.w), __float_as_uint(f1.w));
+                    if constexpr (kRec) istack[sp & 63u] = go_left ? lf + 1u : lf;
+                    sp += 1u;
+                }
+                if constexpr (kRec) idx = go_left ? lf : lf + 1u;
+                lf = __float_as_uint(n0.w);
+                tc = __float_as_uint(n1.w);
+                continue;
+            }
+        }
+        if (sp == 0u) break;
+        sp -= 1u;
+        const uint2 e = stack[sp & 63u];
+        lf = e.x;
+        tc = e.y;
+        if constexpr (kRec) idx = istack[sp & 63u];
+    }
+}
+
+// any-hit traversal (trace.slang:614-717) on the same layout, opaque scenes
+template <bool kRec>
+PTD bool occluded_wf(const World& w, const Fast& f, f3 o, f3 d, float hit_t, int32_t light_tri, Counters* c) {
+    Rec<kRec> rec{};
+    if constexpr (kRec) {
+        rec.c = c;
+        c->shadow_rays += 1;
+    }
+    const f3 rcp = 1.0f / d;
+    const Shear s = make_shear(d, rcp);
+    const f3 nod = -o * rcp;
+    uint2 stack[64];
+    uint32_t istack[kRec ? 64 : 1];
+    uint32_t idx = 0u, sp = 0u;
+    uint32_t lf = __float_as_uint(__ldg(&f.pairs[0].w)), tc = __float_as_uint(__ldg(&f.pairs[1].w));
+    for (;;) {
+        rec.visit(idx);
+        if (tc > 0u) {
+            rec.leaf();
+            for (uint32_t i = 0; i < tc; ++i) {
+                const uint32_t tri = lf + i;
+                if ((int32_t)tri == light_tri) continue;
+                rec.tri();
+                float t, v, wb;
+                if (!triangle_test(load_tri4(f, tri), o, s, &t, &v, &wb)) continue;
+                if (t > 0.0f && t < hit_t) return true;
+            }
+        } else {
+            rec.interior();
+            const float4* p = f.pairs + 2 * (size_t)lf;
+            const float4 l0 = __ldg(p), l1 = __ldg(p + 1), r0 = __ldg(p + 2), r1 = __ldg(p + 3);
+            const float dl = box_test(l0, l1, nod, rcp, hit_t);
+            const float dr = box_test(r0, r1, nod, rcp, hit_t);
+            const bool hl = dl >= 0.0f, hr = dr >= 0.0f;
+            if (hl || hr) {
+                const bool go_left = hl && (!hr || dl < dr);
+                const float4 n0 = go_left ? l0 : r0, n1 = go_left ? l1 : r1;
+                if (hl && hr) {
+                    const float4 f0 = go_left ? r0 : l0, f1 = go_left ? r1 : l1;
+                    stack[sp & 63u] = make_uint2(__float_as_uint(f0.w), __float_as_uint(f1.w));
+                    if constexpr (kRec) istack[sp & 63u] = go_left ? lf + 1u : lf;
+                    sp += 1u;
+                }
+                if constexpr (kRec) idx = go_left ? lf : lf + 1u;
+                lf = __float_as_uint(n0.w);
+                tc = __float_as_uint(n1.w);
+                continue;
+            }
+        }
+        if (sp == 0u) break;
+        sp -= 1u;
+        const uint2 e = stack[sp & 63u];
+        lf = e.x;
+        tc = e.y;
+        if constexpr (kRec) idx = istack[sp & 63u];
+    }
+    return false;
+}
+
+PTD unsigned lane_id() {
+    unsigned l;
+    asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
+    return l;
+}
+
+// warp-aggregated append: one atomic per warp, slots in lane order
+PTD uint32_t warp_append(bool want, uint32_t* counter, unsigned mask) {
+    const unsigned ballot = __ballot_sync(mask, want);
+    if (ballot == 0u) return 0xffffffffu;
+    const unsigned lane = lane_id();
+    const unsigned leader = (unsigned)(__ffs(ballot) - 1);
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(ballot));
+    base = __shfl_sync(mask, base, leader);
+    return want ? base + (uint32_t)__popc(ballot & ((1u << lane) - 1u)) : 0xffffffffu;
+}
+
+// per group: paths p = s * P + pixel, P = visible tile pixels
+struct Group {
+    uint32_t vis_w, vis_h;   // visible part of the tile
+    uint32_t pixels;         // vis_w * vis_h
+    uint32_t paths;          // pixels * samples
+    uint32_t first_sample;   // 1-based n of sample 0 of the group
+    uint32_t samples;
+    uint32_t record_sample;  // sample offset of the group within the pt_trace call
+};
+
+template <bool kRec>
+__global__ void __launch_bounds__(256) raygen_kernel(World w, ptk::Tile t, Group g, Queues q) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p == 0) {
+        q.cnt[0] = g.paths;
+        q.cnt[1] = 0u;
+    }
+    if (p >= g.paths) return;
+    const uint32_t s = p / g.pixels, pix = p - s * g.pixels;
+    const uint32_t gy = pix / g.vis_w, gx = pix - gy * g.vis_w;
+    const uint32_t px = gx + t.origin_x, py = gy + t.origin_y;
+    Counters c;
+    if constexpr (kRec) {
+        c.visit_hash = kFnvBasis;
+        c.extend_rays = c.shadow_rays = c.interior_visits = c.leaf_visits = c.triangle_tests = c.rand_draws = 0;
+        c.hits = c.sky_misses = c.light_samples = c.sky_light_samples = 0;
+    }
+    Rng<kRec> rng;
+    rng.s = seed(px, py, g.first_sample + s);
+    if constexpr (kRec) rng.rec.c = &c;
+    PathState ps;
+    camera_ray(w, px, py, t.image_w, t.image_h, rng, ps);
+    q.o[0][p] = make_float4(ps.o.x, ps.o.y, ps.o.z, __uint_as_float(p));
+    q.d[0][p] = make_float4(ps.d.x, ps.d.y, ps.d.z, __uint_as_float(rng.s));
+    q.T[0][p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    q.color[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if constexpr (kRec) {
+        q.rec[p] = c;
+        for (int i = 0; i < PT_RECORD_MAX_BOUNCES; ++i) q.rec_hits[(size_t)p * PT_RECORD_MAX_BOUNCES + i] = -2;
+    }
+}
+
+__global__ void bounce_reset_kernel(uint32_t* cnt, int next) {
+    cnt[next] = 0u;
+    cnt[2] = 0u;
+    cnt[3] = 0u;
+    cnt[4] = 0u;
+}
+
+template <bool kRec, bool kAlpha>
+__global__ void __launch_bounds__(kExtendThreads) extend_kernel(World w, Fast f, Queues q, int cur, uint32_t bounce) {
+    const uint32_t count = q.cnt[cur];
+    const unsigned lane = lane_id();
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&q.cnt[3], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= count) break;
+        const uint32_t i = base + lane;
+        if (i < count) {
+            const float4 o4 = q.o[cur][i];
+            const float4 d4 = q.d[cur][i];
+            const uint32_t p = __float_as_uint(o4.w);
+            Counters c;
+            Rng<kRec> rng;
+            rng.s = __float_as_uint(d4.w);
+            if constexpr (kRec) {
+                c = q.rec[p];
+                rng.rec.c = &c;
+            }
+            float hit_t = kFltMax, hv = 0.0f, hw = 0.0f;
+            int32_t hit = -1;
+            closest_hit_wf<kRec, kAlpha>(w, f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), rng, &c, hit_t, hit, hv, hw);
+            q.hit[i] = make_float4(hit_t, __int_as_float(hit), hv, hw);
+            if constexpr (kAlpha) q.d[cur][i].w = __uint_as_float(rng.s);
+            if constexpr (kRec) {
+                q.rec[p] = c;
+                if (bounce < PT_RECORD_MAX_BOUNCES) q.rec_hits[(size_t)p * PT_RECORD_MAX_BOUNCES + bounce] = hit;
+            }
+        }
+    }
+}
+
+template <bool kRec, bool kAlpha>
+__global__ void __launch_bounds__(kShadeThreads) shade_kernel(World w, Fast f, Queues q, int cur, uint32_t bounce,
+                                                              uint32_t max_bounces) {
+    const uint32_t count = q.cnt[cur];
+    const int next = cur ^ 1;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    const unsigned lane = lane_id();
+    for (uint32_t base = warp * 32u; base < count; base += warps * 32u) {
+        const uint32_t i = base + lane;
+        bool cont = false;
+        ShadowRay sr;
+        sr.valid = false;
+        PathState ps;
+        uint32_t p = 0, rs = 0;
+        if (i < count) {
+            const float4 o4 = q.o[cur][i], d4 = q.d[cur][i], t4 = q.T[cur][i], h4 = q.hit[i];
+            p = __float_as_uint(o4.w);
+            const float4 c4 = q.color[p];
+            ps.o = mk(o4.x, o4.y, o4.z);
+            ps.d = mk(d4.x, d4.y, d4.z);
+            ps.throughput = mk(t4.x, t4.y, t4.z);
+            ps.prev_pdf = t4.w;
+            ps.color = mk(c4.x, c4.y, c4.z);
+            Counters c;
+            Rng<kRec> rng;
+            rng.s = __float_as_uint(d4.w);
+            if constexpr (kRec) {
+                c = q.rec[p];
+                rng.rec.c = &c;
+            }
+            const int32_t hit = __float_as_int(h4.y);
+            if (hit == -1) {
+                if constexpr (kRec) c.sky_misses += 1;
+                shade_miss(w, bounce, ps);
+            } else {
+                if constexpr (kRec) c.hits += 1;
+                cont = shade_hit<kRec, kAlpha>(w, bounce, max_bounces, ps, h4.x, (uint32_t)hit, h4.z, h4.w, rng, &c, &sr);
+            }
+            q.color[p] = make_float4(ps.color.x, ps.color.y, ps.color.z, 0.0f);
+            rs = rng.s;
+            if constexpr (kRec) q.rec[p] = c;
+        }
+        const uint32_t slot = warp_append(cont, &q.cnt[next], 0xffffffffu);
+        if (cont) {
+            q.o[next][slot] = make_float4(ps.o.x, ps.o.y, ps.o.z, __uint_as_float(p));
+            q.d[next][slot] = make_float4(ps.d.x, ps.d.y, ps.d.z, __uint_as_float(rs));
+            q.T[next][slot] = make_float4(ps.throughput.x, ps.throughput.y, ps.throughput.z, ps.prev_pdf);
+        }
+        if constexpr (!kAlpha) {
+            const uint32_t sslot = warp_append(sr.valid, &q.cnt[2], 0xffffffffu);
+            if (sr.valid) {
+                q.so[sslot] = make_float4(sr.o.x, sr.o.y, sr.o.z, __uint_as_float(p));
+                q.sd[sslot] = make_float4(sr.d.x, sr.d.y, sr.d.z, sr.dist);
+                q.sc[sslot] = make_float4(sr.contribution.x, sr.contribution.y, sr.contribution.z, __int_as_float(sr.light_tri));
+            }
+        }
+    }
+}
+
+template <bool kRec>
+__global__ void __launch_bounds__(kExtendThreads) shadow_kernel(World w, Fast f, Queues q) {
+    const uint32_t count = q.cnt[2];
+    const unsigned lane = lane_id();
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&q.cnt[4], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= count) break;
+        const uint32_t i = base + lane;
+        if (i < count) {
+            const float4 o4 = q.so[i], d4 = q.sd[i], c4 = q.sc[i];
+            const uint32_t p = __float_as_uint(o4.w);
+            Counters c;
+            if constexpr (kRec) c = q.rec[p];
+            const bool occ = occluded_wf<kRec>(w, f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), d4.w,
+                                               __float_as_int(c4.w), &c);
+            if (!occ) {
+                const float4 col = q.color[p];
+                const f3 sum = mk(col.x, col.y, col.z) + mk(c4.x, c4.y, c4.z);
+                q.color[p] = make_float4(sum.x, sum.y, sum.z, 0.0f);
+            }
+            if constexpr (kRec) q.rec[p] = c;
+        }
+    }
+}
+
+// accumulate, trace.slang:1299-1308, samples of the group in order
+__global__ void accumulate_kernel(ptk::Tile t, Group g, const float4* color) {
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= g.pixels) return;
+    const uint32_t gy = pix / g.vis_w, gx = pix - gy * g.vis_w;
+    const uint32_t idx = gy * t.tile_w + gx;
+    f3 acc = mk(0.0f, 0.0f, 0.0f);
+    if (g.first_sample > 1u) {
+        const float4 a = t.accum[idx];
+        acc = mk(a.x, a.y, a.z);
+    }
+    uint32_t n = g.first_sample;
+    for (uint32_t s = 0; s < g.samples; ++s, ++n) {
+        const float4 c = color[(size_t)s * g.pixels + pix];
+        acc = (n > 1u ? acc : mk(0.0f, 0.0f, 0.0f)) + mk(c.x, c.y, c.z);
+    }
+    n -= 1u;
+    t.accum[idx] = make_float4(acc.x, acc.y, acc.z, 1.0f);
+    const f3 out = kExposure * acc / (float)n;
+    t.image[idx] = make_float4(out.x, out.y, out.z, 1.0f);
+}
+
+__global__ void finalize_records_kernel(ptk::Tile t, Group g, Queues q, ptk::Sinks sinks) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= g.paths) return;
+    const uint32_t s = p / g.pixels, pix = p - s * g.pixels;
+    const uint32_t gy = pix / g.vis_w, gx = pix - gy * g.vis_w;
+    const Counters c = q.rec[p];
+    const float4 col = q.color[p];
+    if (sinks.records) {
+        pt_path_record* r = sinks.records + (size_t)(g.record_sample + s) * t.tile_w * t.tile_h + gy * t.tile_w + gx;
+        r->visit_hash = c.visit_hash;
+        for (int k = 0; k < PT_RECORD_MAX_BOUNCES; ++k) r->hit[k] = q.rec_hits[(size_t)p * PT_RECORD_MAX_BOUNCES + k];
+        r->extend_rays = c.extend_rays;
+        r->shadow_rays = c.shadow_rays;
+        r->interior_visits = c.interior_visits;
+        r->leaf_visits = c.leaf_visits;
+        r->triangle_tests = c.triangle_tests;
+        r->rand_draws = c.rand_draws;
+        r->hits = c.hits;
+        r->sky_misses = c.sky_misses;
+        r->light_samples = c.light_samples;
+        r->sky_light_samples = c.sky_light_samples;
+        r->radiance[0] = col.x;
+        r->radiance[1] = col.y;
+        r->radiance[2] = col.z;
+    }
+    if (sinks.totals) add_totals(sinks.totals, c);
+}
+
+__global__ void pad_triangles_kernel(const pt_triangle_geometry* geo, uint64_t n, float4* tri4) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* v = geo[i].v0;
+    tri4[3 * i + 0] = make_float4(v[0], v[1], v[2], 0.0f);
+    tri4[3 * i + 1] = make_float4(v[3], v[4], v[5], 0.0f);
+    tri4[3 * i + 2] = make_float4(v[6], v[7], v[8], 0.0f);
+}
+
+}  // namespace ptd
+
+namespace ptw {
+
+namespace {
+
+struct Buf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t reserve(size_t n) {
+        if (n <= bytes && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, n ? n : 16);
+        if (e == cudaSuccess) bytes = n ? n : 16;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+constexpr uint64_t kMaxPaths = 1ull << 25;  // paths in flight per group
+
+#define PTW_TRY(x)                          \
+    do {                                    \
+        const cudaError_t e_ = (x);         \
+        if (e_ != cudaSuccess) return e_;   \
+    } while (0)
+
+}  // namespace
+
+struct Wavefront {
+    Buf o[2], d[2], T[2], hit, color, so, sd, sc, cnt, rec, rec_hits;
+    Buf pairs, tri4;
+    bool stale = true;
+    const void* layout_nodes = nullptr;  // world buffers the layouts were built from
+    const void* layout_geo = nullptr;
+    uint64_t capacity = 0;
+    int sms = 0;
+    int extend_blocks[2][2] = {{0, 0}, {0, 0}};
+    int shade_blocks = 0;
+};
+
+int create(Wavefront** out) {
+    *out = new Wavefront();
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&(*out)->sms, cudaDevAttrMultiProcessorCount, dev);
+    return 0;
+}
+
+void destroy(Wavefront* wf) {
+    if (!wf) return;
+    for (Buf* b : {&wf->o[0], &wf->o[1], &wf->d[0], &wf->d[1], &wf->T[0], &wf->T[1], &wf->hit, &wf->color, &wf->so,
+                   &wf->sd, &wf->sc, &wf->cnt, &wf->rec, &wf->rec_hits, &wf->pairs, &wf->tri4})
+        b->release();
+    delete wf;
+}
+
+void world_changed(Wavefront* wf) {
+    if (wf) wf->stale = true;
+}
+
+namespace {
+
+cudaError_t build_layouts(Wavefront* wf, const ptd::World& w, uint64_t nodes, uint64_t tris, cudaStream_t stream) {
+    PTW_TRY(wf->pairs.reserve((nodes + 1) * 32 + 256));
+    PTW_TRY(cudaMemcpyAsync(static_cast<char*>(wf->pairs.p) + 32, w.nodes, nodes * 32, cudaMemcpyDeviceToDevice, stream));
+    PTW_TRY(wf->tri4.reserve(tris * 48));
+    ptd::pad_triangles_kernel<<<(unsigned)((tris + 255) / 256), 256, 0, stream>>>(w.geo, tris, static_cast<float4*>(wf->tri4.p));
+    PTW_TRY(cudaGetLastError());
+    wf->stale = false;
+    wf->layout_nodes = w.nodes;
+    wf->layout_geo = w.geo;
+    return cudaSuccess;
+}
+
+cudaError_t reserve_paths(Wavefront* wf, uint64_t paths, bool record) {
+    const size_t b = paths * 16;
+    for (Buf* x : {&wf->o[0], &wf->o[1], &wf->d[0], &wf->d[1], &wf->T[0], &wf->T[1], &wf->hit, &wf->color, &wf->so,
+                   &wf->sd, &wf->sc})
+        PTW_TRY(x->reserve(b));
+    PTW_TRY(wf->cnt.reserve(64));
+    if (record) {
+        PTW_TRY(wf->rec.reserve(paths * sizeof(ptd::Counters)));
+        PTW_TRY(wf->rec_hits.reserve(paths * PT_RECORD_MAX_BOUNCES * 4));
+    }
+    wf->capacity = paths;
+    return cudaSuccess;
+}
+
+template <class K>
+int occupancy(K kernel, int threads) {
+    int blocks = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, threads, 0);
+    return blocks > 0 ? blocks : 1;
+}
+
+template <bool kRec, bool kAlpha>
+cudaError_t run_group(Wavefront* wf, const ptd::World& w, const ptd::Fast& f, const ptd::Queues& q,
+                      const ptk::Tile& tile, const ptd::Group& g, ptk::Sinks sinks, cudaStream_t stream,
+                      const Timer& timer) {
+    using namespace ptd;
+    const int ext_blocks = wf->sms * occupancy(extend_kernel<kRec, kAlpha>, kExtendThreads);
+    const int sha_blocks = wf->sms * occupancy(shade_kernel<kRec, kAlpha>, kShadeThreads);
+    const int shd_blocks = wf->sms * occupancy(shadow_kernel<kRec>, kExtendThreads);
+    PTW_TRY(timer(PT_KC_RAYGEN, [&] {
+        raygen_kernel<kRec><<<(g.paths + 255u) / 256u, 256, 0, stream>>>(w, tile, g, q);
+        return cudaGetLastError();
+    }));
+    int cur = 0;
+    for (uint32_t bounce = 0; bounce <= tile.max_bounces; ++bounce) {
+        bounce_reset_kernel<<<1, 1, 0, stream>>>(q.cnt, cur ^ 1);
+        PTW_TRY(cudaGetLastError());
+        PTW_TRY(timer(PT_KC_EXTEND, [&] {
+            extend_kernel<kRec, kAlpha><<<ext_blocks, kExtendThreads, 0, stream>>>(w, f, q, cur, bounce);
+            return cudaGetLastError();
+        }));
+        PTW_TRY(timer(PT_KC_SHADE, [&] {
+            shade_kernel<kRec, kAlpha><<<sha_blocks, kShadeThreads, 0, stream>>>(w, f, q, cur, bounce, tile.max_bounces);
+            return cudaGetLastError();
+        }));
+        if constexpr (!kAlpha) {
+            PTW_TRY(timer(PT_KC_SHADOW, [&] {
+                shadow_kernel<kRec><<<shd_blocks, kExtendThreads, 0, stream>>>(w, f, q);
+                return cudaGetLastError();
+            }));
+        }
+        cur ^= 1;
+    }
+    PTW_TRY(timer(PT_KC_ACCUMULATE, [&] {
+        accumulate_kernel<<<(g.pixels + 255u) / 256u, 256, 0, stream>>>(tile, g, q.color);
+        return cudaGetLastError();
+    }));
+    if constexpr (kRec) {
+        finalize_records_kernel<<<(g.paths + 255u) / 256u, 256, 0, stream>>>(tile, g, q, sinks);
+        PTW_TRY(cudaGetLastError());
+    }
+    return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t trace(Wavefront* wf, const ptd::World& w, const ptk::Tile& tile, uint32_t first, uint32_t samples,
+                  ptk::Sinks sinks, cudaStream_t stream, const Timer& timer) {
+    const uint32_t vis_w = tile.tile_w < tile.image_w - tile.origin_x ? tile.tile_w : tile.image_w - tile.origin_x;
+    const uint32_t vis_h = tile.tile_h < tile.image_h - tile.origin_y ? tile.tile_h : tile.image_h - tile.origin_y;
+    const uint64_t pixels = (uint64_t)vis_w * vis_h;
+    if (pixels == 0 || samples == 0) return cudaSuccess;
+    if (wf->stale || wf->layout_nodes != w.nodes || wf->layout_geo != w.geo) return cudaErrorNotReady;  // prepare() first
+    uint32_t group = (uint32_t)(kMaxPaths / pixels);
+    if (group == 0) group = 1;
+    if (group > samples) group = samples;
+    const uint64_t paths = pixels * group;
+    const bool record = sinks.any();
+    if (paths > wf->capacity || (record && wf->rec.bytes < paths * sizeof(ptd::Counters)))
+        PTW_TRY(reserve_paths(wf, paths > wf->capacity ? paths : wf->capacity, record));
+    ptd::Queues q;
+    for (int k = 0; k < 2; ++k) {
+        q.o[k] = static_cast<float4*>(wf->o[k].p);
+        q.d[k] = static_cast<float4*>(wf->d[k].p);
+        q.T[k] = static_cast<float4*>(wf->T[k].p);
+    }
+    q.hit = static_cast<float4*>(wf->hit.p);
+    q.color = static_cast<float4*>(wf->color.p);
+    q.so = static_cast<float4*>(wf->so.p);
+    q.sd = static_cast<float4*>(wf->sd.p);
+    q.sc = static_cast<float4*>(wf->sc.p);
+    q.cnt = static_cast<uint32_t*>(wf->cnt.p);
+    q.rec = static_cast<ptd::Counters*>(wf->rec.p);
+    q.rec_hits = static_cast<int32_t*>(wf->rec_hits.p);
+    ptd::Fast f;
+    f.pairs = reinterpret_cast<const float4*>(static_cast<const char*>(wf->pairs.p) + 32);
+    f.tri4 = static_cast<const float4*>(wf->tri4.p);
+    for (uint32_t s0 = 0; s0 < samples; s0 += group) {
+        ptd::Group g;
+        g.vis_w = vis_w;
+        g.vis_h = vis_h;
+        g.pixels = (uint32_t)pixels;
+        g.samples = samples - s0 < group ? samples - s0 : group;
+        g.paths = (uint32_t)(pixels * g.samples);
+        g.first_sample = first + s0;
+        g.record_sample = s0;
+        cudaError_t e;
+        if (record)
+            e = w.any_alpha ? run_group<true, true>(wf, w, f, q, tile, g, sinks, stream, timer)
+                            : run_group<true, false>(wf, w, f, q, tile, g, sinks, stream, timer);
+        else
+            e = w.any_alpha ? run_group<false, true>(wf, w, f, q, tile, g, sinks, stream, timer)
+                            : run_group<false, false>(wf, w, f, q, tile, g, sinks, stream, timer);
+        PTW_TRY(e);
+    }
+    return cudaSuccess;
+}
+
+cudaError_t prepare(Wavefront* wf, const ptd::World& w, uint64_t nodes, uint64_t tris, cudaStream_t stream) {
+    if (!wf->stale && wf->layout_nodes == w.nodes && wf->layout_geo == w.geo) return cudaSuccess;
+    return build_layouts(wf, w, nodes, tris, stream);
+}
+
+}  // namespace ptw
