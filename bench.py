@@ -35,6 +35,9 @@ import numpy as np  # noqa: E402
 WIDTH, HEIGHT, SPP, MAX_BOUNCES = 1920, 1080, 64, 8
 METRIC = "Mrays/s"
 KERNEL_NAMES = {"wavefront": 0, "plain": 1}
+# DRAM bytes (read + write) per launch of the dominant kernel for this
+# workload, from the ncu capture summarised in profiles/ (None until captured)
+TRAFFIC_PER_LAUNCH: dict = {}
 
 
 def parse_args():
@@ -79,17 +82,22 @@ def build_world():
     return world, world.take_updates()
 
 
-def algorithmic_bytes(t: dict, emissive: int, paths: int) -> int:
-    """Bytes a ray batch must read or write at least once (roofline numerator):
-    per ray 32 (root) + 64 per interior node (both children) + 36 per
-    triangle test; per hit 112 attribute + 224 material + 36 hit triangle;
-    per triangle-light sample 16 * (2 + ceil(log2 E)) alias entries; per sky
-    sample 2 * 12; per escaped ray 64 (bilinear sky); per path 48
+def algorithmic_bytes(t: dict, emissive: int, paths: int) -> dict:
+    """Bytes the work must read or write at least once (roofline numerator), per kernel class:
+    every traversal 32 (root) + 64 per interior node (both children) + 36 per
+    triangle test; every hit 112 attribute + 224 material + 36 hit triangle;
+    every triangle-light sample 16 * (2 + ceil(log2 E)) alias entries; every
+    sky sample 2 * 12; every escaped ray 64 (bilinear sky); every path 48
     (accumulation read + write, storage texture write)."""
-    rays = t["extend_rays"] + t["shadow_rays"]
     alias = 16 * (2 + math.ceil(math.log2(max(emissive, 1))))
-    return int(32 * rays + 64 * t["interior_visits"] + 36 * t["triangle_tests"] + 372 * t["hits"]
-               + alias * t["light_samples"] + 24 * t["sky_light_samples"] + 64 * t["sky_misses"] + 48 * paths)
+    extend = (32 * t["extend_rays"] + 64 * (t["interior_visits"] - t["shadow_interior_visits"])
+              + 36 * (t["triangle_tests"] - t["shadow_triangle_tests"]))
+    shadow = 32 * t["shadow_rays"] + 64 * t["shadow_interior_visits"] + 36 * t["shadow_triangle_tests"]
+    shade = 372 * t["hits"] + alias * t["light_samples"] + 24 * t["sky_light_samples"] + 64 * t["sky_misses"]
+    accumulate = 48 * paths
+    total = extend + shadow + shade + accumulate
+    return {"extend": extend, "shadow": shadow, "shade": shade, "accumulate": accumulate, "raygen": 0,
+            "plain": total, "total": total}
 
 
 class ClockSampler:
@@ -320,14 +328,14 @@ def run_ours(args):
     cls_launches = max(1, times.launches[cls])
     avg_launch_s = times.milliseconds[cls] / cls_launches / 1e3
     launches_per_step = cls_launches / args.steps
-    bytes_per_launch = bytes_per_step / launches_per_step
+    bytes_per_launch = bytes_per_step[cls] / launches_per_step
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = bytes_per_launch / avg_launch_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": cls, "bytes_per_launch": bytes_per_launch,
-                "avg_launch_ms": avg_launch_s * 1e3,
-                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback 6.8 TB/s"}
+                "traffic": TRAFFIC_PER_LAUNCH.get((args.kernel, cls)), "kernel": cls,
+                "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs), of measured" if peaks else "fallback 6.8 TB/s"}
 
     # end to end through the C ABI: world upload from pinned host memory, the
     # render, and the RGBA8 result read back, every step

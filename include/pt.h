@@ -294,29 +294,36 @@ typedef struct pt_path_record {
     int32_t hit[PT_RECORD_MAX_BOUNCES]; /* closest-hit triangle per bounce; -1 miss; -2 not reached */
     uint32_t extend_rays;
     uint32_t shadow_rays;
-    uint32_t interior_visits;           /* interior nodes fetched (each tests 2 children) */
+    uint32_t interior_visits;           /* interior nodes fetched (each tests 2 children), all traversals */
     uint32_t leaf_visits;
     uint32_t triangle_tests;
+    uint32_t shadow_interior_visits;    /* the part of the three counters above spent in shadow rays */
+    uint32_t shadow_leaf_visits;
+    uint32_t shadow_triangle_tests;
     uint32_t rand_draws;
     uint32_t hits;                      /* extend rays that hit a triangle */
     uint32_t sky_misses;                /* extend rays that escaped */
     uint32_t light_samples;             /* sample_light calls that drew a triangle light */
     uint32_t sky_light_samples;         /* sample_light calls that drew the skybox */
     float radiance[3];                  /* final_color of this sample */
-} pt_path_record;                       /* 128 B */
+    uint32_t pad;
+} pt_path_record;                       /* 144 B */
 
 /* totals over every path of a pt_trace_counted call, in this order */
-#define PT_COUNT_FIELDS 10
+#define PT_COUNT_FIELDS 13
 #define PT_COUNT_EXTEND_RAYS 0
 #define PT_COUNT_SHADOW_RAYS 1
 #define PT_COUNT_INTERIOR_VISITS 2
 #define PT_COUNT_LEAF_VISITS 3
 #define PT_COUNT_TRIANGLE_TESTS 4
-#define PT_COUNT_RAND_DRAWS 5
-#define PT_COUNT_HITS 6
-#define PT_COUNT_SKY_MISSES 7
-#define PT_COUNT_LIGHT_SAMPLES 8
-#define PT_COUNT_SKY_LIGHT_SAMPLES 9
+#define PT_COUNT_SHADOW_INTERIOR_VISITS 5
+#define PT_COUNT_SHADOW_LEAF_VISITS 6
+#define PT_COUNT_SHADOW_TRIANGLE_TESTS 7
+#define PT_COUNT_RAND_DRAWS 8
+#define PT_COUNT_HITS 9
+#define PT_COUNT_SKY_MISSES 10
+#define PT_COUNT_LIGHT_SAMPLES 11
+#define PT_COUNT_SKY_LIGHT_SAMPLES 12
 /* Like pt_trace, with the counting kernel variants: adds the pt_path_record
  * counters of every traced path into totals[PT_COUNT_FIELDS] (not cleared). */
 int pt_trace_counted(pt_ctx* ctx, uint32_t sample_count, uint32_t* traced, uint64_t totals[PT_COUNT_FIELDS]);

@@ -67,6 +67,10 @@ int ptw_build(ptw_world* world);
  * 1x1 skybox.  Without a call the skybox is black. */
 int ptw_set_skybox_rgba(ptw_world* world, const float* rgba, uint32_t width, uint32_t height);
 
+/* the procedural sky of the large scene (vertical gradient plus a Gaussian
+ * sun lobe), width x height, passed through ptw_set_skybox_rgba */
+int ptw_set_procedural_skybox(ptw_world* world, uint32_t width, uint32_t height);
+
 /* World::edit_skybox_average_luminance (world.rs:646-648): clamped at 0 */
 int ptw_edit_skybox_average_luminance(ptw_world* world, float luminance);
 

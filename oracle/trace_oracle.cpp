@@ -136,6 +136,7 @@ struct Tracer {
     const oracle_world& w;
     uint32_t rng = 0;
     pt_path_record* rec = nullptr;
+    bool in_shadow = false;  // counting inside occluded()
 
     explicit Tracer(const oracle_world& world) : w(world) {}
 
@@ -469,7 +470,10 @@ struct Tracer {
 
     // watertight ray-triangle test, trace.slang:807-834; returns false when rejected
     bool triangle_test(uint32_t tri, V3<T> o, const Shear& s, T* t_out, T* v_out, T* w_out) {
-        if (rec) rec->triangle_tests += 1;
+        if (rec) {
+            rec->triangle_tests += 1;
+            if (in_shadow) rec->shadow_triangle_tests += 1;
+        }
         const V3<T> A = vert(tri, 0) - o, B = vert(tri, 1) - o, C = vert(tri, 2) - o;
         const T ax = M<T>::fma(s.sx, A[s.kz], A[s.kx]);
         const T ay = M<T>::fma(s.sy, A[s.kz], A[s.ky]);
@@ -501,7 +505,10 @@ struct Tracer {
         for (;;) {
             const pt_bvh_node& n = node(node_index);
             if (n.tri_count > 0u) {
-                if (rec) rec->leaf_visits += 1;
+                if (rec) {
+                    rec->leaf_visits += 1;
+                    if (in_shadow) rec->shadow_leaf_visits += 1;
+                }
                 for (uint32_t i = 0; i < n.tri_count; ++i) {
                     const uint32_t tri = n.left_first + i;
                     T t, v, wb;
@@ -515,7 +522,10 @@ struct Tracer {
                     }
                 }
             } else {
-                if (rec) rec->interior_visits += 1;
+                if (rec) {
+                    rec->interior_visits += 1;
+                    if (in_shadow) rec->shadow_interior_visits += 1;
+                }
                 const uint32_t li = n.left_first, ri = n.left_first + 1u;
                 const T dl = intersect_aabb(w.bvh_nodes[li], nod, rcp, *hit_t);
                 const T dr = intersect_aabb(w.bvh_nodes[ri], nod, rcp, *hit_t);
@@ -541,6 +551,13 @@ struct Tracer {
 
     // occluded, trace.slang:614-717
     bool occluded(V3<T> o, V3<T> d, T hit_t, int32_t light_tri) {
+        in_shadow = true;
+        const bool r = occluded_impl(o, d, hit_t, light_tri);
+        in_shadow = false;
+        return r;
+    }
+
+    bool occluded_impl(V3<T> o, V3<T> d, T hit_t, int32_t light_tri) {
         if (rec) rec->shadow_rays += 1;
         const V3<T> rcp = T(1) / d;
         const Shear s = shear(d, rcp);
@@ -550,7 +567,10 @@ struct Tracer {
         for (;;) {
             const pt_bvh_node& n = node(node_index);
             if (n.tri_count > 0u) {
-                if (rec) rec->leaf_visits += 1;
+                if (rec) {
+                    rec->leaf_visits += 1;
+                    if (in_shadow) rec->shadow_leaf_visits += 1;
+                }
                 for (uint32_t i = 0; i < n.tri_count; ++i) {
                     const uint32_t tri = n.left_first + i;
                     if ((int32_t)tri == light_tri) continue;
@@ -559,7 +579,10 @@ struct Tracer {
                     if (t > T(0) && t < hit_t && !passes_through(tri, v, wb)) return true;
                 }
             } else {
-                if (rec) rec->interior_visits += 1;
+                if (rec) {
+                    rec->interior_visits += 1;
+                    if (in_shadow) rec->shadow_interior_visits += 1;
+                }
                 const uint32_t li = n.left_first, ri = n.left_first + 1u;
                 const T dl = intersect_aabb(w.bvh_nodes[li], nod, rcp, hit_t);
                 const T dr = intersect_aabb(w.bvh_nodes[ri], nod, rcp, hit_t);

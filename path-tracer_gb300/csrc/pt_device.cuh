@@ -104,7 +104,8 @@ struct World {
 // per-path instrumentation (pt_path_record) kept in registers while tracing
 struct Counters {
     uint64_t visit_hash;
-    uint32_t extend_rays, shadow_rays, interior_visits, leaf_visits, triangle_tests, rand_draws;
+    uint32_t extend_rays, shadow_rays, interior_visits, leaf_visits, triangle_tests;
+    uint32_t shadow_interior_visits, shadow_leaf_visits, shadow_triangle_tests, rand_draws;
     uint32_t hits, sky_misses, light_samples, sky_light_samples;
 };
 
@@ -112,7 +113,8 @@ struct Counters {
 // __reduce_add_sync sums over exactly the lanes in the active mask)
 PTD void add_totals(unsigned long long* totals, const Counters& c) {
     const uint32_t v[PT_COUNT_FIELDS] = {c.extend_rays, c.shadow_rays, c.interior_visits, c.leaf_visits,
-                                         c.triangle_tests, c.rand_draws, c.hits, c.sky_misses,
+                                         c.triangle_tests, c.shadow_interior_visits, c.shadow_leaf_visits,
+                                         c.shadow_triangle_tests, c.rand_draws, c.hits, c.sky_misses,
                                          c.light_samples, c.sky_light_samples};
     const unsigned mask = __activemask();
     unsigned lane;
@@ -136,10 +138,20 @@ struct Rec {
 template <>
 struct Rec<true> {
     Counters* c;
+    bool shadow = false;  // counting inside an any-hit (shadow) traversal
     PTD void visit(uint32_t i) { c->visit_hash = (c->visit_hash ^ i) * kFnvPrime; }
-    PTD void interior() { c->interior_visits += 1; }
-    PTD void leaf() { c->leaf_visits += 1; }
-    PTD void tri() { c->triangle_tests += 1; }
+    PTD void interior() {
+        c->interior_visits += 1;
+        if (shadow) c->shadow_interior_visits += 1;
+    }
+    PTD void leaf() {
+        c->leaf_visits += 1;
+        if (shadow) c->shadow_leaf_visits += 1;
+    }
+    PTD void tri() {
+        c->triangle_tests += 1;
+        if (shadow) c->shadow_triangle_tests += 1;
+    }
     PTD void draw() { c->rand_draws += 1; }
 };
 

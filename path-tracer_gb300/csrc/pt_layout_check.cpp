@@ -39,6 +39,6 @@ CHECK_SIZE(pt_scene_alias_entry, 16);
 CHECK_SIZE(pt_skybox_uniforms, 16);
 CHECK_SIZE(pt_skybox_alias_entry, 12);
 CHECK_SIZE(pt_trace_parameters, 32);
-CHECK_SIZE(pt_path_record, 128);
+CHECK_SIZE(pt_path_record, 144);
 
 extern "C" int pt_layout_checked(void) { return 1; }

@@ -95,6 +95,7 @@ PTD bool occluded(const World& w, f3 o, f3 d, float hit_t, int32_t light_tri, Rn
     Rec<kRec> rec{};
     if constexpr (kRec) {
         rec.c = c;
+        rec.shadow = true;
         c->shadow_rays += 1;
     }
     const f3 rcp = 1.0f / d;

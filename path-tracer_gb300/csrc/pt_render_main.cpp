@@ -1,0 +1,416 @@
+// pt_render_main.cpp - `pt-render render ...`: the reference's headless
+// renderer (src/render/headless.rs) on top of the C ABI.
+//
+// Flags, defaults and validation follow RenderOptions (headless.rs:15-127);
+// the world is loaded, the skybox luminance and camera overrides applied
+// (headless.rs:180-204), the image traced tile by tile in row-major order with
+// at most 16 samples per trace call (headless.rs:207-285), each finished tile
+// tone mapped (display.wgsl) and the RGB8 image saved.
+//
+// Scenes: "cornell" (36-triangle Cornell box) or "procedural[:SEED]" (the
+// ~2.1M-triangle procedural scene); glTF files are not read by this build.
+// Skyboxes: "black", "procedural" (gradient + sun) or a Radiance .hdr file.
+// Output: .png (or .ppm); JPEG and WebP encoders are not part of this build.
+#include <algorithm>
+#include <cerrno>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pt.h"
+#include "../../include/pt_world.h"
+
+namespace {
+
+struct Options {
+    std::string scene = "cornell";
+    std::string skybox = "black";
+    float skybox_luminance = PTW_DEFAULT_SKYBOX_LUMINANCE;
+    std::string output = "render.png";
+    uint32_t width = 1920, height = 1080, samples = 256, max_bounces = PT_DEFAULT_MAX_BOUNCES, tile_size = 512;
+    bool has_position = false, has_yaw = false, has_pitch = false, has_fov = false;
+    float position[3] = {0, 0, 0};
+    float yaw = 0, pitch = 0, fov = 0;
+    int device = 0;
+};
+
+[[noreturn]] void usage_error(const std::string& msg) {
+    fprintf(stderr, "error: %s\n\nusage: pt-render render [--scene S] [--skybox S] [--skybox-luminance NITS]\n"
+                    "  [--output FILE.png] [--width N] [--height N] [--samples N] [--max-bounces 0..16]\n"
+                    "  [--tile-size N] [--camera-position X,Y,Z] [--camera-yaw DEG] [--camera-pitch DEG]\n"
+                    "  [--camera-fov DEG] [--device N]\n",
+            msg.c_str());
+    exit(2);
+}
+
+// parse_finite, headless.rs:67-74
+float parse_finite(const std::string& flag, const char* s) {
+    char* end = nullptr;
+    errno = 0;
+    const float v = strtof(s, &end);
+    if (end == s || *end != '\0' || errno == ERANGE) usage_error("invalid value for " + flag + ": " + s);
+    if (!std::isfinite(v)) usage_error("invalid value for " + flag + ": must be finite");
+    return v;
+}
+
+uint32_t parse_u32(const std::string& flag, const char* s, uint32_t lo, uint32_t hi) {
+    char* end = nullptr;
+    errno = 0;
+    const unsigned long long v = strtoull(s, &end, 10);
+    if (end == s || *end != '\0' || errno == ERANGE || s[0] == '-' || v < lo || v > hi)
+        usage_error("invalid value for " + flag + ": " + s + " (range " + std::to_string(lo) + ".." + std::to_string(hi) + ")");
+    return (uint32_t)v;
+}
+
+Options parse(int argc, char** argv) {
+    Options o;
+    if (argc < 2 || std::string(argv[1]) != "render") usage_error("expected the `render` command");
+    for (int i = 2; i < argc; ++i) {
+        const std::string f = argv[i];
+        if (i + 1 >= argc) usage_error("missing value for " + f);
+        const char* v = argv[++i];
+        if (f == "--scene") o.scene = v;
+        else if (f == "--skybox") o.skybox = v;
+        else if (f == "--skybox-luminance") {
+            o.skybox_luminance = parse_finite(f, v);
+            if (o.skybox_luminance < 0) usage_error("--skybox-luminance must be nonnegative");
+        } else if (f == "--output") {
+            o.output = v;
+            const auto dot = o.output.rfind('.');
+            const std::string ext = dot == std::string::npos ? "" : o.output.substr(dot + 1);
+            if (ext != "png" && ext != "ppm")
+                usage_error("--output must have a .png extension (.ppm also accepted; JPEG/WebP encoders are not built)");
+        } else if (f == "--width") o.width = parse_u32(f, v, 1, 0xffffffffu);
+        else if (f == "--height") o.height = parse_u32(f, v, 1, 0xffffffffu);
+        else if (f == "--samples") o.samples = parse_u32(f, v, 1, 0xffffffffu);
+        else if (f == "--max-bounces") o.max_bounces = parse_u32(f, v, 0, PT_MAX_BOUNCES_LIMIT);
+        else if (f == "--tile-size") o.tile_size = parse_u32(f, v, 1, 0xffffffffu);
+        else if (f == "--camera-position") {
+            // parse_position, headless.rs:107-116
+            std::string s = v;
+            std::vector<std::string> parts;
+            size_t start = 0;
+            for (size_t k = 0; k <= s.size(); ++k)
+                if (k == s.size() || s[k] == ',') {
+                    std::string p = s.substr(start, k - start);
+                    while (!p.empty() && p.front() == ' ') p.erase(p.begin());
+                    while (!p.empty() && p.back() == ' ') p.pop_back();
+                    parts.push_back(p);
+                    start = k + 1;
+                }
+            if (parts.size() != 3) usage_error("--camera-position must be three comma-separated coordinates");
+            for (int k = 0; k < 3; ++k) o.position[k] = parse_finite(f, parts[k].c_str());
+            o.has_position = true;
+        } else if (f == "--camera-yaw") {
+            o.yaw = parse_finite(f, v);
+            o.has_yaw = true;
+        } else if (f == "--camera-pitch") {
+            o.pitch = parse_finite(f, v);
+            if (o.pitch < -90.0f || o.pitch > 90.0f) usage_error("--camera-pitch must be from -90 to 90");
+            o.has_pitch = true;
+        } else if (f == "--camera-fov") {
+            o.fov = parse_finite(f, v);
+            if (!(o.fov > 0.0f && o.fov < 180.0f)) usage_error("--camera-fov must be strictly between 0 and 180");
+            o.has_fov = true;
+        } else if (f == "--device") o.device = (int)parse_u32(f, v, 0, 1024);
+        else usage_error("unknown flag " + f);
+    }
+    return o;
+}
+
+// Radiance RGBE (.hdr) reader: "#?RADIANCE"/"#?RGBE" header, FORMAT=32-bit_rle_rgbe,
+// "-Y H +X W" resolution, new-style run-length scanlines or flat pixels.
+bool read_hdr(const std::string& path, std::vector<float>& rgba, uint32_t& w, uint32_t& h, std::string& err) {
+    FILE* f = fopen(path.c_str(), "rb");
+    if (!f) {
+        err = "cannot read skybox " + path + ": " + strerror(errno);
+        return false;
+    }
+    std::vector<uint8_t> data;
+    uint8_t buf[1 << 16];
+    size_t n;
+    while ((n = fread(buf, 1, sizeof buf, f)) > 0) data.insert(data.end(), buf, buf + n);
+    fclose(f);
+    size_t pos = 0;
+    auto line = [&]() {
+        std::string s;
+        while (pos < data.size() && data[pos] != '\n') s.push_back((char)data[pos++]);
+        if (pos < data.size()) pos++;
+        return s;
+    };
+    const std::string magic = line();
+    if (magic.rfind("#?", 0) != 0) {
+        err = "not a Radiance HDR file";
+        return false;
+    }
+    for (;;) {
+        if (pos >= data.size()) {
+            err = "truncated HDR header";
+            return false;
+        }
+        const std::string s = line();
+        if (s.empty()) break;
+        if (s.rfind("FORMAT=", 0) == 0 && s != "FORMAT=32-bit_rle_rgbe") {
+            err = "unsupported HDR format " + s;
+            return false;
+        }
+    }
+    const std::string res = line();
+    int hh = 0, ww = 0;
+    if (sscanf(res.c_str(), "-Y %d +X %d", &hh, &ww) != 2 || hh <= 0 || ww <= 0) {
+        err = "unsupported HDR orientation: " + res;
+        return false;
+    }
+    w = (uint32_t)ww;
+    h = (uint32_t)hh;
+    rgba.assign((size_t)w * h * 4, 0.0f);
+    std::vector<uint8_t> scan((size_t)w * 4);
+    for (uint32_t y = 0; y < h; ++y) {
+        if (pos + 4 > data.size()) {
+            err = "truncated HDR data";
+            return false;
+        }
+        if (w >= 8 && w < 32768 && data[pos] == 2 && data[pos + 1] == 2 && !(data[pos + 2] & 0x80)) {
+            if ((uint32_t)((data[pos + 2] << 8) | data[pos + 3]) != w) {
+                err = "bad HDR scanline";
+                return false;
+            }
+            pos += 4;
+            for (int c = 0; c < 4; ++c) {
+                uint32_t x = 0;
+                while (x < w) {
+                    if (pos >= data.size()) {
+                        err = "truncated HDR data";
+                        return false;
+                    }
+                    uint32_t count = data[pos++];
+                    if (count > 128) {
+                        count -= 128;
+                        if (pos >= data.size() || x + count > w) {
+                            err = "bad HDR run";
+                            return false;
+                        }
+                        const uint8_t v = data[pos++];
+                        for (uint32_t k = 0; k < count; ++k) scan[(x++) * 4 + c] = v;
+                    } else {
+                        if (count == 0 || pos + count > data.size() || x + count > w) {
+                            err = "bad HDR run";
+                            return false;
+                        }
+                        for (uint32_t k = 0; k < count; ++k) scan[(x++) * 4 + c] = data[pos++];
+                    }
+                }
+            }
+        } else {
+            if (pos + (size_t)w * 4 > data.size()) {
+                err = "truncated HDR data";
+                return false;
+            }
+            memcpy(scan.data(), &data[pos], (size_t)w * 4);
+            pos += (size_t)w * 4;
+        }
+        for (uint32_t x = 0; x < w; ++x) {
+            const uint8_t* p = &scan[x * 4];
+            float* o = &rgba[((size_t)y * w + x) * 4];
+            if (p[3] == 0) {
+                o[0] = o[1] = o[2] = 0.0f;
+            } else {
+                const float scale = std::ldexp(1.0f, (int)p[3] - 136);
+                o[0] = (float)p[0] * scale;
+                o[1] = (float)p[1] * scale;
+                o[2] = (float)p[2] * scale;
+            }
+            o[3] = 1.0f;
+        }
+    }
+    return true;
+}
+
+uint32_t crc32(const uint8_t* d, size_t n, uint32_t c = 0xffffffffu) {
+    static uint32_t table[256];
+    static bool init = false;
+    if (!init) {
+        for (uint32_t i = 0; i < 256; ++i) {
+            uint32_t x = i;
+            for (int k = 0; k < 8; ++k) x = (x & 1) ? 0xedb88320u ^ (x >> 1) : x >> 1;
+            table[i] = x;
+        }
+        init = true;
+    }
+    for (size_t i = 0; i < n; ++i) c = table[(c ^ d[i]) & 0xff] ^ (c >> 8);
+    return c;
+}
+
+// PNG with an uncompressed (stored-block) zlib stream
+bool write_png(const std::string& path, const std::vector<uint8_t>& rgb, uint32_t w, uint32_t h, std::string& err) {
+    std::vector<uint8_t> raw;
+    raw.reserve((size_t)h * (w * 3 + 1));
+    for (uint32_t y = 0; y < h; ++y) {
+        raw.push_back(0);
+        raw.insert(raw.end(), rgb.begin() + (size_t)y * w * 3, rgb.begin() + (size_t)(y + 1) * w * 3);
+    }
+    std::vector<uint8_t> z = {0x78, 0x01};
+    uint32_t a = 1, b = 0;
+    for (uint8_t v : raw) {
+        a = (a + v) % 65521;
+        b = (b + a) % 65521;
+    }
+    for (size_t off = 0; off < raw.size() || off == 0; off += 65535) {
+        const size_t len = std::min<size_t>(65535, raw.size() - off);
+        z.push_back(off + len >= raw.size() ? 1 : 0);
+        z.push_back(len & 0xff);
+        z.push_back(len >> 8);
+        z.push_back(~len & 0xff);
+        z.push_back((~len >> 8) & 0xff);
+        z.insert(z.end(), raw.begin() + off, raw.begin() + off + len);
+        if (raw.empty()) break;
+    }
+    const uint32_t adler = (b << 16) | a;
+    for (int s = 24; s >= 0; s -= 8) z.push_back((adler >> s) & 0xff);
+    FILE* f = fopen(path.c_str(), "wb");
+    if (!f) {
+        err = "cannot save " + path + ": " + strerror(errno);
+        return false;
+    }
+    const uint8_t sig[8] = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1a, '\n'};
+    fwrite(sig, 1, 8, f);
+    auto chunk = [&](const char* type, const std::vector<uint8_t>& d) {
+        uint8_t len[4] = {(uint8_t)(d.size() >> 24), (uint8_t)(d.size() >> 16), (uint8_t)(d.size() >> 8), (uint8_t)d.size()};
+        fwrite(len, 1, 4, f);
+        std::vector<uint8_t> td(type, type + 4);
+        td.insert(td.end(), d.begin(), d.end());
+        fwrite(td.data(), 1, td.size(), f);
+        const uint32_t c = crc32(td.data(), td.size()) ^ 0xffffffffu;
+        uint8_t cb[4] = {(uint8_t)(c >> 24), (uint8_t)(c >> 16), (uint8_t)(c >> 8), (uint8_t)c};
+        fwrite(cb, 1, 4, f);
+    };
+    std::vector<uint8_t> ihdr = {(uint8_t)(w >> 24), (uint8_t)(w >> 16), (uint8_t)(w >> 8), (uint8_t)w,
+                                 (uint8_t)(h >> 24), (uint8_t)(h >> 16), (uint8_t)(h >> 8), (uint8_t)h,
+                                 8, 2, 0, 0, 0};
+    chunk("IHDR", ihdr);
+    chunk("IDAT", z);
+    chunk("IEND", {});
+    const bool ok = ferror(f) == 0;
+    fclose(f);
+    if (!ok) err = "cannot save " + path;
+    return ok;
+}
+
+bool write_ppm(const std::string& path, const std::vector<uint8_t>& rgb, uint32_t w, uint32_t h, std::string& err) {
+    FILE* f = fopen(path.c_str(), "wb");
+    if (!f) {
+        err = "cannot save " + path + ": " + strerror(errno);
+        return false;
+    }
+    fprintf(f, "P6\n%u %u\n255\n", w, h);
+    fwrite(rgb.data(), 1, rgb.size(), f);
+    fclose(f);
+    return true;
+}
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+int fail(const char* what, const std::string& msg) {
+    fprintf(stderr, "error: %s: %s\n", what, msg.c_str());
+    return 1;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    const Options opt = parse(argc, argv);
+    const double started = now_s();
+    fprintf(stderr, "Rendering %s\n", opt.scene.c_str());
+
+    // load_world, headless.rs:180-204
+    ptw_world* world = nullptr;
+    int rc;
+    if (opt.scene == "cornell") {
+        rc = ptw_scene_cornell_box(&world);
+    } else if (opt.scene.rfind("procedural", 0) == 0) {
+        ptw_procedural_params p;
+        ptw_procedural_defaults(&p);
+        if (opt.scene.size() > 11 && opt.scene[10] == ':') p.seed = strtoull(opt.scene.c_str() + 11, nullptr, 10);
+        p.skybox_width = p.skybox_height = 0;  // the --skybox flag decides the sky
+        rc = ptw_scene_procedural(&p, &world);
+    } else {
+        return fail("scene", "cannot read scene " + opt.scene + ": only the built-in scenes `cornell` and `procedural[:SEED]` are available");
+    }
+    if (rc) return fail("scene", "scene construction failed");
+    if (opt.skybox == "procedural") {
+        rc = ptw_set_procedural_skybox(world, 1024, 512);
+    } else if (opt.skybox != "black") {
+        std::vector<float> px;
+        uint32_t w = 0, h = 0;
+        std::string err;
+        if (!read_hdr(opt.skybox, px, w, h, err)) return fail("skybox", err);
+        if (w / 2 != h) fprintf(stderr, "Skybox image should usually have 2:1 aspect ratio, but is %ux%u\n", w, h);
+        rc = ptw_set_skybox_rgba(world, px.data(), w, h);
+    }
+    if (rc) return fail("skybox", ptw_last_error(world));
+    ptw_set_aspect_ratio(world, (float)opt.width / (float)opt.height);
+    ptw_edit_skybox_average_luminance(world, opt.skybox_luminance);
+    const float deg = 3.14159265358979323846f / 180.0f;
+    const float yaw = opt.yaw * deg, pitch = opt.pitch * deg, fov = opt.fov * deg;
+    if (opt.has_position || opt.has_yaw || opt.has_pitch || opt.has_fov)
+        ptw_edit_camera(world, opt.has_position ? opt.position : nullptr, opt.has_yaw ? &yaw : nullptr,
+                        opt.has_pitch ? &pitch : nullptr, opt.has_fov ? &fov : nullptr);
+    pt_world_updates updates;
+    if ((rc = ptw_take_updates(world, &updates))) return fail("world", ptw_last_error(world));
+
+    const uint32_t tile[2] = {std::min(opt.tile_size, opt.width), std::min(opt.tile_size, opt.height)};
+    pt_ctx* ctx = nullptr;
+    if ((rc = pt_create(opt.device, &updates, tile[0], tile[1], &ctx))) return fail("path tracer", "pt_create failed");
+    pt_set_max_bounces(ctx, opt.max_bounces);
+    ptw_destroy(world);  // the GPU has its own copy of the world
+
+    // render_tiles, headless.rs:207-285
+    const uint32_t image[2] = {opt.width, opt.height};
+    std::vector<uint8_t> rgb((size_t)opt.width * opt.height * 3, 0);
+    std::vector<uint8_t> rgba((size_t)tile[0] * tile[1] * 4);
+    const double t0 = now_s();
+    double last_log = t0;
+    const double total = (double)opt.width * opt.height * opt.samples;
+    double traced_samples = 0;
+    for (uint32_t y = 0; y < opt.height; y += tile[1]) {
+        for (uint32_t x = 0; x < opt.width; x += tile[0]) {
+            const uint32_t origin[2] = {x, y};
+            const uint32_t vis[2] = {std::min(tile[0], opt.width - x), std::min(tile[1], opt.height - y)};
+            if ((rc = pt_set_tile(ctx, image, origin, tile))) return fail("set_tile", pt_last_error(ctx));
+            uint32_t remaining = opt.samples;
+            while (remaining > 0) {
+                uint32_t traced = 0;
+                if ((rc = pt_trace(ctx, remaining, &traced))) return fail("trace", pt_last_error(ctx));
+                if ((rc = pt_synchronize(ctx, 0))) return fail("trace", pt_last_error(ctx));
+                remaining -= traced;
+                traced_samples += (double)vis[0] * vis[1] * traced;
+                if (now_s() - last_log >= 1.0) {
+                    last_log = now_s();
+                    const double fraction = traced_samples / total, elapsed = last_log - t0;
+                    fprintf(stderr, "Progress %.1f%%; elapsed %.1fs; remaining approximately %.1fs\n", fraction * 100.0,
+                            elapsed, elapsed * (1.0 - fraction) / fraction);
+                }
+            }
+            if ((rc = pt_display_tile(ctx, rgba.data()))) return fail("readback", pt_last_error(ctx));
+            for (uint32_t row = 0; row < vis[1]; ++row)
+                for (uint32_t col = 0; col < vis[0]; ++col)
+                    for (int c = 0; c < 3; ++c)
+                        rgb[((size_t)(y + row) * opt.width + x + col) * 3 + c] = rgba[((size_t)row * tile[0] + col) * 4 + c];
+        }
+    }
+    pt_destroy(ctx);
+    std::string err;
+    const bool ok = opt.output.size() > 4 && opt.output.substr(opt.output.size() - 4) == ".ppm"
+                        ? write_ppm(opt.output, rgb, opt.width, opt.height, err)
+                        : write_png(opt.output, rgb, opt.width, opt.height, err);
+    if (!ok) return fail("output", err);
+    fprintf(stderr, "Saved %s in %.1fs\n", opt.output.c_str(), now_s() - started);
+    return 0;
+}

@@ -252,6 +252,42 @@ int ptw_scene_cornell_box(ptw_world** out) {
     return PT_OK;
 }
 
+// sky: vertical gradient plus a Gaussian sun lobe, equirectangular, top row up
+int ptw_set_procedural_skybox(ptw_world* w, uint32_t W, uint32_t H) {
+    if (!w || W == 0 || H == 0) return PT_ERR_INVALID_ARG;
+    std::vector<float> px((size_t)W * H * 4);
+    const V3 sun = normalize(V3{-0.45f, 0.64f, -0.62f});
+    const float sigma2 = 0.0015f;
+    for (uint32_t y = 0; y < H; ++y) {
+        const float theta = ((float)y + 0.5f) / (float)H * kPi;
+        const float st = ptm::sinf_(theta), ct = ptm::cosf_(theta);
+        for (uint32_t x = 0; x < W; ++x) {
+            const float phi = (((float)x + 0.5f) / (float)W - 0.5f) * (2.0f * kPi);
+            const V3 d{st * ptm::cosf_(phi), ct, st * ptm::sinf_(phi)};
+            float r, g, b;
+            if (ct > 0.0f) {
+                const float s = ptm::sqrt_(ct);
+                r = 0.9f + (0.25f - 0.9f) * s;
+                g = 0.85f + (0.45f - 0.85f) * s;
+                b = 0.8f + (0.9f - 0.8f) * s;
+            } else {
+                const float s = 1.0f + ct;
+                r = 0.25f * s;
+                g = 0.22f * s;
+                b = 0.2f * s;
+            }
+            const float sd = 1.0f - dot(d, sun);
+            const float lobe = 2000.0f * ptm::exp2f_(-(sd / sigma2) * 1.44269504f);
+            float* o = &px[((size_t)y * W + x) * 4];
+            o[0] = r + lobe;
+            o[1] = g + 0.95f * lobe;
+            o[2] = b + 0.85f * lobe;
+            o[3] = 1.0f;
+        }
+    }
+    return ptw_set_skybox_rgba(w, px.data(), W, H);
+}
+
 void ptw_procedural_defaults(ptw_procedural_params* p) {
     if (!p) return;
     std::memset(p, 0, sizeof(*p));
@@ -363,46 +399,14 @@ int ptw_scene_procedural(const ptw_procedural_params* params, ptw_world** out) {
         rc = e.add_to(w, mi);
     }
     if (!rc) rc = ptw_build(w);
-    // sky: vertical gradient plus a Gaussian sun lobe
     if (!rc && P.skybox_width > 0 && P.skybox_height > 0) {
-        const uint32_t W = P.skybox_width, H = P.skybox_height;
-        std::vector<float> px((size_t)W * H * 4);
-        const V3 sun = normalize(V3{-0.45f, 0.64f, -0.62f});
-        const float sigma2 = 0.0015f;
-        for (uint32_t y = 0; y < H; ++y) {
-            const float theta = ((float)y + 0.5f) / (float)H * kPi;
-            const float st = ptm::sinf_(theta), ct = ptm::cosf_(theta);
-            for (uint32_t x = 0; x < W; ++x) {
-                const float phi = (((float)x + 0.5f) / (float)W - 0.5f) * (2.0f * kPi);
-                const V3 d{st * ptm::cosf_(phi), ct, st * ptm::sinf_(phi)};
-                float r, g, b;
-                if (ct > 0.0f) {
-                    const float s = ptm::sqrt_(ct);
-                    r = 0.9f + (0.25f - 0.9f) * s;
-                    g = 0.85f + (0.45f - 0.85f) * s;
-                    b = 0.8f + (0.9f - 0.8f) * s;
-                } else {
-                    const float s = 1.0f + ct;
-                    r = 0.25f * s;
-                    g = 0.22f * s;
-                    b = 0.2f * s;
-                }
-                const float sd = 1.0f - dot(d, sun);
-                const float lobe = 2000.0f * ptm::exp2f_(-(sd / sigma2) * 1.44269504f);
-                float* o = &px[((size_t)y * W + x) * 4];
-                o[0] = r + lobe;
-                o[1] = g + 0.95f * lobe;
-                o[2] = b + 0.85f * lobe;
-                o[3] = 1.0f;
-            }
-        }
-        rc = ptw_set_skybox_rgba(w, px.data(), W, H);
+        rc = ptw_set_procedural_skybox(w, P.skybox_width, P.skybox_height);
         if (!rc) rc = ptw_edit_skybox_average_luminance(w, P.skybox_luminance);
     }
     if (!rc) {
         // elevated camera looking down the terrain
-        const float pos[3] = {0.0f, 14.0f, 26.0f};
-        const float yaw = 0.0f, pitch = -0.42f, fov = 1.2f;
+        const float pos[3] = {0.0f, 14.0f, 20.0f};
+        const float yaw = 0.0f, pitch = -0.45f, fov = 1.2f;
         rc = ptw_edit_camera(w, pos, &yaw, &pitch, &fov);
     }
     if (rc) {

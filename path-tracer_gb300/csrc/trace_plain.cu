@@ -11,6 +11,7 @@ namespace ptd {
 PTD void init_counters(Counters& c) {
     c.visit_hash = kFnvBasis;
     c.extend_rays = c.shadow_rays = c.interior_visits = c.leaf_visits = c.triangle_tests = c.rand_draws = 0;
+    c.shadow_interior_visits = c.shadow_leaf_visits = c.shadow_triangle_tests = 0;
     c.hits = c.sky_misses = c.light_samples = c.sky_light_samples = 0;
 }
 
@@ -22,6 +23,9 @@ PTD void write_record(pt_path_record* r, const Counters& c, const int32_t* hits,
     r->interior_visits = c.interior_visits;
     r->leaf_visits = c.leaf_visits;
     r->triangle_tests = c.triangle_tests;
+    r->shadow_interior_visits = c.shadow_interior_visits;
+    r->shadow_leaf_visits = c.shadow_leaf_visits;
+    r->shadow_triangle_tests = c.shadow_triangle_tests;
     r->rand_draws = c.rand_draws;
     r->hits = c.hits;
     r->sky_misses = c.sky_misses;

@@ -39,6 +39,31 @@ struct Queues {
     int32_t* rec_hits;
 };
 
+// the queues one stage reads and writes, with the ping-pong already resolved
+struct Stage {
+    float4* o;  // current ray queue
+    float4* d;
+    float4* T;
+    float4* no;  // next ray queue
+    float4* nd;
+    float4* nT;
+    uint32_t* count;       // length of the current queue
+    uint32_t* next_count;  // length of the next queue
+};
+
+PTD Stage stage_of(const Queues& q, int cur) {
+    Stage s;
+    s.o = cur ? q.o[1] : q.o[0];
+    s.d = cur ? q.d[1] : q.d[0];
+    s.T = cur ? q.T[1] : q.T[0];
+    s.no = cur ? q.o[0] : q.o[1];
+    s.nd = cur ? q.d[0] : q.d[1];
+    s.nT = cur ? q.T[0] : q.T[1];
+    s.count = cur ? q.cnt + 1 : q.cnt;
+    s.next_count = cur ? q.cnt : q.cnt + 1;
+    return s;
+}
+
 constexpr int kExtendThreads = 128;
 constexpr int kShadeThreads = 128;
 
@@ -57,30 +82,60 @@ PTD float box_test(float4 lo, float4 hi, f3 nod, f3 rcp, float hit_t) {
     return intersect_aabb(bmin, bmax, nod, rcp, hit_t);
 }
 
-// closest-hit traversal (trace.slang:764-884) on the aligned child-pair
-// layout; the deferred stack holds the (left_first, tri_count) of each node
-// so a pop needs no memory access; visit order is the reference's.
-template <bool kRec, bool kAlpha>
-PTD void closest_hit_wf(const World& w, const Fast& f, f3 o, f3 d, Rng<kRec>& rng, Counters* c, float& hit_t,
-                        int32_t& hit, float& hv, float& hw) {
-    Rec<kRec> rec{};
-    if constexpr (kRec) {
-        rec.c = c;
-        c->extend_rays += 1;
+// One ray's traversal (trace.slang:764-884 closest hit, or 614-717 any hit
+// when kShadow) on the aligned child-pair layout, as a state machine advanced
+// one node visit per step().  The deferred stack holds the (left_first,
+// tri_count) of each node, so a pop needs no memory access.  Node visits
+// happen in exactly the reference's order.  The stacks live outside the
+// object so its scalar state can stay in registers.
+template <bool kRec, bool kAlpha, bool kShadow>
+struct Traverser {
+    f3 o, d, rcp, nod;
+    Shear s;
+    float hit_t, hv, hw;
+    int32_t hit, light_tri;
+    uint32_t lf, tc, sp, idx;
+    Rng<kRec> rng;
+    Counters c;
+    Rec<kRec> rec;
+
+    PTD void init(const Fast& f, f3 origin, f3 dir, float t_max, int32_t light) {
+        o = origin;
+        d = dir;
+        rcp = 1.0f / d;
+        s = make_shear(d, rcp);
+        nod = -o * rcp;
+        hit_t = t_max;
+        hv = hw = 0.0f;
+        hit = -1;
+        light_tri = light;
+        sp = 0u;
+        idx = 0u;
+        lf = __float_as_uint(__ldg(&f.pairs[0].w));
+        tc = __float_as_uint(__ldg(&f.pairs[1].w));
+        if constexpr (kRec) {
+            rec.c = &c;
+            rng.rec.c = &c;
+            if constexpr (kShadow) {
+                rec.shadow = true;
+                c.shadow_rays += 1;
+            } else {
+                c.extend_rays += 1;
+            }
+        }
     }
-    const f3 rcp = 1.0f / d;
-    const Shear s = make_shear(d, rcp);
-    const f3 nod = -o * rcp;
-    uint2 stack[64];
-    uint32_t istack[kRec ? 64 : 1];
-    uint32_t idx = 0u, sp = 0u;
-    uint32_t lf = __float_as_uint(__ldg(&f.pairs[0].w)), tc = __float_as_uint(__ldg(&f.pairs[1].w));
-    for (;;) {
+
+    // one node visit; true when the traversal has finished (for kShadow,
+    // hit == 1 marks an occluder)
+    PTD bool step(const World& w, const Fast& f, uint2* stack, uint32_t* istack) {
         rec.visit(idx);
         if (tc > 0u) {
             rec.leaf();
             for (uint32_t i = 0; i < tc; ++i) {
                 const uint32_t tri = lf + i;
+                if constexpr (kShadow) {
+                    if ((int32_t)tri == light_tri) continue;
+                }
                 rec.tri();
                 float t, v, wb;
                 if (!triangle_test(load_tri4(f, tri), o, s, &t, &v, &wb)) continue;
@@ -88,10 +143,15 @@ PTD void closest_hit_wf(const World& w, const Fast& f, f3 o, f3 d, Rng<kRec>& rn
                     if constexpr (kAlpha) {
                         if (passes_through(w, tri, v, wb, rng)) continue;
                     }
-                    hit_t = t;
-                    hit = (int32_t)tri;
-                    hv = v;
-                    hw = wb;
+                    if constexpr (kShadow) {
+                        hit = 1;
+                        return true;
+                    } else {
+                        hit_t = t;
+                        hit = (int32_t)tri;
+                        hv = v;
+                        hw = wb;
+                    }
                 }
             }
         } else {
@@ -103,86 +163,30 @@ PTD void closest_hit_wf(const World& w, const Fast& f, f3 o, f3 d, Rng<kRec>& rn
             const bool hl = dl >= 0.0f, hr = dr >= 0.0f;
             if (hl || hr) {
                 const bool go_left = hl && (!hr || dl < dr);
-                const float4 n0 = go_left ? l0 : r0, n1 = go_left ? l1 : r1;
                 if (hl && hr) {
                     const float4 f0 = go_left ? r0 : l0, f1 = go_left ? r1 : l1;
                     stack[sp & 63u] = make_uint2(__float_as_uint(f0.w), __float_as_uint(f1.w));
                     if constexpr (kRec) istack[sp & 63u] = go_left ? lf + 1u : lf;
                     sp += 1u;
                 }
+                const float4 n0 = go_left ? l0 : r0, n1 = go_left ? l1 : r1;
                 if constexpr (kRec) idx = go_left ? lf : lf + 1u;
                 lf = __float_as_uint(n0.w);
                 tc = __float_as_uint(n1.w);
-                continue;
+                return false;
             }
         }
-        if (sp == 0u) break;
+        if (sp == 0u) return true;
         sp -= 1u;
         const uint2 e = stack[sp & 63u];
         lf = e.x;
         tc = e.y;
         if constexpr (kRec) idx = istack[sp & 63u];
+        return false;
     }
-}
+};
 
-// any-hit traversal (trace.slang:614-717) on the same layout, opaque scenes
-template <bool kRec>
-PTD bool occluded_wf(const World& w, const Fast& f, f3 o, f3 d, float hit_t, int32_t light_tri, Counters* c) {
-    Rec<kRec> rec{};
-    if constexpr (kRec) {
-        rec.c = c;
-        c->shadow_rays += 1;
-    }
-    const f3 rcp = 1.0f / d;
-    const Shear s = make_shear(d, rcp);
-    const f3 nod = -o * rcp;
-    uint2 stack[64];
-    uint32_t istack[kRec ? 64 : 1];
-    uint32_t idx = 0u, sp = 0u;
-    uint32_t lf = __float_as_uint(__ldg(&f.pairs[0].w)), tc = __float_as_uint(__ldg(&f.pairs[1].w));
-    for (;;) {
-        rec.visit(idx);
-        if (tc > 0u) {
-            rec.leaf();
-            for (uint32_t i = 0; i < tc; ++i) {
-                const uint32_t tri = lf + i;
-                if ((int32_t)tri == light_tri) continue;
-                rec.tri();
-                float t, v, wb;
-                if (!triangle_test(load_tri4(f, tri), o, s, &t, &v, &wb)) continue;
-                if (t > 0.0f && t < hit_t) return true;
-            }
-        } else {
-            rec.interior();
-            const float4* p = f.pairs + 2 * (size_t)lf;
-            const float4 l0 = __ldg(p), l1 = __ldg(p + 1), r0 = __ldg(p + 2), r1 = __ldg(p + 3);
-            const float dl = box_test(l0, l1, nod, rcp, hit_t);
-            const float dr = box_test(r0, r1, nod, rcp, hit_t);
-            const bool hl = dl >= 0.0f, hr = dr >= 0.0f;
-            if (hl || hr) {
-                const bool go_left = hl && (!hr || dl < dr);
-                const float4 n0 = go_left ? l0 : r0, n1 = go_left ? l1 : r1;
-                if (hl && hr) {
-                    const float4 f0 = go_left ? r0 : l0, f1 = go_left ? r1 : l1;
-                    stack[sp & 63u] = make_uint2(__float_as_uint(f0.w), __float_as_uint(f1.w));
-                    if constexpr (kRec) istack[sp & 63u] = go_left ? lf + 1u : lf;
-                    sp += 1u;
-                }
-                if constexpr (kRec) idx = go_left ? lf : lf + 1u;
-                lf = __float_as_uint(n0.w);
-                tc = __float_as_uint(n1.w);
-                continue;
-            }
-        }
-        if (sp == 0u) break;
-        sp -= 1u;
-        const uint2 e = stack[sp & 63u];
-        lf = e.x;
-        tc = e.y;
-        if constexpr (kRec) idx = istack[sp & 63u];
-    }
-    return false;
-}
+constexpr int kStepsPerRefill = 8;
 
 PTD unsigned lane_id() {
     unsigned l;
@@ -227,6 +231,8 @@ __global__ void __launch_bounds__(256) raygen_kernel(World w, ptk::Tile t, Group
     if constexpr (kRec) {
         c.visit_hash = kFnvBasis;
         c.extend_rays = c.shadow_rays = c.interior_visits = c.leaf_visits = c.triangle_tests = c.rand_draws = 0;
+        c.shadow_interior_visits = c.shadow_leaf_visits = c.shadow_triangle_tests = 0;
+    c.shadow_interior_visits = c.shadow_leaf_visits = c.shadow_triangle_tests = 0;
         c.hits = c.sky_misses = c.light_samples = c.sky_light_samples = 0;
     }
     Rng<kRec> rng;
@@ -251,35 +257,56 @@ __global__ void bounce_reset_kernel(uint32_t* cnt, int next) {
     cnt[4] = 0u;
 }
 
+// Persistent extend kernel: every lane traverses its own ray and takes a new
+// one from the queue (one atomic per warp for all idle lanes) as soon as it
+// finishes, so long and short rays do not leave lanes idle.
 template <bool kRec, bool kAlpha>
 __global__ void __launch_bounds__(kExtendThreads) extend_kernel(World w, Fast f, Queues q, int cur, uint32_t bounce) {
-    const uint32_t count = q.cnt[cur];
+    const Stage st = stage_of(q, cur);
+    const uint32_t count = *st.count;
     const unsigned lane = lane_id();
+    Traverser<kRec, kAlpha, false> tr;
+    uint2 stack[64];
+    uint32_t istack[kRec ? 64 : 1];
+    uint32_t slot = 0, path = 0;
+    bool active = false, exhausted = false;
     for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(&q.cnt[3], 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= count) break;
-        const uint32_t i = base + lane;
-        if (i < count) {
-            const float4 o4 = q.o[cur][i];
-            const float4 d4 = q.d[cur][i];
-            const uint32_t p = __float_as_uint(o4.w);
-            Counters c;
-            Rng<kRec> rng;
-            rng.s = __float_as_uint(d4.w);
-            if constexpr (kRec) {
-                c = q.rec[p];
-                rng.rec.c = &c;
+        if (!exhausted) {
+            const unsigned idle = __ballot_sync(0xffffffffu, !active);
+            if (idle) {
+                const unsigned leader = (unsigned)(__ffs(idle) - 1);
+                uint32_t base = 0;
+                if (lane == leader) base = atomicAdd(&q.cnt[3], (uint32_t)__popc(idle));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (!active) {
+                    const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                    if (i < count) {
+                        slot = i;
+                        const float4 o4 = st.o[i], d4 = st.d[i];
+                        path = __float_as_uint(o4.w);
+                        tr.rng.s = __float_as_uint(d4.w);
+                        if constexpr (kRec) tr.c = q.rec[path];
+                        tr.init(f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), kFltMax, -1);
+                        active = true;
+                    }
+                }
+                if (base + (uint32_t)__popc(idle) >= count) exhausted = true;
             }
-            float hit_t = kFltMax, hv = 0.0f, hw = 0.0f;
-            int32_t hit = -1;
-            closest_hit_wf<kRec, kAlpha>(w, f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), rng, &c, hit_t, hit, hv, hw);
-            q.hit[i] = make_float4(hit_t, __int_as_float(hit), hv, hw);
-            if constexpr (kAlpha) q.d[cur][i].w = __uint_as_float(rng.s);
-            if constexpr (kRec) {
-                q.rec[p] = c;
-                if (bounce < PT_RECORD_MAX_BOUNCES) q.rec_hits[(size_t)p * PT_RECORD_MAX_BOUNCES + bounce] = hit;
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active) {
+#pragma unroll 1
+            for (int k = 0; k < kStepsPerRefill; ++k) {
+                if (tr.step(w, f, stack, istack)) {
+                    q.hit[slot] = make_float4(tr.hit_t, __int_as_float(tr.hit), tr.hv, tr.hw);
+                    if constexpr (kAlpha) st.d[slot].w = __uint_as_float(tr.rng.s);
+                    if constexpr (kRec) {
+                        q.rec[path] = tr.c;
+                        if (bounce < PT_RECORD_MAX_BOUNCES) q.rec_hits[(size_t)path * PT_RECORD_MAX_BOUNCES + bounce] = tr.hit;
+                    }
+                    active = false;
+                    break;
+                }
             }
         }
     }
@@ -288,8 +315,8 @@ __global__ void __launch_bounds__(kExtendThreads) extend_kernel(World w, Fast f,
 template <bool kRec, bool kAlpha>
 __global__ void __launch_bounds__(kShadeThreads) shade_kernel(World w, Fast f, Queues q, int cur, uint32_t bounce,
                                                               uint32_t max_bounces) {
-    const uint32_t count = q.cnt[cur];
-    const int next = cur ^ 1;
+    const Stage st = stage_of(q, cur);
+    const uint32_t count = *st.count;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     const unsigned lane = lane_id();
@@ -301,7 +328,7 @@ __global__ void __launch_bounds__(kShadeThreads) shade_kernel(World w, Fast f, Q
         PathState ps;
         uint32_t p = 0, rs = 0;
         if (i < count) {
-            const float4 o4 = q.o[cur][i], d4 = q.d[cur][i], t4 = q.T[cur][i], h4 = q.hit[i];
+            const float4 o4 = st.o[i], d4 = st.d[i], t4 = st.T[i], h4 = q.hit[i];
             p = __float_as_uint(o4.w);
             const float4 c4 = q.color[p];
             ps.o = mk(o4.x, o4.y, o4.z);
@@ -328,11 +355,11 @@ __global__ void __launch_bounds__(kShadeThreads) shade_kernel(World w, Fast f, Q
             rs = rng.s;
             if constexpr (kRec) q.rec[p] = c;
         }
-        const uint32_t slot = warp_append(cont, &q.cnt[next], 0xffffffffu);
+        const uint32_t slot = warp_append(cont, st.next_count, 0xffffffffu);
         if (cont) {
-            q.o[next][slot] = make_float4(ps.o.x, ps.o.y, ps.o.z, __uint_as_float(p));
-            q.d[next][slot] = make_float4(ps.d.x, ps.d.y, ps.d.z, __uint_as_float(rs));
-            q.T[next][slot] = make_float4(ps.throughput.x, ps.throughput.y, ps.throughput.z, ps.prev_pdf);
+            st.no[slot] = make_float4(ps.o.x, ps.o.y, ps.o.z, __uint_as_float(p));
+            st.nd[slot] = make_float4(ps.d.x, ps.d.y, ps.d.z, __uint_as_float(rs));
+            st.nT[slot] = make_float4(ps.throughput.x, ps.throughput.y, ps.throughput.z, ps.prev_pdf);
         }
         if constexpr (!kAlpha) {
             const uint32_t sslot = warp_append(sr.valid, &q.cnt[2], 0xffffffffu);
@@ -345,29 +372,55 @@ __global__ void __launch_bounds__(kShadeThreads) shade_kernel(World w, Fast f, Q
     }
 }
 
+// Persistent shadow kernel (opaque scenes): any-hit traversal of every queued
+// shadow ray with the same lane refill; unoccluded rays add their light.
 template <bool kRec>
 __global__ void __launch_bounds__(kExtendThreads) shadow_kernel(World w, Fast f, Queues q) {
     const uint32_t count = q.cnt[2];
     const unsigned lane = lane_id();
+    Traverser<kRec, false, true> tr;
+    uint2 stack[64];
+    uint32_t istack[kRec ? 64 : 1];
+    uint32_t path = 0;
+    float4 contribution = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    bool active = false, exhausted = false;
     for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(&q.cnt[4], 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= count) break;
-        const uint32_t i = base + lane;
-        if (i < count) {
-            const float4 o4 = q.so[i], d4 = q.sd[i], c4 = q.sc[i];
-            const uint32_t p = __float_as_uint(o4.w);
-            Counters c;
-            if constexpr (kRec) c = q.rec[p];
-            const bool occ = occluded_wf<kRec>(w, f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), d4.w,
-                                               __float_as_int(c4.w), &c);
-            if (!occ) {
-                const float4 col = q.color[p];
-                const f3 sum = mk(col.x, col.y, col.z) + mk(c4.x, c4.y, c4.z);
-                q.color[p] = make_float4(sum.x, sum.y, sum.z, 0.0f);
+        if (!exhausted) {
+            const unsigned idle = __ballot_sync(0xffffffffu, !active);
+            if (idle) {
+                const unsigned leader = (unsigned)(__ffs(idle) - 1);
+                uint32_t base = 0;
+                if (lane == leader) base = atomicAdd(&q.cnt[4], (uint32_t)__popc(idle));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (!active) {
+                    const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                    if (i < count) {
+                        const float4 o4 = q.so[i], d4 = q.sd[i];
+                        contribution = q.sc[i];
+                        path = __float_as_uint(o4.w);
+                        if constexpr (kRec) tr.c = q.rec[path];
+                        tr.init(f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), d4.w, __float_as_int(contribution.w));
+                        active = true;
+                    }
+                }
+                if (base + (uint32_t)__popc(idle) >= count) exhausted = true;
             }
-            if constexpr (kRec) q.rec[p] = c;
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active) {
+#pragma unroll 1
+            for (int k = 0; k < kStepsPerRefill; ++k) {
+                if (tr.step(w, f, stack, istack)) {
+                    if (tr.hit != 1) {
+                        const float4 col = q.color[path];
+                        const f3 sum = mk(col.x, col.y, col.z) + mk(contribution.x, contribution.y, contribution.z);
+                        q.color[path] = make_float4(sum.x, sum.y, sum.z, 0.0f);
+                    }
+                    if constexpr (kRec) q.rec[path] = tr.c;
+                    active = false;
+                    break;
+                }
+            }
         }
     }
 }
@@ -410,6 +463,12 @@ __global__ void finalize_records_kernel(ptk::Tile t, Group g, Queues q, ptk::Sin
         r->interior_visits = c.interior_visits;
         r->leaf_visits = c.leaf_visits;
         r->triangle_tests = c.triangle_tests;
+        r->shadow_interior_visits = c.shadow_interior_visits;
+        r->shadow_leaf_visits = c.shadow_leaf_visits;
+        r->shadow_triangle_tests = c.shadow_triangle_tests;
+    r->shadow_interior_visits = c.shadow_interior_visits;
+    r->shadow_leaf_visits = c.shadow_leaf_visits;
+    r->shadow_triangle_tests = c.shadow_triangle_tests;
         r->rand_draws = c.rand_draws;
         r->hits = c.hits;
         r->sky_misses = c.sky_misses;

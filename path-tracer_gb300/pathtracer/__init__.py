@@ -348,10 +348,11 @@ class PathTracer:
 
 RECORD_DTYPE = np.dtype([("visit_hash", "<u8"), ("hit", "<i4", (abi.PT_RECORD_MAX_BOUNCES,)),
                          ("extend_rays", "<u4"), ("shadow_rays", "<u4"), ("interior_visits", "<u4"),
-                         ("leaf_visits", "<u4"), ("triangle_tests", "<u4"), ("rand_draws", "<u4"),
+                         ("leaf_visits", "<u4"), ("triangle_tests", "<u4"), ("shadow_interior_visits", "<u4"),
+                         ("shadow_leaf_visits", "<u4"), ("shadow_triangle_tests", "<u4"), ("rand_draws", "<u4"),
                          ("hits", "<u4"), ("sky_misses", "<u4"), ("light_samples", "<u4"),
-                         ("sky_light_samples", "<u4"), ("radiance", "<f4", (3,))])
-assert RECORD_DTYPE.itemsize == 128
+                         ("sky_light_samples", "<u4"), ("radiance", "<f4", (3,)), ("pad", "<u4")])
+assert RECORD_DTYPE.itemsize == 144
 
 
 def records_to_numpy(recs, count: int) -> np.ndarray:

@@ -40,7 +40,8 @@ PT_TILE_ACCUMULATION = 1
 PT_KERNEL_CLASS_COUNT = 6
 KERNEL_CLASSES = ["raygen", "extend", "shade", "shadow", "accumulate", "plain"]
 PT_RECORD_MAX_BOUNCES = 17
-COUNT_FIELDS = ["extend_rays", "shadow_rays", "interior_visits", "leaf_visits", "triangle_tests", "rand_draws",
+COUNT_FIELDS = ["extend_rays", "shadow_rays", "interior_visits", "leaf_visits", "triangle_tests",
+                "shadow_interior_visits", "shadow_leaf_visits", "shadow_triangle_tests", "rand_draws",
                 "hits", "sky_misses", "light_samples", "sky_light_samples"]
 EXPOSURE = 0.00002604166
 
@@ -129,8 +130,9 @@ class WorldUpdates(C.Structure):
 class PathRecord(C.Structure):
     _fields_ = [("visit_hash", c_u64), ("hit", c_i32 * PT_RECORD_MAX_BOUNCES), ("extend_rays", c_u32),
                 ("shadow_rays", c_u32), ("interior_visits", c_u32), ("leaf_visits", c_u32),
-                ("triangle_tests", c_u32), ("rand_draws", c_u32), ("hits", c_u32), ("sky_misses", c_u32),
-                ("light_samples", c_u32), ("sky_light_samples", c_u32), ("radiance", c_f * 3)]
+                ("triangle_tests", c_u32), ("shadow_interior_visits", c_u32), ("shadow_leaf_visits", c_u32),
+                ("shadow_triangle_tests", c_u32), ("rand_draws", c_u32), ("hits", c_u32), ("sky_misses", c_u32),
+                ("light_samples", c_u32), ("sky_light_samples", c_u32), ("radiance", c_f * 3), ("pad", c_u32)]
 
 
 class Mesh(C.Structure):
@@ -148,7 +150,7 @@ class ProceduralParams(C.Structure):
 STRUCT_SIZES = {
     TriangleGeometry: 36, TriangleAttribute: 112, BvhNode: 32, Material: 224, Camera: 64,
     SceneUniforms: 16, SceneAliasEntry: 16, SkyboxUniforms: 16, SkyboxAliasEntry: 12,
-    TraceParameters: 32, PathRecord: 128,
+    TraceParameters: 32, PathRecord: 144,
 }
 
 P = C.POINTER
@@ -187,6 +189,7 @@ SIGNATURES = {
     "ptw_add_atlas_layer": (C.c_int, [_vp, C.c_int, _vp, P(c_i32)]),
     "ptw_build": (C.c_int, [_vp]),
     "ptw_set_skybox_rgba": (C.c_int, [_vp, _vp, c_u32, c_u32]),
+    "ptw_set_procedural_skybox": (C.c_int, [_vp, c_u32, c_u32]),
     "ptw_edit_skybox_average_luminance": (C.c_int, [_vp, c_f]),
     "ptw_set_aspect_ratio": (C.c_int, [_vp, c_f]),
     "ptw_edit_camera": (C.c_int, [_vp, P(c_f), P(c_f), P(c_f), P(c_f)]),

@@ -127,10 +127,15 @@ def test_display_tile_matches_tonemap(tracer):
 
 def test_synchronize_and_profiling(tracer):
     tracer.set_profiling(True)
+    tracer.set_kernel(abi.PT_KERNEL_PLAIN)
     tracer.trace(4)
     tracer.synchronize(timeout_ms=60000)
     times = tracer.kernel_times()
     assert times.launches["plain"] == 4 and times.milliseconds["plain"] > 0
+    tracer.set_kernel(abi.PT_KERNEL_WAVEFRONT)
+    tracer.trace(2)
+    times = tracer.kernel_times()
+    assert times.launches["extend"] == tracer.max_bounces() + 1 and times.launches["raygen"] == 1
     tracer.reset_kernel_times()
     assert tracer.kernel_times().launches["plain"] == 0
     assert tracer.launch_count() >= 4

@@ -26,7 +26,8 @@ def pixels_of(origin, size, image):
 def assert_records_equal(gpu, ref):
     assert gpu.shape == ref.shape
     for field in ("visit_hash", "hit", "extend_rays", "shadow_rays", "interior_visits", "leaf_visits",
-                  "triangle_tests", "rand_draws", "hits", "sky_misses", "light_samples", "sky_light_samples"):
+                  "triangle_tests", "shadow_interior_visits", "shadow_leaf_visits", "shadow_triangle_tests",
+                  "rand_draws", "hits", "sky_misses", "light_samples", "sky_light_samples"):
         bad = np.nonzero(np.any((gpu[field] != ref[field]).reshape(gpu.shape[0], -1), axis=1))[0]
         assert bad.size == 0, f"{field} differs in {bad.size} paths, first {bad[:5]}"
     np.testing.assert_array_equal(gpu["radiance"].view(np.uint32), ref["radiance"].view(np.uint32))
@@ -124,7 +125,7 @@ def test_intersect_random_rays_cornell(cornell):
     np.testing.assert_array_equal(t.view(np.uint32), rt.view(np.uint32))
     np.testing.assert_array_equal(rec["visit_hash"], rrec["visit_hash"])
     np.testing.assert_array_equal(rec["triangle_tests"], rrec["triangle_tests"])
-    assert (hit >= 0).mean() > 0.5
+    assert (hit >= 0).mean() > 0.3
     tr.close()
 
 
@@ -157,6 +158,7 @@ def test_large_scene_tile_bit_exact(large_world, kernel):
     tr = pt.PathTracer(u, (64, 64))
     tr.set_kernel(kernel)
     tr.set_max_bounces(8)
+    light = sky = 0
     for origin in ((900, 500), (1880, 1050)):
         tr.set_tile((1920, 1080), origin, (64, 64))
         gpu = tr.trace_recorded(4).reshape(4, 64, 64)
@@ -165,7 +167,9 @@ def test_large_scene_tile_bit_exact(large_world, kernel):
         px = pixels_of(origin, (64, 64), (1920, 1080))
         _, ref = oracle.trace_paths(ow, (1920, 1080), 8, px, 1, 4, records=True)
         assert_records_equal(gpu, ref)
-        assert ref["sky_light_samples"].sum() > 0 and ref["light_samples"].sum() > 0
+        light += int(ref["light_samples"].sum())
+        sky += int(ref["sky_light_samples"].sum())
+    assert light > 0 and sky > 0  # both light categories exercised
     tr.close()
 
 
