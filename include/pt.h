@@ -341,6 +341,70 @@ int pt_trace_recorded(pt_ctx* ctx, uint32_t sample_count, uint32_t* traced,
 int pt_debug_intersect(pt_ctx* ctx, uint64_t n, const float* origins, const float* directions,
                        const float* t_max, int32_t* hit, float* hit_t, pt_path_record* records);
 
+/* ------------------------------------------------- allocation-free tracing */
+
+/* The world as device buffers the caller already owns: the same layouts as
+ * pt_scene_upload / pt_skybox_upload, but every pointer is a device address. */
+typedef struct pt_device_world {
+    const pt_triangle_geometry* geometries;   /* triangle_count entries */
+    const pt_triangle_attribute* attributes;  /* triangle_count entries */
+    uint64_t triangle_count;
+    const pt_material* materials;
+    uint64_t material_count;
+    const pt_bvh_node* bvh_nodes;             /* 16-byte aligned */
+    uint64_t node_count;
+    const uint8_t* srgb_texture_atlases;      /* srgb_atlas_count layers, may be NULL if 0 */
+    uint32_t srgb_atlas_count;
+    const uint8_t* linear_texture_atlases;
+    uint32_t linear_atlas_count;
+    const float* skybox_rgba;                 /* width * height RGBA32F, 16-byte aligned */
+    const pt_skybox_alias_entry* skybox_aliases;
+    const pt_scene_alias_entry* scene_aliases;
+    pt_camera camera;
+    pt_scene_uniforms scene_uniforms;
+    pt_skybox_uniforms skybox_uniforms;
+    int32_t any_non_opaque;                   /* 1 if some material is not PT_ALPHA_MODE_OPAQUE */
+} pt_device_world;
+
+/* largest (visible tile pixels x samples) one pt_trace_noalloc call accepts */
+#define PT_NOALLOC_MAX_PATHS 262144u
+/* size of the library's static device scratch array (every GPU that loads
+ * the library holds it until the process exits) */
+#define PT_NOALLOC_SCRATCH_BYTES (48u << 20)
+
+/* No counterpart in the reference: an extra entry point for callers that
+ * cannot allocate device memory themselves or through this library - for
+ * example a host application whose allocator owns all device memory and
+ * hands plug-ins ready-made buffers, or a latency-critical render thread that
+ * must not hit the device-wide synchronisation of cudaMalloc / cudaFree.
+ *
+ * Traces `samples` samples of one tile with the wavefront kernels and adds
+ * them to the caller's accumulation buffer, exactly like pt_trace (same
+ * bits), but allocates nothing: the world, `accum` and `image` (tile_width *
+ * tile_height * 4 floats each, row stride tile_width, 16-byte aligned) are
+ * the caller's device buffers, the queues live in a static device array of
+ * PT_NOALLOC_SCRATCH_BYTES, and at most PT_NOALLOC_MAX_PATHS paths are
+ * accepted per call (larger requests fail with PT_ERR_OUT_OF_LIMITS; split
+ * them into several calls or tiles).  params->sample_count is the number of
+ * samples already in `accum` (0 starts a new accumulation); image_size,
+ * tile_origin and max_bounces mean what they mean for pt_set_tile and
+ * pt_set_max_bounces.  Work is queued on `stream` (a cudaStream_t of the
+ * current device; NULL = legacy default stream) and the call returns without
+ * waiting.
+ *
+ * The first call on each device sets up the scratch array on that device
+ * (looks up its device address and uploads a 1 KB sRGB table, a synchronous
+ * copy); make that first call before any stream capture.  Every call on a
+ * device shares the one scratch array, which keeps the previous call's
+ * contents: calls that overlap on the GPU (different streams or threads
+ * without ordering) race and corrupt each other.  The world is not
+ * validated, so it must be a world pt_apply_updates would accept.  If
+ * `error` is not NULL, a failure message is written there (at most
+ * error_size bytes, NUL-terminated). */
+int pt_trace_noalloc(const pt_device_world* world, const pt_trace_parameters* params, uint32_t tile_width,
+                     uint32_t tile_height, uint32_t samples, float* accum, float* image, void* stream,
+                     char* error, size_t error_size);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,6 +13,9 @@
 //   block read with four 16-byte loads; triangles padded to 3 x float4.
 // Every path runs exactly the arithmetic of the plain kernel (pt_path.cuh),
 // in the same order, so results are bit-identical.
+#include <cmath>
+#include <cstdio>
+#include <mutex>
 #include <vector>
 
 #include "pt_path.cuh"
@@ -88,7 +91,7 @@ PTD float box_test(float4 lo, float4 hi, f3 nod, f3 rcp, float hit_t) {
 // tri_count) of each node, so a pop needs no memory access.  Node visits
 // happen in exactly the reference's order.  The stacks live outside the
 // object so its scalar state can stay in registers.
-template <bool kRec, bool kAlpha, bool kShadow>
+template <bool kRec, bool kAlpha, bool kShadow, bool kTri36 = false>
 struct Traverser {
     f3 o, d, rcp, nod;
     Shear s;
@@ -138,7 +141,12 @@ struct Traverser {
                 }
                 rec.tri();
                 float t, v, wb;
-                if (!triangle_test(load_tri4(f, tri), o, s, &t, &v, &wb)) continue;
+                Tri tv;
+                if constexpr (kTri36)
+                    tv = load_tri(w, tri);  // the caller's 36-byte triangles
+                else
+                    tv = load_tri4(f, tri);
+                if (!triangle_test(tv, o, s, &t, &v, &wb)) continue;
                 if (t > 0.0f && t < hit_t) {
                     if constexpr (kAlpha) {
                         if (passes_through(w, tri, v, wb, rng)) continue;
@@ -260,12 +268,12 @@ __global__ void bounce_reset_kernel(uint32_t* cnt, int next) {
 // Persistent extend kernel: every lane traverses its own ray and takes a new
 // one from the queue (one atomic per warp for all idle lanes) as soon as it
 // finishes, so long and short rays do not leave lanes idle.
-template <bool kRec, bool kAlpha>
+template <bool kRec, bool kAlpha, bool kTri36 = false>
 __global__ void __launch_bounds__(kExtendThreads) extend_kernel(World w, Fast f, Queues q, int cur, uint32_t bounce) {
     const Stage st = stage_of(q, cur);
     const uint32_t count = *st.count;
     const unsigned lane = lane_id();
-    Traverser<kRec, kAlpha, false> tr;
+    Traverser<kRec, kAlpha, false, kTri36> tr;
     uint2 stack[64];
     uint32_t istack[kRec ? 64 : 1];
     uint32_t slot = 0, path = 0;
@@ -374,11 +382,11 @@ __global__ void __launch_bounds__(kShadeThreads) shade_kernel(World w, Fast f, Q
 
 // Persistent shadow kernel (opaque scenes): any-hit traversal of every queued
 // shadow ray with the same lane refill; unoccluded rays add their light.
-template <bool kRec>
+template <bool kRec, bool kTri36 = false>
 __global__ void __launch_bounds__(kExtendThreads) shadow_kernel(World w, Fast f, Queues q) {
     const uint32_t count = q.cnt[2];
     const unsigned lane = lane_id();
-    Traverser<kRec, false, true> tr;
+    Traverser<kRec, false, true, kTri36> tr;
     uint2 stack[64];
     uint32_t istack[kRec ? 64 : 1];
     uint32_t path = 0;
@@ -592,14 +600,17 @@ int occupancy(K kernel, int threads) {
     return blocks > 0 ? blocks : 1;
 }
 
-template <bool kRec, bool kAlpha>
-cudaError_t run_group(Wavefront* wf, const ptd::World& w, const ptd::Fast& f, const ptd::Queues& q,
+// one group of paths through raygen, max_bounces + 1 rounds of extend /
+// shade / shadow, and accumulate; kTri36 reads the reference's 36-byte
+// triangles instead of the padded copy
+template <bool kRec, bool kAlpha, bool kTri36, class TimerF>
+cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const ptd::Queues& q,
                       const ptk::Tile& tile, const ptd::Group& g, ptk::Sinks sinks, cudaStream_t stream,
-                      const Timer& timer) {
+                      TimerF&& timer) {
     using namespace ptd;
-    const int ext_blocks = wf->sms * occupancy(extend_kernel<kRec, kAlpha>, kExtendThreads);
-    const int sha_blocks = wf->sms * occupancy(shade_kernel<kRec, kAlpha>, kShadeThreads);
-    const int shd_blocks = wf->sms * occupancy(shadow_kernel<kRec>, kExtendThreads);
+    const int ext_blocks = sms * occupancy(extend_kernel<kRec, kAlpha, kTri36>, kExtendThreads);
+    const int sha_blocks = sms * occupancy(shade_kernel<kRec, kAlpha>, kShadeThreads);
+    const int shd_blocks = sms * occupancy(shadow_kernel<kRec, kTri36>, kExtendThreads);
     PTW_TRY(timer(PT_KC_RAYGEN, [&] {
         raygen_kernel<kRec><<<(g.paths + 255u) / 256u, 256, 0, stream>>>(w, tile, g, q);
         return cudaGetLastError();
@@ -609,7 +620,7 @@ cudaError_t run_group(Wavefront* wf, const ptd::World& w, const ptd::Fast& f, co
         bounce_reset_kernel<<<1, 1, 0, stream>>>(q.cnt, cur ^ 1);
         PTW_TRY(cudaGetLastError());
         PTW_TRY(timer(PT_KC_EXTEND, [&] {
-            extend_kernel<kRec, kAlpha><<<ext_blocks, kExtendThreads, 0, stream>>>(w, f, q, cur, bounce);
+            extend_kernel<kRec, kAlpha, kTri36><<<ext_blocks, kExtendThreads, 0, stream>>>(w, f, q, cur, bounce);
             return cudaGetLastError();
         }));
         PTW_TRY(timer(PT_KC_SHADE, [&] {
@@ -618,7 +629,7 @@ cudaError_t run_group(Wavefront* wf, const ptd::World& w, const ptd::Fast& f, co
         }));
         if constexpr (!kAlpha) {
             PTW_TRY(timer(PT_KC_SHADOW, [&] {
-                shadow_kernel<kRec><<<shd_blocks, kExtendThreads, 0, stream>>>(w, f, q);
+                shadow_kernel<kRec, kTri36><<<shd_blocks, kExtendThreads, 0, stream>>>(w, f, q);
                 return cudaGetLastError();
             }));
         }
@@ -679,11 +690,11 @@ cudaError_t trace(Wavefront* wf, const ptd::World& w, const ptk::Tile& tile, uin
         g.record_sample = s0;
         cudaError_t e;
         if (record)
-            e = w.any_alpha ? run_group<true, true>(wf, w, f, q, tile, g, sinks, stream, timer)
-                            : run_group<true, false>(wf, w, f, q, tile, g, sinks, stream, timer);
+            e = w.any_alpha ? run_group<true, true, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer)
+                            : run_group<true, false, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer);
         else
-            e = w.any_alpha ? run_group<false, true>(wf, w, f, q, tile, g, sinks, stream, timer)
-                            : run_group<false, false>(wf, w, f, q, tile, g, sinks, stream, timer);
+            e = w.any_alpha ? run_group<false, true, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer)
+                            : run_group<false, false, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer);
         PTW_TRY(e);
     }
     return cudaSuccess;
@@ -695,3 +706,169 @@ cudaError_t prepare(Wavefront* wf, const ptd::World& w, uint64_t nodes, uint64_t
 }
 
 }  // namespace ptw
+
+// ---------------------------------------------------------------------------
+// pt_trace_noalloc: the wavefront trace for callers that cannot allocate.
+// Its queues, counters and sRGB table live in the static device array below;
+// in host code the array's name is only a stand-in, so its device address is
+// looked up once per device with cudaGetSymbolAddress.
+namespace {
+
+constexpr uint64_t kNoAllocPaths = PT_NOALLOC_MAX_PATHS;
+constexpr size_t kNoAllocQueueBytes = 11ull * 16ull * kNoAllocPaths;  // o, d, T (x2), hit, colour, shadow o/d/c
+constexpr size_t kNoAllocCountersOffset = kNoAllocQueueBytes;
+constexpr size_t kNoAllocLutOffset = kNoAllocCountersOffset + 256;
+static_assert(kNoAllocLutOffset + 1024 <= PT_NOALLOC_SCRATCH_BYTES, "static scratch too small");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[PT_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kNoAllocMaxDevices = 64;
+struct NoAllocDevice {
+    bool ready;
+    unsigned char* scratch;  // device address of g_noalloc_scratch on this device
+    int sms;
+};
+NoAllocDevice g_noalloc_devices[kNoAllocMaxDevices];
+std::mutex g_noalloc_mutex;
+
+int noalloc_fail(char* error, size_t size, int code, const char* msg) {
+    if (error && size) snprintf(error, size, "%s", msg);
+    return code;
+}
+
+int noalloc_cuda(char* error, size_t size, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return PT_OK;
+    if (error && size) snprintf(error, size, "%s: %s", what, cudaGetErrorString(e));
+    return PT_ERR_CUDA;
+}
+
+// once per device, with that device current
+int noalloc_setup(int dev, char* error, size_t size) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    NoAllocDevice& d = g_noalloc_devices[dev];
+    if (d.ready) return PT_OK;
+    unsigned char* ptr = nullptr;
+    int rc = noalloc_cuda(error, size, cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch), "cudaGetSymbolAddress");
+    if (rc) return rc;
+    float lut[256];
+    for (int i = 0; i < 256; ++i) {
+        const double v = (double)i / 255.0;
+        lut[i] = (float)(v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4));
+    }
+    rc = noalloc_cuda(error, size, cudaMemcpy(ptr + kNoAllocLutOffset, lut, sizeof lut, cudaMemcpyHostToDevice),
+                      "sRGB table upload");
+    if (rc) return rc;
+    int sms = 0;
+    rc = noalloc_cuda(error, size, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+    if (rc) return rc;
+    d.scratch = ptr;
+    d.sms = sms;
+    d.ready = true;
+    return PT_OK;
+}
+
+}  // namespace
+
+extern "C" int pt_trace_noalloc(const pt_device_world* world, const pt_trace_parameters* params, uint32_t tile_width,
+                                uint32_t tile_height, uint32_t samples, float* accum, float* image, void* stream,
+                                char* error, size_t error_size) {
+    if (!world || !params || !accum || !image)
+        return noalloc_fail(error, error_size, PT_ERR_INVALID_ARG, "world, params, accum and image are required");
+    if (!world->geometries || !world->attributes || !world->materials || !world->bvh_nodes || !world->skybox_rgba ||
+        world->triangle_count == 0 || world->node_count == 0)
+        return noalloc_fail(error, error_size, PT_ERR_INVALID_ARG, "the world needs triangles, materials, BVH nodes and a skybox");
+    if (((uintptr_t)world->bvh_nodes | (uintptr_t)world->skybox_rgba | (uintptr_t)accum | (uintptr_t)image) & 15u)
+        return noalloc_fail(error, error_size, PT_ERR_INVALID_ARG, "BVH nodes, skybox, accum and image must be 16-byte aligned");
+    if (tile_width == 0 || tile_height == 0)
+        return noalloc_fail(error, error_size, PT_ERR_OUT_OF_LIMITS, "tile size must be positive");
+    if (!(params->tile_origin[0] < params->image_size[0] && params->tile_origin[1] < params->image_size[1]))
+        return noalloc_fail(error, error_size, PT_ERR_INVALID_ARG, "tile origin must be within the image");
+    if (params->max_bounces > PT_MAX_BOUNCES_LIMIT)
+        return noalloc_fail(error, error_size, PT_ERR_INVALID_ARG, "max bounces must be at most 16");
+    const uint32_t vis_w = tile_width < params->image_size[0] - params->tile_origin[0]
+                               ? tile_width : params->image_size[0] - params->tile_origin[0];
+    const uint32_t vis_h = tile_height < params->image_size[1] - params->tile_origin[1]
+                               ? tile_height : params->image_size[1] - params->tile_origin[1];
+    const uint64_t pixels = (uint64_t)vis_w * vis_h;
+    if (pixels * samples > kNoAllocPaths) {
+        char msg[200];
+        snprintf(msg, sizeof msg, "%llu paths (%u x %u visible pixels x %u samples) exceed the %u paths one call can hold",
+                 (unsigned long long)(pixels * samples), vis_w, vis_h, samples, PT_NOALLOC_MAX_PATHS);
+        return noalloc_fail(error, error_size, PT_ERR_OUT_OF_LIMITS, msg);
+    }
+    if (samples == 0) return PT_OK;
+    int dev = 0;
+    int rc = noalloc_cuda(error, error_size, cudaGetDevice(&dev), "cudaGetDevice");
+    if (rc) return rc;
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return noalloc_fail(error, error_size, PT_ERR_OUT_OF_LIMITS, "device index too large");
+    if ((rc = noalloc_setup(dev, error, error_size))) return rc;
+    unsigned char* base = g_noalloc_devices[dev].scratch;
+
+    ptd::World w;
+    w.geo = world->geometries;
+    w.attr = world->attributes;
+    w.mat = world->materials;
+    w.nodes = world->bvh_nodes;
+    w.srgb = world->srgb_texture_atlases;
+    w.linear = world->linear_texture_atlases;
+    w.srgb_count = world->srgb_texture_atlases ? world->srgb_atlas_count : 0u;
+    w.linear_count = world->linear_texture_atlases ? world->linear_atlas_count : 0u;
+    w.sky = reinterpret_cast<const float4*>(world->skybox_rgba);
+    w.sky_alias = world->skybox_aliases;
+    w.scene_alias = world->scene_aliases;
+    w.sky_u = world->skybox_uniforms;
+    w.scene = world->scene_uniforms;
+    w.camera = world->camera;
+    w.srgb_lut = reinterpret_cast<const float*>(base + kNoAllocLutOffset);
+    w.any_alpha = world->any_non_opaque ? 1 : 0;
+
+    ptd::Queues q;
+    float4* slots = reinterpret_cast<float4*>(base);
+    float4* arrays[11];
+    for (int k = 0; k < 11; ++k) arrays[k] = slots + (size_t)k * kNoAllocPaths;
+    q.o[0] = arrays[0];
+    q.o[1] = arrays[1];
+    q.d[0] = arrays[2];
+    q.d[1] = arrays[3];
+    q.T[0] = arrays[4];
+    q.T[1] = arrays[5];
+    q.hit = arrays[6];
+    q.color = arrays[7];
+    q.so = arrays[8];
+    q.sd = arrays[9];
+    q.sc = arrays[10];
+    q.cnt = reinterpret_cast<uint32_t*>(base + kNoAllocCountersOffset);
+    q.rec = nullptr;
+    q.rec_hits = nullptr;
+
+    ptd::Fast f;
+    f.pairs = reinterpret_cast<const float4*>(world->bvh_nodes);  // child pairs read in place
+    f.tri4 = nullptr;                                              // triangles read in the 36-byte layout
+
+    ptk::Tile t;
+    t.image_w = params->image_size[0];
+    t.image_h = params->image_size[1];
+    t.origin_x = params->tile_origin[0];
+    t.origin_y = params->tile_origin[1];
+    t.tile_w = tile_width;
+    t.tile_h = tile_height;
+    t.max_bounces = params->max_bounces;
+    t.accum = reinterpret_cast<float4*>(accum);
+    t.image = reinterpret_cast<float4*>(image);
+
+    ptd::Group g;
+    g.vis_w = vis_w;
+    g.vis_h = vis_h;
+    g.pixels = (uint32_t)pixels;
+    g.samples = samples;
+    g.paths = (uint32_t)(pixels * samples);
+    g.first_sample = params->sample_count + 1u;
+    g.record_sample = 0;
+
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    auto untimed = [](int, auto&& launch) { return launch(); };
+    const cudaError_t e = w.any_alpha
+                              ? ptw::run_group<false, true, true>(g_noalloc_devices[dev].sms, w, f, q, t, g, ptk::Sinks{nullptr, nullptr}, s, untimed)
+                              : ptw::run_group<false, false, true>(g_noalloc_devices[dev].sms, w, f, q, t, g, ptk::Sinks{nullptr, nullptr}, s, untimed);
+    return noalloc_cuda(error, error_size, e, "trace launch");
+}

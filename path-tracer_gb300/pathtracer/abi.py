@@ -147,6 +147,20 @@ class ProceduralParams(C.Structure):
                 ("skybox_height", c_u32), ("skybox_luminance", c_f), ("textured", c_i32), ("non_opaque", c_i32)]
 
 
+class DeviceWorld(C.Structure):
+    """pt_device_world: the world as device buffers owned by the caller."""
+    _fields_ = [("geometries", C.c_void_p), ("attributes", C.c_void_p), ("triangle_count", c_u64),
+                ("materials", C.c_void_p), ("material_count", c_u64), ("bvh_nodes", C.c_void_p),
+                ("node_count", c_u64), ("srgb_texture_atlases", C.c_void_p), ("srgb_atlas_count", c_u32),
+                ("linear_texture_atlases", C.c_void_p), ("linear_atlas_count", c_u32),
+                ("skybox_rgba", C.c_void_p), ("skybox_aliases", C.c_void_p), ("scene_aliases", C.c_void_p),
+                ("camera", Camera), ("scene_uniforms", SceneUniforms), ("skybox_uniforms", SkyboxUniforms),
+                ("any_non_opaque", c_i32)]
+
+
+PT_NOALLOC_MAX_PATHS = 262144
+PT_NOALLOC_SCRATCH_BYTES = 48 << 20
+
 STRUCT_SIZES = {
     TriangleGeometry: 36, TriangleAttribute: 112, BvhNode: 32, Material: 224, Camera: 64,
     SceneUniforms: 16, SceneAliasEntry: 16, SkyboxUniforms: 16, SkyboxAliasEntry: 12,
@@ -179,6 +193,8 @@ SIGNATURES = {
     "pt_trace_recorded": (C.c_int, [_vp, c_u32, P(c_u32), _vp]),
     "pt_trace_counted": (C.c_int, [_vp, c_u32, P(c_u32), P(c_u64)]),
     "pt_debug_intersect": (C.c_int, [_vp, c_u64, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "pt_trace_noalloc": (C.c_int, [P(DeviceWorld), P(TraceParameters), c_u32, c_u32, c_u32, _vp, _vp, _vp,
+                                   C.c_char_p, C.c_size_t]),
     # pt_world.h
     "ptw_create": (C.c_int, [P(_vp)]),
     "ptw_destroy": (None, [_vp]),
