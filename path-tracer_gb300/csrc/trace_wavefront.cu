@@ -67,8 +67,24 @@ PTD Stage stage_of(const Queues& q, int cur) {
     return s;
 }
 
-constexpr int kExtendThreads = 128;
-constexpr int kShadeThreads = 128;
+// launch shapes (overridable at build time for tuning sweeps)
+#ifndef PT_EXTEND_THREADS
+#define PT_EXTEND_THREADS 128
+#endif
+#ifndef PT_EXTEND_MIN_BLOCKS
+#define PT_EXTEND_MIN_BLOCKS 1
+#endif
+#ifndef PT_SHADE_THREADS
+#define PT_SHADE_THREADS 128
+#endif
+#ifndef PT_SHADE_MIN_BLOCKS
+#define PT_SHADE_MIN_BLOCKS 8
+#endif
+#ifndef PT_STEPS_PER_REFILL
+#define PT_STEPS_PER_REFILL 32
+#endif
+constexpr int kExtendThreads = PT_EXTEND_THREADS;
+constexpr int kShadeThreads = PT_SHADE_THREADS;
 
 PTD Tri load_tri4(const Fast& f, uint32_t tri) {
     const float4* p = f.tri4 + 3 * (size_t)tri;
@@ -194,7 +210,7 @@ struct Traverser {
     }
 };
 
-constexpr int kStepsPerRefill = 8;
+constexpr int kStepsPerRefill = PT_STEPS_PER_REFILL;
 
 PTD unsigned lane_id() {
     unsigned l;
@@ -269,7 +285,7 @@ __global__ void bounce_reset_kernel(uint32_t* cnt, int next) {
 // one from the queue (one atomic per warp for all idle lanes) as soon as it
 // finishes, so long and short rays do not leave lanes idle.
 template <bool kRec, bool kAlpha, bool kTri36 = false>
-__global__ void __launch_bounds__(kExtendThreads) extend_kernel(World w, Fast f, Queues q, int cur, uint32_t bounce) {
+__global__ void __launch_bounds__(kExtendThreads, PT_EXTEND_MIN_BLOCKS) extend_kernel(World w, Fast f, Queues q, int cur, uint32_t bounce) {
     const Stage st = stage_of(q, cur);
     const uint32_t count = *st.count;
     const unsigned lane = lane_id();
@@ -321,7 +337,7 @@ __global__ void __launch_bounds__(kExtendThreads) extend_kernel(World w, Fast f,
 }
 
 template <bool kRec, bool kAlpha>
-__global__ void __launch_bounds__(kShadeThreads) shade_kernel(World w, Fast f, Queues q, int cur, uint32_t bounce,
+__global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kernel(World w, Fast f, Queues q, int cur, uint32_t bounce,
                                                               uint32_t max_bounces) {
     const Stage st = stage_of(q, cur);
     const uint32_t count = *st.count;
@@ -383,7 +399,7 @@ __global__ void __launch_bounds__(kShadeThreads) shade_kernel(World w, Fast f, Q
 // Persistent shadow kernel (opaque scenes): any-hit traversal of every queued
 // shadow ray with the same lane refill; unoccluded rays add their light.
 template <bool kRec, bool kTri36 = false>
-__global__ void __launch_bounds__(kExtendThreads) shadow_kernel(World w, Fast f, Queues q) {
+__global__ void __launch_bounds__(kExtendThreads, PT_EXTEND_MIN_BLOCKS) shadow_kernel(World w, Fast f, Queues q) {
     const uint32_t count = q.cnt[2];
     const unsigned lane = lane_id();
     Traverser<kRec, false, true, kTri36> tr;

@@ -36,6 +36,8 @@ NVCC_FLAGS = ARCH + [
     "-Xcudafe", "--diag_suppress=177",
 ]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
+# extra device-compiler flags (e.g. launch-shape -D overrides for tuning sweeps)
+NVCC_FLAGS += os.environ.get("PT_EXTRA_NVCC_FLAGS", "").split()
 
 LIB = OUT / "libpt.so"
 CLI = OUT / "pt-render"
