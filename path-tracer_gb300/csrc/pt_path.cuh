@@ -154,12 +154,11 @@ struct PathState {
 
 // camera ray, trace.slang:736-748; returns the RNG state after the jitter draws
 template <bool kRec>
-PTD void camera_ray(const World& w, uint32_t px, uint32_t py, uint32_t img_w, uint32_t img_h, Rng<kRec>& rng,
-                    PathState& ps) {
+PTD void camera_ray(const pt_camera& cam, uint32_t px, uint32_t py, uint32_t img_w, uint32_t img_h,
+                    Rng<kRec>& rng, PathState& ps) {
     const float jx = rng();
     const float jy = rng();
     const f2 puv = {((float)px + jx) / (float)img_w, ((float)py + jy) / (float)img_h};
-    const pt_camera& cam = w.camera;
     ps.o = mk(cam.position[0], cam.position[1], cam.position[2]);
     const f3 llc = mk(cam.lower_left_corner_minus_position[0], cam.lower_left_corner_minus_position[1],
                       cam.lower_left_corner_minus_position[2]);
@@ -169,6 +168,12 @@ PTD void camera_ray(const World& w, uint32_t px, uint32_t py, uint32_t img_w, ui
     ps.throughput = mk(1.0f, 1.0f, 1.0f);
     ps.color = mk(0.0f, 0.0f, 0.0f);
     ps.prev_pdf = 0.0f;
+}
+
+template <bool kRec>
+PTD void camera_ray(const World& w, uint32_t px, uint32_t py, uint32_t img_w, uint32_t img_h, Rng<kRec>& rng,
+                    PathState& ps) {
+    camera_ray(w.camera, px, py, img_w, img_h, rng, ps);
 }
 
 // escaped ray, trace.slang:887-927

@@ -251,3 +251,44 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         fn.argtypes = args
     _LIB = lib
     return lib
+
+
+# ---------------------------------------------------------------- pt_batch.h
+
+PT_JOB_QUEUED = 0
+PT_JOB_RUNNING = 1
+PT_JOB_DONE = 2
+
+
+class EngineConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("hbm_budget_bytes", c_u64), ("wave_paths", c_u32), ("tile_size", c_u32),
+                ("steps_per_refill", c_u32), ("use_graphs", c_u32)]
+
+
+class JobDesc(C.Structure):
+    _fields_ = [("scene_id", c_u64), ("camera", Camera), ("width", c_u32), ("height", c_u32),
+                ("samples", c_u32), ("max_bounces", c_u32), ("continue_job", c_u64)]
+
+
+class EngineStats(C.Structure):
+    _fields_ = [("waves", c_u64), ("items", c_u64), ("paths", c_u64), ("jobs_submitted", c_u64),
+                ("jobs_done", c_u64), ("scenes_cached", c_u64), ("scene_hits", c_u64), ("scenes_evicted", c_u64),
+                ("hbm_used", c_u64), ("hbm_budget", c_u64), ("gpu_ms", C.c_double), ("wave_paths", c_u32),
+                ("tile_size", c_u32), ("steps_per_refill", c_u32), ("use_graphs", c_u32)]
+
+
+SIGNATURES.update({
+    "pte_create": (C.c_int, [P(EngineConfig), P(_vp)]),
+    "pte_destroy": (None, [_vp]),
+    "pte_last_error": (C.c_char_p, [_vp]),
+    "pte_scene_add": (C.c_int, [_vp, P(WorldUpdates), P(c_u64)]),
+    "pte_scene_release": (C.c_int, [_vp, c_u64]),
+    "pte_submit": (C.c_int, [_vp, P(JobDesc), P(c_u64)]),
+    "pte_poll": (C.c_int, [_vp, c_u32, P(c_u64), c_u32, P(c_u32)]),
+    "pte_wait_idle": (C.c_int, [_vp, c_u32]),
+    "pte_job_status": (C.c_int, [_vp, c_u64, P(C.c_int), P(c_u32)]),
+    "pte_job_read": (C.c_int, [_vp, c_u64, C.c_int, _vp]),
+    "pte_job_release": (C.c_int, [_vp, c_u64]),
+    "pte_stats": (C.c_int, [_vp, P(EngineStats)]),
+    "pte_autotune": (C.c_int, [_vp, P(JobDesc), c_u32, P(EngineConfig)]),
+})

@@ -1,0 +1,87 @@
+"""Python wrapper of the batched render engine (include/pt_batch.h)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import PathTracerError, abi
+from .abi import load
+
+
+class Engine:
+    """Many render jobs of uneven size, samples, depth and scene traced together on one GPU."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, wave_paths: int = 0, tile_size: int = 0,
+                 steps_per_refill: int = 0, use_graphs: bool = True):
+        self._lib = load()
+        cfg = abi.EngineConfig(device, hbm_budget_bytes, wave_paths, tile_size, steps_per_refill, int(use_graphs))
+        h = C.c_void_p()
+        rc = self._lib.pte_create(C.byref(cfg), C.byref(h))
+        if rc != abi.PT_OK:
+            raise PathTracerError(rc, "pte_create failed (see stderr)")
+        self._h = h
+
+    def _check(self, rc: int) -> None:
+        if rc != abi.PT_OK:
+            raise PathTracerError(rc, self._lib.pte_last_error(self._h).decode())
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.pte_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_scene(self, full_updates: abi.WorldUpdates) -> int:
+        sid = C.c_uint64()
+        self._check(self._lib.pte_scene_add(self._h, C.byref(full_updates), C.byref(sid)))
+        return sid.value
+
+    def release_scene(self, scene_id: int) -> None:
+        self._check(self._lib.pte_scene_release(self._h, scene_id))
+
+    def submit(self, scene_id: int, camera: abi.Camera, width: int, height: int, samples: int, max_bounces: int,
+               continue_job: int = 0) -> int:
+        d = abi.JobDesc(scene_id, camera, width, height, samples, max_bounces, continue_job)
+        jid = C.c_uint64()
+        self._check(self._lib.pte_submit(self._h, C.byref(d), C.byref(jid)))
+        return jid.value
+
+    def poll(self, timeout_ms: int = 0, capacity: int = 256) -> list[int]:
+        done = (C.c_uint64 * capacity)()
+        n = C.c_uint32()
+        self._check(self._lib.pte_poll(self._h, timeout_ms, done, capacity, C.byref(n)))
+        return list(done[:n.value])
+
+    def wait_idle(self, timeout_ms: int = 0) -> None:
+        self._check(self._lib.pte_wait_idle(self._h, timeout_ms))
+
+    def status(self, job_id: int) -> tuple[int, int]:
+        st = C.c_int()
+        n = C.c_uint32()
+        self._check(self._lib.pte_job_status(self._h, job_id, C.byref(st), C.byref(n)))
+        return st.value, n.value
+
+    def read(self, job_id: int, width: int, height: int, which: int = abi.PT_TILE_IMAGE) -> np.ndarray:
+        out = np.empty((height, width, 4), dtype=np.float32)
+        self._check(self._lib.pte_job_read(self._h, job_id, which, out.ctypes.data))
+        return out
+
+    def release(self, job_id: int) -> None:
+        self._check(self._lib.pte_job_release(self._h, job_id))
+
+    def stats(self) -> dict:
+        s = abi.EngineStats()
+        self._check(self._lib.pte_stats(self._h, C.byref(s)))
+        return {name: getattr(s, name) for name, _ in abi.EngineStats._fields_}
+
+    def autotune(self, jobs: list[abi.JobDesc]) -> dict:
+        arr = (abi.JobDesc * len(jobs))(*jobs)
+        cfg = abi.EngineConfig()
+        self._check(self._lib.pte_autotune(self._h, arr, len(jobs), C.byref(cfg)))
+        return {name: getattr(cfg, name) for name, _ in abi.EngineConfig._fields_}

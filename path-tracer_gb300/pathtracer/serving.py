@@ -1,0 +1,199 @@
+"""Serving loop over the batched engine: requests arrive as a Poisson stream,
+are admitted into the engine as they arrive (continuous batching: they join
+the next wave while earlier requests are still on the GPU), and the latency
+from arrival to completion is recorded per request.
+
+Request mix (the batching / serving workloads): image side log-uniform in
+[64, 1024] with aspect 1:1 to 16:9, samples in {1, 4, 16, 64}, max_bounces in
+[4, 12], scene drawn from procedural scenes of about 10k, 100k, 1M (and
+optionally 4M) triangles with random camera poses; a fraction of requests
+are progressive refinements that add samples to the resident accumulation of
+an earlier request.  Requests the engine refuses (HBM budget) are counted as
+rejected.
+
+    python -m pathtracer.serving --rate 50 --duration 10
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+import pathtracer as pt
+from pathtracer import abi
+from pathtracer.engine import Engine
+
+# procedural scene parameters for about 10k, 100k, 1M and 4M triangles
+SCENE_SIZES = {
+    "10k": dict(grid_x=48, grid_z=48, boxes=200, spheres=2, sphere_subdivision=3, emissive_triangles=16),
+    "100k": dict(grid_x=160, grid_z=160, boxes=1000, spheres=30, sphere_subdivision=3, emissive_triangles=32),
+    "1M": dict(grid_x=512, grid_z=512, boxes=2000, spheres=90, sphere_subdivision=4, emissive_triangles=64),
+    "4M": dict(grid_x=1024, grid_z=1024, boxes=4000, spheres=360, sphere_subdivision=4, emissive_triangles=64),
+}
+
+
+def build_scene(size: str, seed: int = 7) -> pt.World:
+    return pt.World.procedural(seed=seed, skybox_width=512, skybox_height=256, **SCENE_SIZES[size])
+
+
+@dataclass
+class Request:
+    arrival: float
+    scene: str
+    width: int
+    height: int
+    samples: int
+    max_bounces: int
+    yaw: float
+    pitch: float
+    progressive: bool = False
+
+
+@dataclass
+class ServeResult:
+    latencies_ms: list = field(default_factory=list)
+    latencies_512_16_ms: list = field(default_factory=list)
+    completed: int = 0
+    rejected: int = 0
+    paths: int = 0
+    wall_s: float = 0.0
+
+
+def request_stream(rate: float, duration: float, scenes: list[str], seed: int = 1,
+                   progressive_fraction: float = 0.1, fixed: tuple | None = None) -> list[Request]:
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration:
+            return out
+        if fixed is not None:
+            w, h, spp, depth = fixed
+        else:
+            side = math.exp(rng.uniform(math.log(64), math.log(1024)))
+            aspect = rng.uniform(1.0, 16.0 / 9.0)
+            w, h = max(8, int(side * math.sqrt(aspect))), max(8, int(side / math.sqrt(aspect)))
+            spp = int(rng.choice([1, 4, 16, 64]))
+            depth = int(rng.integers(4, 13))
+        out.append(Request(t, scenes[int(rng.integers(len(scenes)))], w, h, spp, depth,
+                           float(rng.uniform(-0.6, 0.6)), float(rng.uniform(-0.5, -0.2)),
+                           progressive=bool(rng.random() < progressive_fraction)))
+
+
+class Server:
+    """Admission + continuous batching on one engine; scenes cached by content hash."""
+
+    def __init__(self, engine: Engine, worlds: dict[str, pt.World]):
+        self.engine = engine
+        self.worlds = worlds
+        self.full = {name: w.take_updates() for name, w in worlds.items()}
+        self.scene_ids = {name: engine.add_scene(u) for name, u in self.full.items()}
+        self._last = {name: abi.Camera.from_buffer_copy(u.camera.contents) for name, u in self.full.items()}
+
+    def camera(self, name: str, req: Request) -> abi.Camera:
+        w = self.worlds[name]
+        w.set_aspect_ratio(req.width / req.height)
+        w.edit_camera(yaw=req.yaw, pitch=req.pitch)
+        u = w.take_updates()
+        if u.camera:
+            self._last[name] = abi.Camera.from_buffer_copy(u.camera.contents)
+        return abi.Camera.from_buffer_copy(self._last[name])
+
+    def run(self, requests: list[Request], max_outstanding_paths: int = 2_000_000_000) -> ServeResult:
+        eng, res = self.engine, ServeResult()
+        arrival_of, is_512_16, paths_of = {}, {}, {}
+        finished: dict[tuple, list[int]] = {}  # (scene, w, h, depth) -> finished job ids to refine
+        outstanding, i = 0, 0
+        t0 = time.perf_counter()
+        while i < len(requests) or arrival_of:
+            now = time.perf_counter() - t0
+            while i < len(requests) and requests[i].arrival <= now:
+                r = requests[i]
+                i += 1
+                key = (r.scene, r.width, r.height, r.max_bounces)
+                cont = 0
+                if r.progressive and finished.get(key):
+                    cont = finished[key].pop()
+                paths = r.width * r.height * r.samples
+                if outstanding + paths > max_outstanding_paths:
+                    res.rejected += 1
+                    continue
+                try:
+                    jid = eng.submit(self.scene_ids[r.scene], self.camera(r.scene, r), r.width, r.height, r.samples,
+                                     r.max_bounces, continue_job=cont)
+                except pt.PathTracerError:
+                    res.rejected += 1
+                    continue
+                arrival_of[jid] = (r.arrival, key, cont)
+                is_512_16[jid] = (r.width, r.height, r.samples) == (512, 512, 16)
+                paths_of[jid] = paths
+                outstanding += paths
+            for jid in eng.poll(timeout_ms=1):
+                done_at = time.perf_counter() - t0
+                arrival, key, cont = arrival_of.pop(jid)
+                lat = (done_at - arrival) * 1e3
+                res.latencies_ms.append(lat)
+                if is_512_16.pop(jid):
+                    res.latencies_512_16_ms.append(lat)
+                res.completed += 1
+                p = paths_of.pop(jid)
+                res.paths += p
+                outstanding -= p
+                if cont:
+                    eng.release(cont)
+                finished.setdefault(key, []).append(jid)
+                while len(finished[key]) > 4:
+                    eng.release(finished[key].pop(0))
+        res.wall_s = time.perf_counter() - t0
+        for ids in finished.values():
+            for jid in ids:
+                eng.release(jid)
+        return res
+
+
+def percentiles(xs: list) -> dict:
+    if not xs:
+        return {"p50": None, "p99": None, "p999": None, "n": 0}
+    a = np.asarray(xs)
+    return {"p50": float(np.percentile(a, 50)), "p99": float(np.percentile(a, 99)),
+            "p999": float(np.percentile(a, 99.9)), "n": int(a.size)}
+
+
+def main(argv=None) -> None:
+    p = argparse.ArgumentParser()
+    p.add_argument("--rate", type=float, default=50.0, help="mean requests per second")
+    p.add_argument("--duration", type=float, default=10.0, help="seconds of arrivals")
+    p.add_argument("--scenes", default="10k,100k,1M")
+    p.add_argument("--fixed", default="", help="W,H,SPP,DEPTH: every request this shape (e.g. 512,512,16,8)")
+    p.add_argument("--progressive", type=float, default=0.1)
+    p.add_argument("--budget-gb", type=float, default=150.0)
+    p.add_argument("--seed", type=int, default=1)
+    args = p.parse_args(argv)
+    names = args.scenes.split(",")
+    t = time.perf_counter()
+    worlds = {n: build_scene(n) for n in names}
+    build_s = time.perf_counter() - t
+    eng = Engine(hbm_budget_bytes=int(args.budget_gb * (1 << 30)))
+    server = Server(eng, worlds)
+    fixed = tuple(int(x) for x in args.fixed.split(",")) if args.fixed else None
+    reqs = request_stream(args.rate, args.duration, names, args.seed, args.progressive, fixed)
+    res = server.run(reqs)
+    st = eng.stats()
+    print(json.dumps({
+        "rate_req_s": args.rate, "duration_s": args.duration, "requests": len(reqs), "completed": res.completed,
+        "rejected": res.rejected, "latency_ms": percentiles(res.latencies_ms),
+        "latency_512x512x16_ms": percentiles(res.latencies_512_16_ms),
+        "samples_per_s": res.paths / res.wall_s, "wall_s": res.wall_s, "gpu_ms": st["gpu_ms"],
+        "waves": st["waves"], "scene_build_s": build_s,
+        "triangles": {n: worlds[n].triangle_count() for n in names},
+    }))
+    eng.close()
+
+
+if __name__ == "__main__":
+    main()
