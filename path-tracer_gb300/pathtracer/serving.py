@@ -156,6 +156,51 @@ class Server:
         return res
 
 
+def closed_loop(server: Server, requests: list[Request], mode: str) -> dict:
+    """Render every request back to back (arrival times ignored) and return samples per second.
+
+    mode "plain": one job at a time through pt_trace with the plain kernel
+    (one thread per pixel, one launch per sample, at most 16 samples per call,
+    the host waiting for each call) - the reference's dispatch organisation;
+    "wavefront": one job at a time through pt_trace with the wavefront kernels;
+    "engine": all jobs submitted to the batched engine at once.
+    One PathTracer per scene is reused across requests (camera update + set_tile)."""
+    total = sum(r.width * r.height * r.samples for r in requests)
+    if mode == "engine":
+        eng = server.engine
+        t0 = time.perf_counter()
+        ids = [eng.submit(server.scene_ids[r.scene], server.camera(r.scene, r), r.width, r.height, r.samples,
+                          r.max_bounces) for r in requests]
+        eng.wait_idle(timeout_ms=0)
+        dt = time.perf_counter() - t0
+        for j in ids:
+            eng.release(j)
+        return {"mode": mode, "samples": total, "seconds": dt, "samples_per_s": total / dt}
+    kernel = abi.PT_KERNEL_PLAIN if mode == "plain" else abi.PT_KERNEL_WAVEFRONT
+    tracers = {}
+    for name, full in server.full.items():
+        tracers[name] = pt.PathTracer(full, (64, 64))
+        tracers[name].set_kernel(kernel)
+    t0 = time.perf_counter()
+    for r in requests:
+        tr = tracers[r.scene]
+        cam = server.camera(r.scene, r)
+        u = abi.WorldUpdates()
+        u.camera = C.pointer(cam)
+        u.reset_accumulation = 1
+        tr.apply_updates(u)
+        tr.set_max_bounces(r.max_bounces)
+        tr.set_tile((r.width, r.height), (0, 0), (r.width, r.height))
+        left = r.samples
+        while left > 0:
+            left -= tr.trace(left)
+            tr.synchronize()
+    dt = time.perf_counter() - t0
+    for tr in tracers.values():
+        tr.close()
+    return {"mode": mode, "samples": total, "seconds": dt, "samples_per_s": total / dt}
+
+
 def percentiles(xs: list) -> dict:
     if not xs:
         return {"p50": None, "p99": None, "p999": None, "n": 0}
@@ -173,6 +218,9 @@ def main(argv=None) -> None:
     p.add_argument("--progressive", type=float, default=0.1)
     p.add_argument("--budget-gb", type=float, default=150.0)
     p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--compare", type=int, default=0,
+                   help="instead of serving: render this many requests of the mix back to back with the plain "
+                        "kernel, the wavefront kernel (one job per call) and the batched engine")
     args = p.parse_args(argv)
     names = args.scenes.split(",")
     t = time.perf_counter()
@@ -181,6 +229,16 @@ def main(argv=None) -> None:
     eng = Engine(hbm_budget_bytes=int(args.budget_gb * (1 << 30)))
     server = Server(eng, worlds)
     fixed = tuple(int(x) for x in args.fixed.split(",")) if args.fixed else None
+    if args.compare:
+        reqs = request_stream(1000.0, args.compare / 1000.0 * 2.0 + 1.0, names, args.seed, 0.0, fixed)[:args.compare]
+        out = {"requests": len(reqs), "triangles": {n: worlds[n].triangle_count() for n in names}}
+        for mode in ("engine", "wavefront", "plain"):
+            out[mode] = closed_loop(server, reqs, mode)
+        out["engine_over_plain"] = out["engine"]["samples_per_s"] / out["plain"]["samples_per_s"]
+        out["wavefront_over_plain"] = out["wavefront"]["samples_per_s"] / out["plain"]["samples_per_s"]
+        print(json.dumps(out))
+        eng.close()
+        return
     reqs = request_stream(args.rate, args.duration, names, args.seed, args.progressive, fixed)
     res = server.run(reqs)
     st = eng.stats()
