@@ -131,48 +131,26 @@ __global__ void __launch_bounds__(kExtendThreads) extend_kernel(const SceneDev* 
                                                                 uint32_t steps_per_refill) {
     const Stage st = stage_of(b.q, cur);
     const uint32_t count = *st.count;
-    const unsigned lane = lane_id();
     Traverser<false, kAlpha, false> tr;
     uint2 stack[64];
     uint32_t istack[1];
     const SceneDev* sc = scenes;
     uint32_t slot = 0;
-    bool active = false, exhausted = false;
-    for (;;) {
-        if (!exhausted) {
-            const unsigned idle = __ballot_sync(0xffffffffu, !active);
-            if (idle) {
-                const unsigned leader = (unsigned)(__ffs(idle) - 1);
-                uint32_t base = 0;
-                if (lane == leader) base = atomicAdd(&b.q.cnt[3], (uint32_t)__popc(idle));
-                base = __shfl_sync(0xffffffffu, base, leader);
-                if (!active) {
-                    const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
-                    if (i < count) {
-                        slot = i;
-                        const float4 o4 = st.o[i], d4 = st.d[i];
-                        sc = scenes + (b.tag[__float_as_uint(o4.w)] & 0xffu);
-                        tr.rng.s = __float_as_uint(d4.w);
-                        tr.init(sc->f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), kFltMax, -1);
-                        active = true;
-                    }
-                }
-                if (base + (uint32_t)__popc(idle) >= count) exhausted = true;
-            }
-        }
-        if (!__any_sync(0xffffffffu, active)) break;
-        if (active) {
-#pragma unroll 1
-            for (uint32_t k = 0; k < steps_per_refill; ++k) {
-                if (tr.step(sc->w, sc->f, stack, istack)) {
-                    b.q.hit[slot] = make_float4(tr.hit_t, __int_as_float(tr.hit), tr.hv, tr.hw);
-                    if constexpr (kAlpha) st.d[slot].w = __uint_as_float(tr.rng.s);
-                    active = false;
-                    break;
-                }
-            }
-        }
-    }
+    lane_refill_loop(
+        &b.q.cnt[3], count, steps_per_refill, kRefillBelow,
+        [&](uint32_t i) {
+            slot = i;
+            const float4 o4 = st.o[i], d4 = st.d[i];
+            sc = scenes + (b.tag[__float_as_uint(o4.w)] & 0xffu);
+            tr.rng.s = __float_as_uint(d4.w);
+            tr.init(sc->f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), kFltMax, -1);
+        },
+        [&]() {
+            if (!tr.step(sc->w, sc->f, stack, istack)) return false;
+            b.q.hit[slot] = make_float4(tr.hit_t, __int_as_float(tr.hit), tr.hv, tr.hw);
+            if constexpr (kAlpha) st.d[slot].w = __uint_as_float(tr.rng.s);
+            return true;
+        });
 }
 
 template <bool kAlpha>
@@ -237,52 +215,30 @@ __global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kern
 __global__ void __launch_bounds__(kExtendThreads) shadow_kernel(const SceneDev* scenes, WaveBufs b,
                                                                 uint32_t steps_per_refill) {
     const uint32_t count = b.q.cnt[2];
-    const unsigned lane = lane_id();
     Traverser<false, false, true> tr;
     uint2 stack[64];
     uint32_t istack[1];
     const SceneDev* sc = scenes;
     uint32_t path = 0;
     float4 contribution = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    bool active = false, exhausted = false;
-    for (;;) {
-        if (!exhausted) {
-            const unsigned idle = __ballot_sync(0xffffffffu, !active);
-            if (idle) {
-                const unsigned leader = (unsigned)(__ffs(idle) - 1);
-                uint32_t base = 0;
-                if (lane == leader) base = atomicAdd(&b.q.cnt[4], (uint32_t)__popc(idle));
-                base = __shfl_sync(0xffffffffu, base, leader);
-                if (!active) {
-                    const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
-                    if (i < count) {
-                        const float4 o4 = b.q.so[i], d4 = b.q.sd[i];
-                        contribution = b.q.sc[i];
-                        path = __float_as_uint(o4.w);
-                        sc = scenes + (b.tag[path] & 0xffu);
-                        tr.init(sc->f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), d4.w, __float_as_int(contribution.w));
-                        active = true;
-                    }
-                }
-                if (base + (uint32_t)__popc(idle) >= count) exhausted = true;
+    lane_refill_loop(
+        &b.q.cnt[4], count, steps_per_refill, kRefillBelow,
+        [&](uint32_t i) {
+            const float4 o4 = b.q.so[i], d4 = b.q.sd[i];
+            contribution = b.q.sc[i];
+            path = __float_as_uint(o4.w);
+            sc = scenes + (b.tag[path] & 0xffu);
+            tr.init(sc->f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), d4.w, __float_as_int(contribution.w));
+        },
+        [&]() {
+            if (!tr.step(sc->w, sc->f, stack, istack)) return false;
+            if (tr.hit != 1) {
+                const float4 col = b.q.color[path];
+                const f3 sum = mk(col.x, col.y, col.z) + mk(contribution.x, contribution.y, contribution.z);
+                b.q.color[path] = make_float4(sum.x, sum.y, sum.z, 0.0f);
             }
-        }
-        if (!__any_sync(0xffffffffu, active)) break;
-        if (active) {
-#pragma unroll 1
-            for (uint32_t k = 0; k < steps_per_refill; ++k) {
-                if (tr.step(sc->w, sc->f, stack, istack)) {
-                    if (tr.hit != 1) {
-                        const float4 col = b.q.color[path];
-                        const f3 sum = mk(col.x, col.y, col.z) + mk(contribution.x, contribution.y, contribution.z);
-                        b.q.color[path] = make_float4(sum.x, sum.y, sum.z, 0.0f);
-                    }
-                    active = false;
-                    break;
-                }
-            }
-        }
-    }
+            return true;
+        });
 }
 
 // accumulate, trace.slang:1299-1308: one block per item, samples in order;

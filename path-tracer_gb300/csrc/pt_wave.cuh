@@ -68,6 +68,14 @@ PTD Stage stage_of(const Queues& q, int cur) {
 #ifndef PT_STEPS_PER_REFILL
 #define PT_STEPS_PER_REFILL 32
 #endif
+// idle lanes of a traversal warp take new rays once fewer than this many are busy
+#ifndef PT_REFILL_BELOW
+#define PT_REFILL_BELOW 32
+#endif
+// 1: a traversal step tests one triangle of a leaf; 0: a whole leaf
+#ifndef PT_TRI_PER_STEP
+#define PT_TRI_PER_STEP 1
+#endif
 constexpr int kExtendThreads = PT_EXTEND_THREADS;
 constexpr int kShadeThreads = PT_SHADE_THREADS;
 
@@ -99,6 +107,7 @@ struct Traverser {
     float hit_t, hv, hw;
     int32_t hit, light_tri;
     uint32_t lf, tc, sp, idx;
+    uint32_t tri_left;  // triangles of the current leaf still to test (PT_TRI_PER_STEP)
     Rng<kRec> rng;
     Counters c;
     Rec<kRec> rec;
@@ -115,6 +124,7 @@ struct Traverser {
         light_tri = light;
         sp = 0u;
         idx = 0u;
+        tri_left = 0u;
         lf = __float_as_uint(__ldg(&f.pairs[0].w));
         tc = __float_as_uint(__ldg(&f.pairs[1].w));
         if constexpr (kRec) {
@@ -129,6 +139,88 @@ struct Traverser {
         }
     }
 
+    PTD bool pop(uint2* stack, uint32_t* istack) {
+        if (sp == 0u) return true;
+        sp -= 1u;
+        const uint2 e = stack[sp & 63u];
+        lf = e.x;
+        tc = e.y;
+        if constexpr (kRec) idx = istack[sp & 63u];
+        return false;
+    }
+
+    // the watertight test of one triangle against the ray; for kShadow true
+    // when the triangle occludes
+    PTD bool test_triangle(const World& w, const Fast& f, uint32_t tri) {
+        rec.tri();
+        float t, v, wb;
+        Tri tv;
+        if constexpr (kTri36)
+            tv = load_tri(w, tri);  // the caller's 36-byte triangles
+        else
+            tv = load_tri4(f, tri);
+        if (!triangle_test(tv, o, s, &t, &v, &wb)) return false;
+        if (t > 0.0f && t < hit_t) {
+            if constexpr (kAlpha) {
+                if (passes_through(w, tri, v, wb, rng)) return false;
+            }
+            if constexpr (kShadow) {
+                hit = 1;
+                return true;
+            } else {
+                hit_t = t;
+                hit = (int32_t)tri;
+                hv = v;
+                hw = wb;
+            }
+        }
+        return false;
+    }
+
+#if PT_TRI_PER_STEP
+    // one interior node visit or one triangle test; true when the traversal
+    // has finished (for kShadow, hit == 1 marks an occluder).  Testing a
+    // leaf's triangles one per step keeps the two divergent paths of a warp
+    // (box pair vs triangle) about equally long.
+    PTD bool step(const World& w, const Fast& f, uint2* stack, uint32_t* istack) {
+        if (tri_left == 0u) {
+            rec.visit(idx);
+            if (tc == 0u) {
+                rec.interior();
+                const float4* p = f.pairs + 2 * (size_t)lf;
+                const float4 l0 = __ldg(p), l1 = __ldg(p + 1), r0 = __ldg(p + 2), r1 = __ldg(p + 3);
+                const float dl = box_test(l0, l1, nod, rcp, hit_t);
+                const float dr = box_test(r0, r1, nod, rcp, hit_t);
+                const bool hl = dl >= 0.0f, hr = dr >= 0.0f;
+                if (hl || hr) {
+                    const bool go_left = hl && (!hr || dl < dr);
+                    if (hl && hr) {
+                        const float4 f0 = go_left ? r0 : l0, f1 = go_left ? r1 : l1;
+                        stack[sp & 63u] = make_uint2(__float_as_uint(f0.w), __float_as_uint(f1.w));
+                        if constexpr (kRec) istack[sp & 63u] = go_left ? lf + 1u : lf;
+                        sp += 1u;
+                    }
+                    const float4 n0 = go_left ? l0 : r0, n1 = go_left ? l1 : r1;
+                    if constexpr (kRec) idx = go_left ? lf : lf + 1u;
+                    lf = __float_as_uint(n0.w);
+                    tc = __float_as_uint(n1.w);
+                    return false;
+                }
+                return pop(stack, istack);
+            }
+            rec.leaf();
+            tri_left = tc;  // lf walks the leaf's triangles
+        }
+        const uint32_t tri = lf;
+        lf += 1u;
+        tri_left -= 1u;
+        bool skip = false;
+        if constexpr (kShadow) skip = (int32_t)tri == light_tri;
+        if (!skip && test_triangle(w, f, tri)) return true;
+        if (tri_left > 0u) return false;
+        return pop(stack, istack);
+    }
+#else
     // one node visit; true when the traversal has finished (for kShadow,
     // hit == 1 marks an occluder)
     PTD bool step(const World& w, const Fast& f, uint2* stack, uint32_t* istack) {
@@ -185,17 +277,13 @@ struct Traverser {
                 return false;
             }
         }
-        if (sp == 0u) return true;
-        sp -= 1u;
-        const uint2 e = stack[sp & 63u];
-        lf = e.x;
-        tc = e.y;
-        if constexpr (kRec) idx = istack[sp & 63u];
-        return false;
+        return pop(stack, istack);
     }
+#endif
 };
 
 constexpr int kStepsPerRefill = PT_STEPS_PER_REFILL;
+constexpr unsigned kRefillBelow = PT_REFILL_BELOW;
 
 PTD unsigned lane_id() {
     unsigned l;
@@ -213,6 +301,51 @@ PTD uint32_t warp_append(bool want, uint32_t* counter, unsigned mask) {
     if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(ballot));
     base = __shfl_sync(mask, base, leader);
     return want ? base + (uint32_t)__popc(ballot & ((1u << lane) - 1u)) : 0xffffffffu;
+}
+
+// The persistent traversal loop of one warp; every lane holds at most one ray.
+// Each round the warp counts its busy lanes: when fewer than refill_below are
+// busy and the queue still has rays, the idle lanes take the next ones (one
+// atomic per warp, queue slots in lane order).  Busy lanes then advance their
+// ray by up to `steps` traversal steps.  start(i) loads queue entry i into the
+// lane; advance() runs one step and returns true once the ray has finished
+// and its result is written.  A warp leaves only when the queue is exhausted
+// and none of its lanes is busy, so every entry below `count` is traced once.
+template <class Start, class Advance>
+PTD void lane_refill_loop(uint32_t* fetch, uint32_t count, uint32_t steps, unsigned refill_below, Start&& start,
+                          Advance&& advance) {
+    const unsigned lane = lane_id();
+    if (refill_below < 1u) refill_below = 1u;
+    bool active = false, exhausted = false;
+    for (;;) {
+        unsigned busy = __ballot_sync(0xffffffffu, active);
+        if (!exhausted && (unsigned)__popc(busy) < refill_below) {
+            const unsigned idle = ~busy;
+            const unsigned leader = (unsigned)(__ffs(idle) - 1);
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!active) {
+                const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (i < count) {
+                    start(i);
+                    active = true;
+                }
+            }
+            if (base + (uint32_t)__popc(idle) >= count) exhausted = true;
+            busy = __ballot_sync(0xffffffffu, active);
+        }
+        if (busy == 0u) break;  // exhausted: a refill above found nothing left
+        if (active) {
+#pragma unroll 1
+            for (uint32_t k = 0; k < steps; ++k) {
+                if (advance()) {
+                    active = false;
+                    break;
+                }
+            }
+        }
+    }
 }
 
 

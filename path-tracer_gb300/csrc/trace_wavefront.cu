@@ -81,52 +81,30 @@ template <bool kRec, bool kAlpha, bool kTri36 = false>
 __global__ void __launch_bounds__(kExtendThreads, PT_EXTEND_MIN_BLOCKS) extend_kernel(World w, Fast f, Queues q, int cur, uint32_t bounce) {
     const Stage st = stage_of(q, cur);
     const uint32_t count = *st.count;
-    const unsigned lane = lane_id();
     Traverser<kRec, kAlpha, false, kTri36> tr;
     uint2 stack[64];
     uint32_t istack[kRec ? 64 : 1];
     uint32_t slot = 0, path = 0;
-    bool active = false, exhausted = false;
-    for (;;) {
-        if (!exhausted) {
-            const unsigned idle = __ballot_sync(0xffffffffu, !active);
-            if (idle) {
-                const unsigned leader = (unsigned)(__ffs(idle) - 1);
-                uint32_t base = 0;
-                if (lane == leader) base = atomicAdd(&q.cnt[3], (uint32_t)__popc(idle));
-                base = __shfl_sync(0xffffffffu, base, leader);
-                if (!active) {
-                    const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
-                    if (i < count) {
-                        slot = i;
-                        const float4 o4 = st.o[i], d4 = st.d[i];
-                        path = __float_as_uint(o4.w);
-                        tr.rng.s = __float_as_uint(d4.w);
-                        if constexpr (kRec) tr.c = q.rec[path];
-                        tr.init(f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), kFltMax, -1);
-                        active = true;
-                    }
-                }
-                if (base + (uint32_t)__popc(idle) >= count) exhausted = true;
+    lane_refill_loop(
+        &q.cnt[3], count, kStepsPerRefill, kRefillBelow,
+        [&](uint32_t i) {
+            slot = i;
+            const float4 o4 = st.o[i], d4 = st.d[i];
+            path = __float_as_uint(o4.w);
+            tr.rng.s = __float_as_uint(d4.w);
+            if constexpr (kRec) tr.c = q.rec[path];
+            tr.init(f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), kFltMax, -1);
+        },
+        [&]() {
+            if (!tr.step(w, f, stack, istack)) return false;
+            q.hit[slot] = make_float4(tr.hit_t, __int_as_float(tr.hit), tr.hv, tr.hw);
+            if constexpr (kAlpha) st.d[slot].w = __uint_as_float(tr.rng.s);
+            if constexpr (kRec) {
+                q.rec[path] = tr.c;
+                if (bounce < PT_RECORD_MAX_BOUNCES) q.rec_hits[(size_t)path * PT_RECORD_MAX_BOUNCES + bounce] = tr.hit;
             }
-        }
-        if (!__any_sync(0xffffffffu, active)) break;
-        if (active) {
-#pragma unroll 1
-            for (int k = 0; k < kStepsPerRefill; ++k) {
-                if (tr.step(w, f, stack, istack)) {
-                    q.hit[slot] = make_float4(tr.hit_t, __int_as_float(tr.hit), tr.hv, tr.hw);
-                    if constexpr (kAlpha) st.d[slot].w = __uint_as_float(tr.rng.s);
-                    if constexpr (kRec) {
-                        q.rec[path] = tr.c;
-                        if (bounce < PT_RECORD_MAX_BOUNCES) q.rec_hits[(size_t)path * PT_RECORD_MAX_BOUNCES + bounce] = tr.hit;
-                    }
-                    active = false;
-                    break;
-                }
-            }
-        }
-    }
+            return true;
+        });
 }
 
 template <bool kRec, bool kAlpha>
@@ -194,52 +172,30 @@ __global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kern
 template <bool kRec, bool kTri36 = false>
 __global__ void __launch_bounds__(kExtendThreads, PT_EXTEND_MIN_BLOCKS) shadow_kernel(World w, Fast f, Queues q) {
     const uint32_t count = q.cnt[2];
-    const unsigned lane = lane_id();
     Traverser<kRec, false, true, kTri36> tr;
     uint2 stack[64];
     uint32_t istack[kRec ? 64 : 1];
     uint32_t path = 0;
     float4 contribution = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    bool active = false, exhausted = false;
-    for (;;) {
-        if (!exhausted) {
-            const unsigned idle = __ballot_sync(0xffffffffu, !active);
-            if (idle) {
-                const unsigned leader = (unsigned)(__ffs(idle) - 1);
-                uint32_t base = 0;
-                if (lane == leader) base = atomicAdd(&q.cnt[4], (uint32_t)__popc(idle));
-                base = __shfl_sync(0xffffffffu, base, leader);
-                if (!active) {
-                    const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
-                    if (i < count) {
-                        const float4 o4 = q.so[i], d4 = q.sd[i];
-                        contribution = q.sc[i];
-                        path = __float_as_uint(o4.w);
-                        if constexpr (kRec) tr.c = q.rec[path];
-                        tr.init(f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), d4.w, __float_as_int(contribution.w));
-                        active = true;
-                    }
-                }
-                if (base + (uint32_t)__popc(idle) >= count) exhausted = true;
+    lane_refill_loop(
+        &q.cnt[4], count, kStepsPerRefill, kRefillBelow,
+        [&](uint32_t i) {
+            const float4 o4 = q.so[i], d4 = q.sd[i];
+            contribution = q.sc[i];
+            path = __float_as_uint(o4.w);
+            if constexpr (kRec) tr.c = q.rec[path];
+            tr.init(f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), d4.w, __float_as_int(contribution.w));
+        },
+        [&]() {
+            if (!tr.step(w, f, stack, istack)) return false;
+            if (tr.hit != 1) {
+                const float4 col = q.color[path];
+                const f3 sum = mk(col.x, col.y, col.z) + mk(contribution.x, contribution.y, contribution.z);
+                q.color[path] = make_float4(sum.x, sum.y, sum.z, 0.0f);
             }
-        }
-        if (!__any_sync(0xffffffffu, active)) break;
-        if (active) {
-#pragma unroll 1
-            for (int k = 0; k < kStepsPerRefill; ++k) {
-                if (tr.step(w, f, stack, istack)) {
-                    if (tr.hit != 1) {
-                        const float4 col = q.color[path];
-                        const f3 sum = mk(col.x, col.y, col.z) + mk(contribution.x, contribution.y, contribution.z);
-                        q.color[path] = make_float4(sum.x, sum.y, sum.z, 0.0f);
-                    }
-                    if constexpr (kRec) q.rec[path] = tr.c;
-                    active = false;
-                    break;
-                }
-            }
-        }
-    }
+            if constexpr (kRec) q.rec[path] = tr.c;
+            return true;
+        });
 }
 
 // accumulate, trace.slang:1299-1308, samples of the group in order
