@@ -53,7 +53,13 @@ def parse_args():
     p.add_argument("--spp", type=int, default=SPP, help="samples per pixel of one step")
     p.add_argument("--profile-run", action="store_true",
                    help="only the timed steps (no counting pass, e2e or CPU baseline): for ncu captures")
-    return p.parse_args()
+    p.add_argument("--image", type=int, nargs=2, metavar=("W", "H"), default=None,
+                   help="image size (default 1920 1080); smaller sizes are for ncu captures, not bench lines")
+    args = p.parse_args()
+    if args.image:
+        global WIDTH, HEIGHT
+        WIDTH, HEIGHT = args.image
+    return args
 
 
 def dist_env():
@@ -63,7 +69,7 @@ def dist_env():
 def workload_config(world, kernel: str) -> dict:
     return {
         "workload": "procedural scene (1024x512-quad heightfield + 2000 boxes + 200 icospheres s4 + 64 emissive "
-                    "triangles, 1024x512 sky), 1920x1080, 64 spp, max_bounces 8, one image per step",
+                    f"triangles, 1024x512 sky), {WIDTH}x{HEIGHT}, {SPP} spp, max_bounces 8, one image per step",
         "triangles": int(world.triangle_count()),
         "bvh_nodes": int(world.node_count()),
         "image": [WIDTH, HEIGHT],
@@ -215,7 +221,7 @@ def oracle_sample(updates, seconds: float, threads: int = 0):
     n_px = max(64, int(want_rays / max(rays_per_px, 1.0)))
     stride = max(1, int(math.sqrt(WIDTH * HEIGHT / n_px)))
     rays, dt, npx = run(stride, SPP)
-    desc = f"every {stride}th pixel in x and y ({npx} pixels) x {SPP} spp of the 1920x1080 image, {threads} threads"
+    desc = f"every {stride}th pixel in x and y ({npx} pixels) x {SPP} spp of the {WIDTH}x{HEIGHT} image, {threads} threads"
     return rays / dt / 1e6, threads, desc, dt
 
 

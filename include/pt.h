@@ -337,7 +337,9 @@ int pt_trace_recorded(pt_ctx* ctx, uint32_t sample_count, uint32_t* traced,
 /* Closest-hit traversal (trace.slang:764-884) of n opaque rays given on the
  * host: origins and directions are 3 floats each, t_max the initial hit_t.
  * Writes the hit triangle (-1 = miss), the hit t, and the record fields
- * visit_hash, interior_visits, leaf_visits, triangle_tests of each ray. */
+ * visit_hash, interior_visits, leaf_visits, triangle_tests of each ray.
+ * With PT_PRECISION_WIDE_BVH selected (include/pt_precision.h), an opaque
+ * world and records == NULL, the rays traverse the 8-wide BVH instead. */
 int pt_debug_intersect(pt_ctx* ctx, uint64_t n, const float* origins, const float* directions,
                        const float* t_max, int32_t* hit, float* hit_t, pt_path_record* records);
 

@@ -126,6 +126,13 @@ uint64_t ptw_build_bvh(const pt_triangle_geometry* triangles, uint64_t count,
  * 17, 12, 4), OpenPBR base-only diffuse materials, black skybox. */
 int ptw_scene_cornell_box(ptw_world** out);
 
+/* The same room as eight meshes (floor, ceiling, back, left, right, short
+ * box, tall box, lamp) with procedural 1024 x 1024 RGBA8 base-colour
+ * textures on four of them (floor and short box: checkers; back wall and
+ * tall box: value noise), packed into one sRGB atlas layer: the precision
+ * workload. */
+int ptw_scene_cornell_box_textured(uint64_t seed, ptw_world** out);
+
 typedef struct ptw_procedural_params {
     uint64_t seed;
     uint32_t grid_x, grid_z;       /* heightfield quads (2 triangles each) */
@@ -135,8 +142,10 @@ typedef struct ptw_procedural_params {
     uint32_t emissive_triangles;   /* small emissive triangles added on top */
     uint32_t skybox_width, skybox_height; /* 0 = black skybox */
     float skybox_luminance;        /* average luminance after normalisation */
-    int32_t textured;              /* 1: procedural RGBA8 textures on 50% of meshes */
-    int32_t non_opaque;            /* 1: some meshes use ALPHA_MODE_MASK / BLEND */
+    int32_t textured;              /* 1: 1024^2 RGBA8 checker / noise base-colour textures on
+                                      about half of the meshes (64 per sRGB atlas layer)   */
+    int32_t non_opaque;            /* 1: about 10% of boxes and spheres ALPHA_MODE_BLEND
+                                      with alpha in [0.3, 0.9]                              */
 } ptw_procedural_params;
 
 /* defaults of the large scene: 1024 x 512-quad heightfield with 4-octave

@@ -124,6 +124,8 @@ __global__ void reset_kernel(uint32_t* cnt, int next) {
     cnt[2] = 0u;
     cnt[3] = 0u;
     cnt[4] = 0u;
+    cnt[5] = 0u;
+    cnt[6] = 0u;
 }
 
 template <bool kAlpha>
@@ -136,6 +138,8 @@ __global__ void __launch_bounds__(kExtendThreads) extend_kernel(const SceneDev* 
     uint32_t istack[1];
     const SceneDev* sc = scenes;
     uint32_t slot = 0;
+    __shared__ FilerSlots<kExtendThreads> filer_slots;
+    ResultFiler filer = filer_slots.of_warp(lane_id());
     lane_refill_loop(
         &b.q.cnt[3], count, steps_per_refill, kRefillBelow,
         [&](uint32_t i) {
@@ -149,8 +153,10 @@ __global__ void __launch_bounds__(kExtendThreads) extend_kernel(const SceneDev* 
             if (!tr.step(sc->w, sc->f, stack, istack)) return false;
             b.q.hit[slot] = make_float4(tr.hit_t, __int_as_float(tr.hit), tr.hv, tr.hw);
             if constexpr (kAlpha) st.d[slot].w = __uint_as_float(tr.rng.s);
+            filer.file(slot, tr.hit != -1);
             return true;
-        });
+        },
+        [&]() { filer.flush(b.q, lane_id()); });
 }
 
 template <bool kAlpha>
@@ -158,18 +164,19 @@ __global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kern
                                                                                    const JobDev* jobs, WaveBufs b,
                                                                                    int cur, uint32_t bounce) {
     const Stage st = stage_of(b.q, cur);
-    const uint32_t count = *st.count;
+    const ShadeRange range(b.q.cnt);
+    const uint32_t count = range.count();
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     const unsigned lane = lane_id();
     for (uint32_t base = warp * 32u; base < count; base += warps * 32u) {
-        const uint32_t i = base + lane;
+        const uint32_t i = range.slot(b.q, base + lane);
         bool cont = false;
         ShadowRay sr;
         sr.valid = false;
         PathState ps;
         uint32_t p = 0, rs = 0;
-        if (i < count) {
+        if (i != 0xffffffffu) {
             const float4 o4 = st.o[i], d4 = st.d[i], t4 = st.T[i], h4 = b.q.hit[i];
             p = __float_as_uint(o4.w);
             const uint32_t tag = b.tag[p];
@@ -436,7 +443,7 @@ struct pt_engine {
 namespace {
 
 uint64_t wave_bytes(uint32_t paths) {
-    return (uint64_t)paths * (11 * 16 + 4) + 2ull * (paths / 64 + 2) * 4 + 4096;
+    return (uint64_t)paths * (11 * 16 + 4 + 8) + 2ull * (paths / 64 + 2) * 4 + 4096;
 }
 
 void drop_graphs(pt_engine* e) {
@@ -462,6 +469,7 @@ int setup_wave(pt_engine* e) {
     int rc = PT_OK;
     for (int k = 0; k < 11 && !rc; ++k) rc = e->cuda(e->wave[k].alloc((size_t)W * 16), "wave buffers");
     if (!rc) rc = e->cuda(e->wave[11].alloc(64), "wave counters");
+    if (!rc) rc = e->cuda(e->wave[12].alloc((size_t)W * 8), "wave hit and miss lists");
     if (!rc) rc = e->cuda(e->d_tag.alloc((size_t)W * 4), "wave buffers");
     if (!rc) rc = e->cuda(e->d_wave_item.alloc((size_t)(e->max_items + 1) * 4), "wave buffers");
     if (!rc) rc = e->cuda(e->d_wave_off.alloc((size_t)(e->max_items + 1) * 4), "wave buffers");
@@ -479,6 +487,8 @@ int setup_wave(pt_engine* e) {
     q.sd = e->wave[9].as<float4>();
     q.sc = e->wave[10].as<float4>();
     q.cnt = e->wave[11].as<uint32_t>();
+    q.hit_list = e->wave[12].as<uint32_t>();
+    q.miss_list = q.hit_list + W;
     q.rec = nullptr;
     q.rec_hits = nullptr;
     e->wb.tag = e->d_tag.as<uint32_t>();

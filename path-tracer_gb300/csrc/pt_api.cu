@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/pt.h"
+#include "../../include/pt_precision.h"
 #include "pt_kernels.h"
 #include "pt_wavefront.h"
 
@@ -70,9 +71,12 @@ struct pt_ctx {
 
     // tile (bind group 0)
     DevBuf accum, image, display, records, totals;
+    DevBuf comp;  // Kahan compensation (PT_PRECISION_KAHAN)
     uint32_t tile_w = 0, tile_h = 0;
     pt_trace_parameters params{};
     int kernel = PT_KERNEL_WAVEFRONT;
+    uint32_t precision = PT_PRECISION_FP32;         // requested form
+    uint32_t precision_active = PT_PRECISION_FP32;  // form of the last trace
     ptw::Wavefront* wavefront = nullptr;
 
     // instrumentation
@@ -298,6 +302,7 @@ int apply(pt_ctx* c, const pt_world_updates* u, bool initial) {
         if ((rc = copy_to(c, c->sky_alias, k->alias_table, k->alias_count * sizeof(pt_skybox_alias_entry), "skybox aliases"))) return rc;
         c->sky_alias_count = k->alias_count;
         c->sky_u = k->uniforms;
+        if (c->wavefront) ptw::sky_changed(c->wavefront);
     }
     if (u->camera) c->camera = *u->camera;
     for (uint64_t i = 0; i < u->material_update_count; ++i) {
@@ -335,6 +340,10 @@ int alloc_tile(pt_ctx* c, uint32_t w, uint32_t h) {
     if (!rc) rc = c->cuda(c->image.reserve(bytes), "storage texture");
     if (!rc) rc = c->cuda(cudaMemsetAsync(c->accum.p, 0, bytes, c->stream), "clear tile");
     if (!rc) rc = c->cuda(cudaMemsetAsync(c->image.p, 0, bytes, c->stream), "clear tile");
+    if (!rc && (c->precision & PT_PRECISION_KAHAN)) {
+        rc = c->cuda(c->comp.reserve(bytes), "Kahan compensation");
+        if (!rc) rc = c->cuda(cudaMemsetAsync(c->comp.p, 0, bytes, c->stream), "clear tile");
+    }
     if (rc) return rc;
     c->tile_w = w;
     c->tile_h = h;
@@ -352,6 +361,7 @@ ptk::Tile tile_of(const pt_ctx* c) {
     t.max_bounces = c->params.max_bounces;
     t.accum = c->accum.as<float4>();
     t.image = c->image.as<float4>();
+    t.comp = (c->precision & PT_PRECISION_KAHAN) ? c->comp.as<float4>() : nullptr;
     return t;
 }
 
@@ -387,10 +397,15 @@ int trace_impl(pt_ctx* c, uint32_t samples, uint32_t* traced, pt_path_record* ho
         }
     } else {
         if (!c->wavefront) ptw::create(&c->wavefront);
-        if ((rc = c->cuda(ptw::prepare(c->wavefront, w, c->node_count, c->tri_count, c->stream), "wavefront layouts"))) return rc;
+        const bool record = rec != nullptr || tot != nullptr;
+        const uint32_t form = ptw::effective_precision(w, c->precision, record);
+        if ((rc = c->cuda(ptw::prepare(c->wavefront, w, c->node_count, c->tri_count, form, c->stream), "wavefront layouts")))
+            return rc;
         const ptw::Timer timer = [c](int cls, const std::function<cudaError_t()>& f) { return c->timed(cls, f); };
-        rc = c->cuda(ptw::trace(c->wavefront, w, t, first, n, ptk::Sinks{rec, tot}, c->stream, timer), "wavefront trace");
+        rc = c->cuda(ptw::trace(c->wavefront, w, t, first, n, ptk::Sinks{rec, tot}, c->stream, timer, form),
+                     "wavefront trace");
         if (rc) return rc;
+        c->precision_active = form;
     }
     c->params.sample_count += n;
     if (traced) *traced = n;
@@ -454,7 +469,7 @@ void pt_destroy(pt_ctx* c) {
     for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
     if (c->wavefront) ptw::destroy(c->wavefront);
     for (DevBuf* b : {&c->geo, &c->attr, &c->mat, &c->nodes, &c->srgb, &c->linear, &c->sky, &c->sky_alias,
-                      &c->scene_alias, &c->srgb_lut, &c->accum, &c->image, &c->display, &c->records, &c->totals})
+                      &c->scene_alias, &c->srgb_lut, &c->accum, &c->image, &c->comp, &c->display, &c->records, &c->totals})
         b->release();
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -515,9 +530,14 @@ int pt_trace_recorded(pt_ctx* c, uint32_t samples, uint32_t* traced, pt_path_rec
 }
 
 int pt_read_tile(pt_ctx* c, int which, float* host_rgba) {
-    if (!c || !host_rgba || (which != PT_TILE_IMAGE && which != PT_TILE_ACCUMULATION)) return PT_ERR_INVALID_ARG;
+    if (!c || !host_rgba || (which != PT_TILE_IMAGE && which != PT_TILE_ACCUMULATION && which != PT_TILE_COMPENSATION))
+        return PT_ERR_INVALID_ARG;
     cudaSetDevice(c->device);
-    const DevBuf& b = which == PT_TILE_IMAGE ? c->image : c->accum;
+    if (which == PT_TILE_COMPENSATION && !(c->precision & PT_PRECISION_KAHAN)) {
+        std::memset(host_rgba, 0, (size_t)c->tile_w * c->tile_h * 16);
+        return PT_OK;
+    }
+    const DevBuf& b = which == PT_TILE_IMAGE ? c->image : (which == PT_TILE_ACCUMULATION ? c->accum : c->comp);
     int rc = c->cuda(cudaMemcpyAsync(host_rgba, b.p, (size_t)c->tile_w * c->tile_h * 16, cudaMemcpyDeviceToHost, c->stream),
                      "tile readback");
     if (!rc) rc = c->cuda(cudaStreamSynchronize(c->stream), "tile readback");
@@ -556,9 +576,31 @@ const char* pt_last_error(const pt_ctx* c) { return c ? c->error.c_str() : "null
 int pt_set_kernel(pt_ctx* c, int kernel) {
     if (!c) return PT_ERR_INVALID_ARG;
     if (kernel != PT_KERNEL_WAVEFRONT && kernel != PT_KERNEL_PLAIN) return c->fail(PT_ERR_INVALID_ARG, "unknown kernel");
+    if (kernel == PT_KERNEL_PLAIN && c->precision != PT_PRECISION_FP32)
+        return c->fail(PT_ERR_STATE, "the precision form runs on the wavefront kernels");
     c->kernel = kernel;
     return PT_OK;
 }
+
+int pt_set_precision(pt_ctx* c, uint32_t flags) {
+    if (!c) return PT_ERR_INVALID_ARG;
+    if (flags & ~PT_PRECISION_COMPRESSED) return c->fail(PT_ERR_INVALID_ARG, "unknown precision bits");
+    if (flags != PT_PRECISION_FP32 && c->kernel != PT_KERNEL_WAVEFRONT)
+        return c->fail(PT_ERR_STATE, "the precision form runs on the wavefront kernels");
+    cudaSetDevice(c->device);
+    c->precision = flags;
+    if ((flags & PT_PRECISION_KAHAN) && c->tile_w) {
+        const size_t bytes = (size_t)c->tile_w * c->tile_h * 16;
+        int rc = c->cuda(c->comp.reserve(bytes), "Kahan compensation");
+        if (!rc) rc = c->cuda(cudaMemsetAsync(c->comp.p, 0, bytes, c->stream), "clear tile");
+        if (rc) return rc;
+    }
+    c->params.sample_count = 0;
+    return PT_OK;
+}
+
+uint32_t pt_precision(const pt_ctx* c) { return c ? c->precision : 0u; }
+uint32_t pt_precision_active(const pt_ctx* c) { return c ? c->precision_active : 0u; }
 
 int pt_get_stream(pt_ctx* c, void** stream) {
     if (!c || !stream) return PT_ERR_INVALID_ARG;
@@ -609,9 +651,19 @@ int pt_debug_intersect(pt_ctx* c, uint64_t n, const float* origins, const float*
     if (!rc) rc = c->cuda(h.reserve(n * 4), "hits");
     if (!rc) rc = c->cuda(ht.reserve(n * 4), "hits");
     if (!rc && records) rc = c->cuda(rec.reserve(n * sizeof(pt_path_record)), "records");
+    const ptd::World w = c->view();
+    const bool wide = (ptw::effective_precision(w, c->precision, records != nullptr) & PT_PRECISION_WIDE_BVH) != 0;
+    if (!rc && wide) {
+        if (!c->wavefront) ptw::create(&c->wavefront);
+        rc = c->cuda(ptw::prepare(c->wavefront, w, c->node_count, c->tri_count, PT_PRECISION_WIDE_BVH, c->stream),
+                     "wide BVH");
+    }
     if (!rc)
         rc = c->cuda(c->timed(PT_KC_EXTEND, [&] {
-            return ptk::launch_debug_intersect(c->view(), n, o.as<float>(), d.as<float>(), tm.as<float>(), h.as<int32_t>(),
+            if (wide)
+                return ptw::debug_intersect_wide(c->wavefront, w, n, o.as<float>(), d.as<float>(), tm.as<float>(),
+                                                 h.as<int32_t>(), ht.as<float>(), c->stream);
+            return ptk::launch_debug_intersect(w, n, o.as<float>(), d.as<float>(), tm.as<float>(), h.as<int32_t>(),
                                                ht.as<float>(), records ? rec.as<pt_path_record>() : nullptr, c->stream);
         }), "debug intersect");
     if (!rc) rc = c->cuda(cudaMemcpyAsync(hit, h.p, n * 4, cudaMemcpyDeviceToHost, c->stream), "hits");

@@ -12,6 +12,9 @@
 
 #include <stdint.h>
 
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include "../../include/pt.h"
 #include "pt_fmath.h"
 
@@ -99,6 +102,9 @@ struct World {
     pt_camera camera;
     const float* srgb_lut;  // sRGB EOTF per byte (Rgba8UnormSrgb decode), 256 floats
     int any_alpha;          // some material is not opaque
+    // compressed copies (precision form); null: read attr / sky
+    const uint2* attr_h = nullptr;  // pt_half_attribute records, 8 x uint2 each
+    const uint2* sky_h = nullptr;   // skybox texels as BF16 RGBA
 };
 
 // per-path instrumentation (pt_path_record) kept in registers while tracing
@@ -209,7 +215,13 @@ PTD uint32_t sky_index(float f, uint32_t n, int off) {
     return (uint32_t)i;
 }
 PTD f3 sky_px(const World& w, uint32_t ix, uint32_t iy) {
-    const float4 p = __ldg(w.sky + (uint64_t)iy * w.sky_u.width + ix);
+    const uint64_t i = (uint64_t)iy * w.sky_u.width + ix;
+    if (w.sky_h) {
+        const uint2 p = __ldg(w.sky_h + i);
+        const __nv_bfloat162 rg = *reinterpret_cast<const __nv_bfloat162*>(&p.x);
+        return mk(__low2float(rg), __high2float(rg), __bfloat162float(__ushort_as_bfloat16((unsigned short)(p.y & 0xffffu))));
+    }
+    const float4 p = __ldg(w.sky + i);
     return mk(p.x, p.y, p.z);
 }
 PTD f3 skybox_bilinear(const World& w, f2 uv) {
@@ -287,8 +299,46 @@ PTD float power_heuristic(float pdf, float other) {
     return p * p / (p * p + q * q);
 }
 
-PTD f2 interp_uv(const pt_triangle_attribute& a, float u, float v, float w2) {
-    return {fract(u * a.uv0[0] + v * a.uv1[0] + w2 * a.uv2[0]), fract(u * a.uv0[1] + v * a.uv1[1] + w2 * a.uv2[1])};
+// Triangle attributes (TriangleAttribute, trace.slang:57-66) from the FP32
+// records, or from the FP16 records of the precision form (pt_half_attribute:
+// n0..n2 at uint2 0..2, t0..t2 at 3..5, uv0..uv2 in words 12..14, material
+// in word 15).
+PTD f3 half3_of(uint2 p) {
+    const __half2 a = *reinterpret_cast<const __half2*>(&p.x);
+    return mk(__low2float(a), __high2float(a), __half2float(__ushort_as_half((unsigned short)(p.y & 0xffffu))));
+}
+PTD uint32_t attr_material(const World& w, uint32_t tri) {
+    if (w.attr_h) return __ldg(reinterpret_cast<const uint32_t*>(w.attr_h + 8 * (size_t)tri) + 15);
+    return __ldg(&w.attr[tri].material_index);
+}
+PTD f3 attr_normal(const World& w, uint32_t tri, int k) {
+    if (w.attr_h) return half3_of(__ldg(w.attr_h + 8 * (size_t)tri + k));
+    const float* n = k == 0 ? w.attr[tri].n0 : (k == 1 ? w.attr[tri].n1 : w.attr[tri].n2);
+    return mk(__ldg(n), __ldg(n + 1), __ldg(n + 2));
+}
+// xyz of tangent k; w of tangent 0 through attr_tangent0_w
+PTD f3 attr_tangent(const World& w, uint32_t tri, int k) {
+    if (w.attr_h) return half3_of(__ldg(w.attr_h + 8 * (size_t)tri + 3 + k));
+    const float* t = k == 0 ? w.attr[tri].t0 : (k == 1 ? w.attr[tri].t1 : w.attr[tri].t2);
+    return mk(__ldg(t), __ldg(t + 1), __ldg(t + 2));
+}
+PTD float attr_tangent0_w(const World& w, uint32_t tri) {
+    if (w.attr_h) return __half2float(__ushort_as_half((unsigned short)(__ldg(&w.attr_h[8 * (size_t)tri + 3].y) >> 16)));
+    return __ldg(&w.attr[tri].t0[3]);
+}
+PTD f2 attr_uv(const World& w, uint32_t tri, int k) {
+    if (w.attr_h) {
+        const uint32_t bits = __ldg(reinterpret_cast<const uint32_t*>(w.attr_h + 8 * (size_t)tri) + 12 + k);
+        const __half2 a = *reinterpret_cast<const __half2*>(&bits);
+        return {__low2float(a), __high2float(a)};
+    }
+    const float* uv = k == 0 ? w.attr[tri].uv0 : (k == 1 ? w.attr[tri].uv1 : w.attr[tri].uv2);
+    return {__ldg(uv), __ldg(uv + 1)};
+}
+
+PTD f2 interp_uv(const World& w, uint32_t tri, float u, float v, float w2) {
+    const f2 a = attr_uv(w, tri, 0), b = attr_uv(w, tri, 1), c = attr_uv(w, tri, 2);
+    return {fract(u * a.x + v * b.x + w2 * c.x), fract(u * a.y + v * b.y + w2 * c.y)};
 }
 
 // coverage, trace.slang:426-443
@@ -303,10 +353,9 @@ PTD float coverage(const World& w, const pt_material& m, f2 uv) {
 // passes_through, trace.slang:446-454
 template <bool kRec>
 PTD bool passes_through(const World& w, uint32_t tri, float v, float w2, Rng<kRec>& rng) {
-    const pt_triangle_attribute& attr = w.attr[tri];
-    const pt_material& m = w.mat[attr.material_index];
+    const pt_material& m = w.mat[attr_material(w, tri)];
     if (m.alpha_mode == PT_ALPHA_MODE_OPAQUE) return false;
-    const f2 uv = interp_uv(attr, 1.0f - v - w2, v, w2);
+    const f2 uv = interp_uv(w, tri, 1.0f - v - w2, v, w2);
     return coverage(w, m, uv) <= rng();
 }
 
@@ -408,9 +457,8 @@ PTD LightSample sample_light(const World& w, f3 origin, Rng<kRec>& rng, Counters
         r.direction = delta / r.distance;
         r.triangle_index = (int32_t)entry.triangle_index;
         r.pdf = triangle_light_pdf(w, entry.triangle_index, r.direction, d2, p0 * entry.selection_probability);
-        const pt_triangle_attribute& attr = w.attr[entry.triangle_index];
-        const f2 uv = interp_uv(attr, u, v, wb);
-        const pt_material& m = w.mat[attr.material_index];
+        const f2 uv = interp_uv(w, entry.triangle_index, u, v, wb);
+        const pt_material& m = w.mat[attr_material(w, entry.triangle_index)];
         r.emission = coverage(w, m, uv) * evaluate_emission(w, m, uv);
     } else {
         if (kRec) c->sky_light_samples += 1;

@@ -16,6 +16,7 @@ struct Tile {
     uint32_t max_bounces;
     float4* accum;  // tile_w * tile_h running sums (w = 1)
     float4* image;  // tile_w * tile_h EXPOSURE * sum / n (alpha 1)
+    float4* comp = nullptr;  // Kahan compensation of accum (precision form); null: plain sums
 };
 
 // plain kernel: one thread per tile pixel, one launch per sample

@@ -202,10 +202,9 @@ struct ShadowRay {
 template <bool kRec, bool kInlineShadow>
 PTD bool shade_hit(const World& w, uint32_t bounce, uint32_t max_bounces, PathState& ps, float hit_t, uint32_t h,
                    float hv, float hw, Rng<kRec>& rng, Counters* c, ShadowRay* shadow) {
-    const pt_triangle_attribute& attr = w.attr[h];
     const float hu = 1.0f - hv - hw;
-    const f2 iuv = interp_uv(attr, hu, hv, hw);
-    const pt_material& m = w.mat[attr.material_index];
+    const f2 iuv = interp_uv(w, h, hu, hv, hw);
+    const pt_material& m = w.mat[attr_material(w, h)];
     f3 base_color = mk(m.base_color[0], m.base_color[1], m.base_color[2]);
     const float base_weight = m.base_weight;
     float base_metalness = m.base_metalness;
@@ -246,14 +245,14 @@ PTD bool shade_hit(const World& w, uint32_t bounce, uint32_t max_bounces, PathSt
     const f3 flat_raw = normalize(cross(tri.v1 - tri.v0, tri.v2 - tri.v0));
     const float bfm = dot(V, flat_raw) > 0.0f ? 1.0f : -1.0f;
     const f3 flat_n = flat_raw * bfm;
-    const f3 n0 = mk(attr.n0[0], attr.n0[1], attr.n0[2]);
-    const f3 n1 = mk(attr.n1[0], attr.n1[1], attr.n1[2]);
-    const f3 n2 = mk(attr.n2[0], attr.n2[1], attr.n2[2]);
+    const f3 n0 = attr_normal(w, h, 0);
+    const f3 n1 = attr_normal(w, h, 1);
+    const f3 n2 = attr_normal(w, h, 2);
     f3 N = normalize(hu * n0 + hv * n1 + hw * n2) * bfm;
-    const f3 t0 = mk(attr.t0[0], attr.t0[1], attr.t0[2]);
-    const f3 t1 = mk(attr.t1[0], attr.t1[1], attr.t1[2]);
-    const f3 t2 = mk(attr.t2[0], attr.t2[1], attr.t2[2]);
-    const float t0w = attr.t0[3];
+    const f3 t0 = attr_tangent(w, h, 0);
+    const f3 t1 = attr_tangent(w, h, 1);
+    const f3 t2 = attr_tangent(w, h, 2);
+    const float t0w = attr_tangent0_w(w, h);
     f3 Tn = orthonormal_tangent(hu * t0 + hv * t1 + hw * t2, N) * bfm;
     f3 Bn = cross(N, Tn) * t0w * bfm;
     bool n_changed = false;

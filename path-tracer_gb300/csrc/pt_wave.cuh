@@ -11,6 +11,7 @@ namespace ptd {
 struct Fast {
     const float4* pairs;  // node i at pairs[2i], pairs[2i+1]
     const float4* tri4;   // triangle i at tri4[3i .. 3i+2]
+    const float4* wide = nullptr;  // pt_wide_node i at wide[8i .. 8i+7] (precision form)
 };
 
 struct Queues {
@@ -22,7 +23,10 @@ struct Queues {
     float4* so;
     float4* sd;
     float4* sc;
-    uint32_t* cnt;  // [0], [1] ray queue lengths, [2] shadow length, [3] extend fetch, [4] shadow fetch
+    uint32_t* hit_list;   // slots of the current queue whose ray hit a triangle
+    uint32_t* miss_list;  // slots whose ray left the scene
+    uint32_t* cnt;  // [0], [1] ray queue lengths, [2] shadow length, [3] extend fetch, [4] shadow fetch,
+                    // [5] hit list length, [6] miss list length
     Counters* rec;  // per path (recording variants)
     int32_t* rec_hits;
 };
@@ -282,6 +286,183 @@ struct Traverser {
 #endif
 };
 
+// Sort 8 keys ascending (a 19-comparator network: no dynamic indexing, so the
+// keys stay in registers).
+PTD void sort8(uint32_t (&k)[8]) {
+#define PT_CE(a, b)                                  \
+    {                                                \
+        const uint32_t lo_ = umin(k[a], k[b]);       \
+        const uint32_t hi_ = umax(k[a], k[b]);       \
+        k[a] = lo_;                                  \
+        k[b] = hi_;                                  \
+    }
+    PT_CE(0, 2) PT_CE(1, 3) PT_CE(4, 6) PT_CE(5, 7)
+    PT_CE(0, 4) PT_CE(1, 5) PT_CE(2, 6) PT_CE(3, 7)
+    PT_CE(0, 1) PT_CE(2, 3) PT_CE(4, 5) PT_CE(6, 7)
+    PT_CE(2, 4) PT_CE(3, 5)
+    PT_CE(1, 4) PT_CE(3, 6)
+    PT_CE(1, 2) PT_CE(3, 4) PT_CE(5, 6)
+#undef PT_CE
+}
+
+// One ray's traversal of the 8-wide BVH of the precision form
+// (include/pt_precision.h), with the same step()/result interface as
+// Traverser.  A visit decodes the node's child boxes exactly as the host
+// quantised them (origin + q * 2^e: the product exact, one rounding) and runs
+// the reference's slab test (trace.slang:597-609) on them; an axis whose
+// direction component is zero constrains nothing (the binary test's value is
+// then not a bound: 0 * inf).  The hit children, nearest first for closest
+// hit, form a list of 3-bit child indices; the deferred stack holds (node,
+// rest of its list), one entry per level.  Triangles are tested one per step
+// with the reference's watertight test, so a hit's (t, v, w) are the binary
+// traversal's for the same triangle.  Opaque scenes only.
+template <bool kShadow, bool kTri36 = false>
+struct WideTraverser {
+    f3 o, d, rcp, nod_lo, nod_hi;
+    Shear s;
+    float hit_t, hv, hw;
+    int32_t hit, light_tri;
+    uint32_t node, list, lf, tri_left, sp;
+    Rng<false> rng;  // unused (no alpha draws in the wide form)
+    Counters c;      // unused (no records in the wide form)
+
+    PTD void init(const Fast& f, f3 origin, f3 dir, float t_max, int32_t light) {
+        o = origin;
+        d = dir;
+        rcp = 1.0f / d;
+        s = make_shear(d, rcp);
+        const f3 nod = -o * rcp;
+        nod_lo = nod;
+        nod_hi = nod;
+        // an axis the ray does not move along: t0 = -inf, t1 = +inf
+        const float inf = __int_as_float(0x7f800000);
+        if (fabsf(rcp.x) == inf) { rcp.x = 0.0f; nod_lo.x = -inf; nod_hi.x = inf; }
+        if (fabsf(rcp.y) == inf) { rcp.y = 0.0f; nod_lo.y = -inf; nod_hi.y = inf; }
+        if (fabsf(rcp.z) == inf) { rcp.z = 0.0f; nod_lo.z = -inf; nod_hi.z = inf; }
+        hit_t = t_max;
+        hv = hw = 0.0f;
+        hit = -1;
+        light_tri = light;
+        sp = 0u;
+        tri_left = 0u;
+        node = 0u;
+        list = visit(f, 0u);
+    }
+
+    // the hit children of node n as 3-bit indices (nearest first unless
+    // kShadow) in bits 0..23, their count in bits 24..27
+    PTD uint32_t visit(const Fast& f, uint32_t n) const {
+        const float4* p = f.wide + 8 * (size_t)n;
+        const float4 h0 = __ldg(p), h1 = __ldg(p + 1), h2 = __ldg(p + 2), h3 = __ldg(p + 3);
+        const uint32_t meta = __float_as_uint(h0.w);
+        const uint32_t count = meta >> 24;
+        const float sx = __uint_as_float((meta & 0xffu) << 23);
+        const float sy = __uint_as_float(((meta >> 8) & 0xffu) << 23);
+        const float sz = __uint_as_float(((meta >> 16) & 0xffu) << 23);
+        const float cx = sx * 8388608.0f, cy = sy * 8388608.0f, cz = sz * 8388608.0f;  // 2^23 * s, exact
+        const uint32_t lox[2] = {__float_as_uint(h1.x), __float_as_uint(h1.y)};
+        const uint32_t loy[2] = {__float_as_uint(h1.z), __float_as_uint(h1.w)};
+        const uint32_t loz[2] = {__float_as_uint(h2.x), __float_as_uint(h2.y)};
+        const uint32_t hix[2] = {__float_as_uint(h2.z), __float_as_uint(h2.w)};
+        const uint32_t hiy[2] = {__float_as_uint(h3.x), __float_as_uint(h3.y)};
+        const uint32_t hiz[2] = {__float_as_uint(h3.z), __float_as_uint(h3.w)};
+        uint32_t k[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            // q as the float 2^23 + q, then (2^23 + q) * s - 2^23 * s = q * s exactly
+            const unsigned sel = 0x7440u | (unsigned)(i & 3);
+            const int wd = i >> 2;
+            const float qlx = fmaf(__uint_as_float(__byte_perm(lox[wd], 0x4B000000u, sel)), sx, -cx);
+            const float qly = fmaf(__uint_as_float(__byte_perm(loy[wd], 0x4B000000u, sel)), sy, -cy);
+            const float qlz = fmaf(__uint_as_float(__byte_perm(loz[wd], 0x4B000000u, sel)), sz, -cz);
+            const float qhx = fmaf(__uint_as_float(__byte_perm(hix[wd], 0x4B000000u, sel)), sx, -cx);
+            const float qhy = fmaf(__uint_as_float(__byte_perm(hiy[wd], 0x4B000000u, sel)), sy, -cy);
+            const float qhz = fmaf(__uint_as_float(__byte_perm(hiz[wd], 0x4B000000u, sel)), sz, -cz);
+            const float bminx = __fadd_rn(h0.x, qlx), bminy = __fadd_rn(h0.y, qly), bminz = __fadd_rn(h0.z, qlz);
+            const float bmaxx = __fadd_rn(h0.x, qhx), bmaxy = __fadd_rn(h0.y, qhy), bmaxz = __fadd_rn(h0.z, qhz);
+            const float t0x = fma_(bminx, rcp.x, nod_lo.x), t0y = fma_(bminy, rcp.y, nod_lo.y);
+            const float t0z = fma_(bminz, rcp.z, nod_lo.z);
+            const float t1x = fma_(bmaxx, rcp.x, nod_hi.x), t1y = fma_(bmaxy, rcp.y, nod_hi.y);
+            const float t1z = fma_(bmaxz, rcp.z, nod_hi.z);
+            const float t_near = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
+            const float t_far = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+            const bool h = (uint32_t)i < count && t_near <= t_far && t_far > 0.0f && t_near < hit_t;
+            if constexpr (kShadow)
+                k[i] = h ? (uint32_t)i : 0xffffffffu;
+            else
+                k[i] = h ? ((__float_as_uint(fmaxf(0.0f, t_near)) & ~7u) | (uint32_t)i) : 0xffffffffu;
+        }
+        if constexpr (!kShadow) sort8(k);
+        uint32_t l = 0u, cnt = 0u;
+#pragma unroll
+        for (int i = 7; i >= 0; --i)
+            if (k[i] != 0xffffffffu) {
+                l = (l << 3) | (k[i] & 7u);
+                ++cnt;
+            }
+        return l | (cnt << 24);
+    }
+
+    PTD bool test_triangle(const World& w, const Fast& f, uint32_t tri) {
+        float t, v, wb;
+        Tri tv;
+        if constexpr (kTri36)
+            tv = load_tri(w, tri);
+        else
+            tv = load_tri4(f, tri);
+        if (!triangle_test(tv, o, s, &t, &v, &wb)) return false;
+        if (t > 0.0f && t < hit_t) {
+            if constexpr (kShadow) {
+                hit = 1;
+                return true;
+            } else {
+                hit_t = t;
+                hit = (int32_t)tri;
+                hv = v;
+                hw = wb;
+            }
+        }
+        return false;
+    }
+
+    // one node visit or one triangle test; true when the traversal has finished
+    PTD bool step(const World& w, const Fast& f, uint2* stack, uint32_t*) {
+        if (tri_left == 0u) {
+            uint32_t cnt = list >> 24;
+            if (cnt == 0u) {
+                if (sp == 0u) return true;
+                sp -= 1u;
+                const uint2 e = stack[sp & 63u];
+                node = e.x;
+                list = e.y;
+                cnt = list >> 24;
+            }
+            const uint32_t k = list & 7u;
+            list = ((list & 0xffffffu) >> 3) | ((cnt - 1u) << 24);
+            const float4* p = f.wide + 8 * (size_t)node;
+            const uint32_t child = __ldg(reinterpret_cast<const uint32_t*>(p + 4) + k);
+            const uint32_t tc = __ldg(reinterpret_cast<const unsigned short*>(p + 6) + k);
+            if (tc == 0u) {
+                if (cnt > 1u) {
+                    stack[sp & 63u] = make_uint2(node, list);
+                    sp += 1u;
+                }
+                node = child;
+                list = visit(f, child);
+                return false;
+            }
+            lf = child;
+            tri_left = tc;
+        }
+        const uint32_t tri = lf;
+        lf += 1u;
+        tri_left -= 1u;
+        bool skip = false;
+        if constexpr (kShadow) skip = (int32_t)tri == light_tri;
+        return !skip && test_triangle(w, f, tri);
+    }
+};
+
 constexpr int kStepsPerRefill = PT_STEPS_PER_REFILL;
 constexpr unsigned kRefillBelow = PT_REFILL_BELOW;
 
@@ -303,21 +484,88 @@ PTD uint32_t warp_append(bool want, uint32_t* counter, unsigned mask) {
     return want ? base + (uint32_t)__popc(ballot & ((1u << lane) - 1u)) : 0xffffffffu;
 }
 
+// Files finished extend rays' queue slots under hits or misses, so that the
+// shading kernel runs warps of hits only and warps of misses only.  Lanes
+// finish at different steps, so a finishing lane only appends to its warp's
+// buffer in shared memory; the warp flushes the buffer to the global lists
+// once per refill round (one global atomic per list and round).  A lane
+// finishes at most one ray per round, so 32 entries per list suffice.
+struct ResultFiler {
+    uint32_t* buf;   // this warp's [2][32] in shared memory: hits, misses
+    uint32_t* fill;  // this warp's [2] entry counts
+    PTD void file(uint32_t slot, bool is_hit) {
+        const uint32_t b = is_hit ? 0u : 1u;
+        const uint32_t j = atomicAdd(&fill[b], 1u);
+        buf[b * 32u + j] = slot;
+    }
+    // all 32 lanes, converged
+    PTD void flush(const Queues& q, unsigned lane) {
+        __syncwarp();
+        const uint32_t nh = fill[0], nm = fill[1];
+        uint32_t bh = 0, bm = 0;
+        if (lane == 0u) {
+            if (nh) bh = atomicAdd(&q.cnt[5], nh);
+            if (nm) bm = atomicAdd(&q.cnt[6], nm);
+        }
+        bh = __shfl_sync(0xffffffffu, bh, 0);
+        bm = __shfl_sync(0xffffffffu, bm, 0);
+        if (lane < nh) q.hit_list[bh + lane] = buf[lane];
+        if (lane < nm) q.miss_list[bm + lane] = buf[32u + lane];
+        __syncwarp();
+        if (lane == 0u) fill[0] = fill[1] = 0u;
+        __syncwarp();
+    }
+};
+
+// shared-memory buffers of the ResultFilers of one extend block
+template <int kThreads>
+struct FilerSlots {
+    uint32_t buf[kThreads / 32][64];
+    uint32_t fill[kThreads / 32][2];
+    PTD ResultFiler of_warp(unsigned lane) {
+        const unsigned wi = threadIdx.x >> 5;
+        if (lane == 0u) fill[wi][0] = fill[wi][1] = 0u;
+        __syncwarp();
+        return ResultFiler{buf[wi], fill[wi]};
+    }
+};
+
+struct NoRound {
+    PTD void operator()() const {}
+};
+
+// The shading kernels' view of the filed results: misses first, padded to
+// whole warps, then hits.  Entry j of that range maps to a queue slot.
+struct ShadeRange {
+    uint32_t n_hit, n_miss, miss_span;
+    PTD ShadeRange(const uint32_t* cnt) : n_hit(cnt[5]), n_miss(cnt[6]), miss_span((cnt[6] + 31u) & ~31u) {}
+    PTD uint32_t count() const { return miss_span + n_hit; }
+    // queue slot of entry j, or 0xffffffff for the padding after the misses and past the end
+    PTD uint32_t slot(const Queues& q, uint32_t j) const {
+        if (j < miss_span) return j < n_miss ? q.miss_list[j] : 0xffffffffu;
+        const uint32_t k = j - miss_span;
+        return k < n_hit ? q.hit_list[k] : 0xffffffffu;
+    }
+};
+
 // The persistent traversal loop of one warp; every lane holds at most one ray.
 // Each round the warp counts its busy lanes: when fewer than refill_below are
 // busy and the queue still has rays, the idle lanes take the next ones (one
 // atomic per warp, queue slots in lane order).  Busy lanes then advance their
 // ray by up to `steps` traversal steps.  start(i) loads queue entry i into the
 // lane; advance() runs one step and returns true once the ray has finished
-// and its result is written.  A warp leaves only when the queue is exhausted
-// and none of its lanes is busy, so every entry below `count` is traced once.
-template <class Start, class Advance>
+// and its result is written.  round() runs with the warp converged at the top
+// of every round (and so after the last one).  A warp leaves only when the
+// queue is exhausted and none of its lanes is busy, so every entry below
+// `count` is traced once.
+template <class Start, class Advance, class Round = NoRound>
 PTD void lane_refill_loop(uint32_t* fetch, uint32_t count, uint32_t steps, unsigned refill_below, Start&& start,
-                          Advance&& advance) {
+                          Advance&& advance, Round&& round = Round()) {
     const unsigned lane = lane_id();
     if (refill_below < 1u) refill_below = 1u;
     bool active = false, exhausted = false;
     for (;;) {
+        round();
         unsigned busy = __ballot_sync(0xffffffffu, active);
         if (!exhausted && (unsigned)__popc(busy) < refill_below) {
             const unsigned idle = ~busy;

@@ -29,10 +29,28 @@ void world_changed(Wavefront* wf);
 // wraps each kernel launch (class id from PT_KC_*) so the caller can time it
 using Timer = std::function<cudaError_t(int cls, const std::function<cudaError_t()>& launch)>;
 
-// (re)build the derived BVH / triangle layouts after world_changed
-cudaError_t prepare(Wavefront* wf, const ptd::World& w, uint64_t nodes, uint64_t tris, cudaStream_t stream);
+// the skybox texels changed (its BF16 copy is rebuilt on the next trace)
+void sky_changed(Wavefront* wf);
+
+// (re)build the derived layouts after world_changed: the child-pair BVH and
+// padded triangles always; for the precision form (PT_PRECISION_* bits of
+// include/pt_precision.h) the 8-wide BVH (collapsed on the host from the
+// device's binary nodes) and the FP16 attributes / BF16 skybox.
+cudaError_t prepare(Wavefront* wf, const ptd::World& w, uint64_t nodes, uint64_t tris, uint32_t precision,
+                    cudaStream_t stream);
+
+// the precision bits a trace with these arguments runs: the wide BVH only for
+// opaque worlds and not for the recording variants (their records describe
+// the binary traversal)
+uint32_t effective_precision(const ptd::World& w, uint32_t precision, bool record);
 
 cudaError_t trace(Wavefront* wf, const ptd::World& w, const ptk::Tile& tile, uint32_t first_sample,
-                  uint32_t samples, ptk::Sinks sinks, cudaStream_t stream, const Timer& timer);
+                  uint32_t samples, ptk::Sinks sinks, cudaStream_t stream, const Timer& timer, uint32_t precision);
+
+// closest hit of given rays through the 8-wide BVH (prepare with
+// PT_PRECISION_WIDE_BVH first); device arrays
+cudaError_t debug_intersect_wide(Wavefront* wf, const ptd::World& w, uint64_t n, const float* origins,
+                                 const float* directions, const float* t_max, int32_t* hit, float* hit_t,
+                                 cudaStream_t stream);
 
 }  // namespace ptw

@@ -202,6 +202,66 @@ void add_icosphere(Mesh& m, V3 c, float radius, uint32_t level) {
     for (size_t f = 0; f < faces.size(); f += 3) m.tri(base + faces[f], base + faces[f + 1], base + faces[f + 2]);
 }
 
+// Procedural RGBA8 textures: 1024 x 1024 each, 64 per 8192 x 8192 atlas
+// layer in an 8 x 8 grid of slots.  Even kinds are checkers (8 x 8 squares
+// of two seeded colours), odd kinds value noise (4 octaves, grey-tinted).
+constexpr uint32_t kTexSize = 1024, kTexPerRow = PT_ATLAS_SIZE / kTexSize;
+constexpr uint32_t kTexPerLayer = kTexPerRow * kTexPerRow;
+
+struct TextureAtlas {
+    std::vector<uint8_t> layer;  // allocated on first use
+    uint32_t used = 0;
+    uint64_t seed;
+
+    // points the material's base colour at texture number `used` (the first
+    // 64 are generated, later ones reuse them in turn)
+    void texture(pt_material& m) {
+        if (layer.empty()) layer.assign((size_t)PT_ATLAS_SIZE * PT_ATLAS_SIZE * 4, 0);
+        const uint32_t slot = used % kTexPerLayer, kind = slot;
+        const bool fresh = used < kTexPerLayer;
+        used += 1;
+        const uint32_t x0 = (slot % kTexPerRow) * kTexSize, y0 = (slot / kTexPerRow) * kTexSize;
+        const float c0[3] = {hash01(kind, 0, 1, seed), hash01(kind, 0, 2, seed), hash01(kind, 0, 3, seed)};
+        const float c1[3] = {hash01(kind, 1, 1, seed), hash01(kind, 1, 2, seed), hash01(kind, 1, 3, seed)};
+        for (uint32_t y = 0; fresh && y < kTexSize; ++y) {
+            uint8_t* row = layer.data() + ((size_t)(y0 + y) * PT_ATLAS_SIZE + x0) * 4;
+            for (uint32_t x = 0; x < kTexSize; ++x) {
+                float r, g, b;
+                if (kind % 2 == 0) {
+                    const bool odd = (((x >> 7) ^ (y >> 7)) & 1u) != 0;
+                    r = odd ? c1[0] : c0[0];
+                    g = odd ? c1[1] : c0[1];
+                    b = odd ? c1[2] : c0[2];
+                } else {
+                    float n = 0.0f, amp = 0.5f, f = 1.0f / 64.0f;
+                    for (uint32_t o = 0; o < 4; ++o) {
+                        n += amp * value_noise((float)x * f, (float)y * f, 16 + o, seed ^ (uint64_t)kind * 0x9E37ull);
+                        amp *= 0.5f;
+                        f *= 2.0f;
+                    }
+                    r = 0.25f + 0.75f * n * (0.6f + 0.4f * c0[0]);
+                    g = 0.25f + 0.75f * n * (0.6f + 0.4f * c0[1]);
+                    b = 0.25f + 0.75f * n * (0.6f + 0.4f * c0[2]);
+                }
+                row[4 * x + 0] = (uint8_t)(r * 255.0f + 0.5f);
+                row[4 * x + 1] = (uint8_t)(g * 255.0f + 0.5f);
+                row[4 * x + 2] = (uint8_t)(b * 255.0f + 0.5f);
+                row[4 * x + 3] = 255u;
+            }
+        }
+        m.base_color_tex_layer = 0;
+        m.base_color_uv[0] = (float)x0 / (float)PT_ATLAS_SIZE;
+        m.base_color_uv[1] = (float)y0 / (float)PT_ATLAS_SIZE;
+        m.base_color_uv[2] = (float)kTexSize / (float)PT_ATLAS_SIZE;
+        m.base_color_uv[3] = (float)kTexSize / (float)PT_ATLAS_SIZE;
+    }
+    int add_to(ptw_world* w) const {
+        if (layer.empty()) return PT_OK;
+        int32_t index = 0;
+        return ptw_add_atlas_layer(w, 1, layer.data(), &index);
+    }
+};
+
 }  // namespace
 
 extern "C" {
@@ -243,6 +303,53 @@ int ptw_scene_cornell_box(ptw_world** out) {
     if (!rc) rc = right.add_to(w, green);
     if (!rc) rc = boxes.add_to(w, white);
     if (!rc) rc = lamp.add_to(w, light);
+    if (!rc) rc = ptw_build(w);
+    if (rc) {
+        ptw_destroy(w);
+        return rc;
+    }
+    *out = w;
+    return PT_OK;
+}
+
+int ptw_scene_cornell_box_textured(uint64_t seed, ptw_world** out) {
+    if (!out) return PT_ERR_INVALID_ARG;
+    ptw_world* w = nullptr;
+    ptw_create(&w);
+    TextureAtlas atlas;
+    atlas.seed = seed;
+    // eight meshes; floor, back wall, short box and tall box (4 of 8) textured
+    const float colors[8][3] = {{0.73f, 0.73f, 0.73f}, {0.73f, 0.73f, 0.73f}, {0.73f, 0.73f, 0.73f},
+                                {0.65f, 0.05f, 0.05f}, {0.12f, 0.45f, 0.15f}, {0.73f, 0.73f, 0.73f},
+                                {0.73f, 0.73f, 0.73f}, {0.73f, 0.73f, 0.73f}};
+    const bool textured[8] = {true, false, true, false, false, true, true, false};
+    uint32_t mat[8];
+    for (int i = 0; i < 8; ++i) {
+        pt_material m = base_only(colors[i][0], colors[i][1], colors[i][2]);
+        if (textured[i]) atlas.texture(m);
+        if (i == 7) {
+            m.emission_color_and_luminance[0] = 17.0f;
+            m.emission_color_and_luminance[1] = 12.0f;
+            m.emission_color_and_luminance[2] = 4.0f;
+            m.emission_color_and_luminance[3] = 1.0f;
+            m.emission_weight = 1.0f;
+        }
+        ptw_add_material(w, &m, &mat[i]);
+    }
+    Mesh floor_, ceiling, back, left, right, short_box, tall_box, lamp;
+    floor_.quad({0, 0, 1}, {1, 0, 1}, {1, 0, 0}, {0, 0, 0}, {0, 1, 0});
+    ceiling.quad({0, 1, 0}, {1, 1, 0}, {1, 1, 1}, {0, 1, 1}, {0, -1, 0});
+    back.quad({0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1});
+    left.quad({0, 0, 0}, {0, 1, 0}, {0, 1, 1}, {0, 0, 1}, {1, 0, 0});
+    right.quad({1, 0, 1}, {1, 1, 1}, {1, 1, 0}, {1, 0, 0}, {-1, 0, 0});
+    add_box(short_box, {0.66f, 0.15f, 0.64f}, {0.15f, 0.15f, 0.15f}, -0.30f, 0.0f);
+    add_box(tall_box, {0.34f, 0.30f, 0.36f}, {0.15f, 0.30f, 0.15f}, 0.29f, 0.0f);
+    lamp.quad({0.375f, 0.999f, 0.375f}, {0.625f, 0.999f, 0.375f}, {0.625f, 0.999f, 0.625f},
+              {0.375f, 0.999f, 0.625f}, {0, -1, 0});
+    const Mesh* meshes[8] = {&floor_, &ceiling, &back, &left, &right, &short_box, &tall_box, &lamp};
+    int rc = PT_OK;
+    for (int i = 0; i < 8 && !rc; ++i) rc = meshes[i]->add_to(w, mat[i]);
+    if (!rc) rc = atlas.add_to(w);
     if (!rc) rc = ptw_build(w);
     if (rc) {
         ptw_destroy(w);
@@ -312,6 +419,18 @@ int ptw_scene_procedural(const ptw_procedural_params* params, ptw_world** out) {
     ptw_world* w = nullptr;
     ptw_create(&w);
     Rng rng{P.seed * 0x2545F4914F6CDD1Dull + 0x1234567ull};
+    // texture and alpha choices draw from their own stream, so the geometry
+    // and materials of a seed do not depend on these options
+    Rng look{P.seed * 0x9E3779B97F4A7C15ull + 0xABCDEFull};
+    TextureAtlas atlas;
+    atlas.seed = P.seed;
+    const auto decorate = [&](pt_material& m, bool may_blend) {
+        if (P.textured && look.uniform() < 0.5f) atlas.texture(m);
+        if (P.non_opaque && may_blend && look.uniform() < 0.1f) {
+            m.alpha_mode = PT_ALPHA_MODE_BLEND;
+            m.base_color[3] = look.range(0.3f, 0.9f);
+        }
+    };
     const float ext_x = 64.0f, ext_z = 32.0f;
     Terrain terrain{P.seed};
     int rc = PT_OK;
@@ -319,6 +438,7 @@ int ptw_scene_procedural(const ptw_procedural_params* params, ptw_world** out) {
     // heightfield
     {
         pt_material m = random_material(rng);
+        decorate(m, false);
         uint32_t mi;
         ptw_add_material(w, &m, &mi);
         Mesh hf;
@@ -348,6 +468,7 @@ int ptw_scene_procedural(const ptw_procedural_params* params, ptw_world** out) {
     // boxes, one material each
     for (uint32_t k = 0; k < P.boxes && !rc; ++k) {
         pt_material m = random_material(rng);
+        decorate(m, true);
         uint32_t mi;
         ptw_add_material(w, &m, &mi);
         const float x = rng.range(-0.47f * ext_x, 0.47f * ext_x), z = rng.range(-0.47f * ext_z, 0.47f * ext_z);
@@ -360,6 +481,7 @@ int ptw_scene_procedural(const ptw_procedural_params* params, ptw_world** out) {
     // icospheres
     for (uint32_t k = 0; k < P.spheres && !rc; ++k) {
         pt_material m = random_material(rng);
+        decorate(m, true);
         uint32_t mi;
         ptw_add_material(w, &m, &mi);
         const float x = rng.range(-0.45f * ext_x, 0.45f * ext_x), z = rng.range(-0.45f * ext_z, 0.45f * ext_z);
@@ -398,6 +520,7 @@ int ptw_scene_procedural(const ptw_procedural_params* params, ptw_world** out) {
         e.tri(vi[0], vi[1], vi[2]);
         rc = e.add_to(w, mi);
     }
+    if (!rc) rc = atlas.add_to(w);
     if (!rc) rc = ptw_build(w);
     if (!rc && P.skybox_width > 0 && P.skybox_height > 0) {
         rc = ptw_set_procedural_skybox(w, P.skybox_width, P.skybox_height);

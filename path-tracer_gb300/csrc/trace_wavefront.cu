@@ -16,8 +16,10 @@
 #include <cmath>
 #include <cstdio>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
+#include "../../include/pt_precision.h"
 #include "pt_wave.cuh"
 #include "pt_wavefront.h"
 
@@ -49,7 +51,6 @@ __global__ void __launch_bounds__(256) raygen_kernel(World w, ptk::Tile t, Group
         c.visit_hash = kFnvBasis;
         c.extend_rays = c.shadow_rays = c.interior_visits = c.leaf_visits = c.triangle_tests = c.rand_draws = 0;
         c.shadow_interior_visits = c.shadow_leaf_visits = c.shadow_triangle_tests = 0;
-    c.shadow_interior_visits = c.shadow_leaf_visits = c.shadow_triangle_tests = 0;
         c.hits = c.sky_misses = c.light_samples = c.sky_light_samples = 0;
     }
     Rng<kRec> rng;
@@ -72,19 +73,26 @@ __global__ void bounce_reset_kernel(uint32_t* cnt, int next) {
     cnt[2] = 0u;
     cnt[3] = 0u;
     cnt[4] = 0u;
+    cnt[5] = 0u;
+    cnt[6] = 0u;
 }
 
 // Persistent extend kernel: every lane traverses its own ray and takes a new
 // one from the queue (one atomic per warp for all idle lanes) as soon as it
-// finishes, so long and short rays do not leave lanes idle.
-template <bool kRec, bool kAlpha, bool kTri36 = false>
+// finishes, so long and short rays do not leave lanes idle.  Finished rays
+// are filed under hits or misses for the shading kernel.  kWide traverses the
+// 8-wide BVH of the precision form instead of the binary one.
+template <bool kRec, bool kAlpha, bool kTri36 = false, bool kWide = false>
 __global__ void __launch_bounds__(kExtendThreads, PT_EXTEND_MIN_BLOCKS) extend_kernel(World w, Fast f, Queues q, int cur, uint32_t bounce) {
+    static_assert(!(kWide && (kRec || kAlpha)), "the wide form keeps no records and runs opaque scenes only");
     const Stage st = stage_of(q, cur);
     const uint32_t count = *st.count;
-    Traverser<kRec, kAlpha, false, kTri36> tr;
+    typename std::conditional<kWide, WideTraverser<false, kTri36>, Traverser<kRec, kAlpha, false, kTri36>>::type tr;
     uint2 stack[64];
     uint32_t istack[kRec ? 64 : 1];
     uint32_t slot = 0, path = 0;
+    __shared__ FilerSlots<kExtendThreads> filer_slots;
+    ResultFiler filer = filer_slots.of_warp(lane_id());
     lane_refill_loop(
         &q.cnt[3], count, kStepsPerRefill, kRefillBelow,
         [&](uint32_t i) {
@@ -103,26 +111,29 @@ __global__ void __launch_bounds__(kExtendThreads, PT_EXTEND_MIN_BLOCKS) extend_k
                 q.rec[path] = tr.c;
                 if (bounce < PT_RECORD_MAX_BOUNCES) q.rec_hits[(size_t)path * PT_RECORD_MAX_BOUNCES + bounce] = tr.hit;
             }
+            filer.file(slot, tr.hit != -1);
             return true;
-        });
+        },
+        [&]() { filer.flush(q, lane_id()); });
 }
 
 template <bool kRec, bool kAlpha>
 __global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kernel(World w, Fast f, Queues q, int cur, uint32_t bounce,
                                                               uint32_t max_bounces) {
     const Stage st = stage_of(q, cur);
-    const uint32_t count = *st.count;
+    const ShadeRange range(q.cnt);
+    const uint32_t count = range.count();
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     const unsigned lane = lane_id();
     for (uint32_t base = warp * 32u; base < count; base += warps * 32u) {
-        const uint32_t i = base + lane;
+        const uint32_t i = range.slot(q, base + lane);
         bool cont = false;
         ShadowRay sr;
         sr.valid = false;
         PathState ps;
         uint32_t p = 0, rs = 0;
-        if (i < count) {
+        if (i != 0xffffffffu) {
             const float4 o4 = st.o[i], d4 = st.d[i], t4 = st.T[i], h4 = q.hit[i];
             p = __float_as_uint(o4.w);
             const float4 c4 = q.color[p];
@@ -169,10 +180,11 @@ __global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kern
 
 // Persistent shadow kernel (opaque scenes): any-hit traversal of every queued
 // shadow ray with the same lane refill; unoccluded rays add their light.
-template <bool kRec, bool kTri36 = false>
+template <bool kRec, bool kTri36 = false, bool kWide = false>
 __global__ void __launch_bounds__(kExtendThreads, PT_EXTEND_MIN_BLOCKS) shadow_kernel(World w, Fast f, Queues q) {
+    static_assert(!(kWide && kRec), "the wide form keeps no records");
     const uint32_t count = q.cnt[2];
-    Traverser<kRec, false, true, kTri36> tr;
+    typename std::conditional<kWide, WideTraverser<true, kTri36>, Traverser<kRec, false, true, kTri36>>::type tr;
     uint2 stack[64];
     uint32_t istack[kRec ? 64 : 1];
     uint32_t path = 0;
@@ -210,9 +222,27 @@ __global__ void accumulate_kernel(ptk::Tile t, Group g, const float4* color) {
         acc = mk(a.x, a.y, a.z);
     }
     uint32_t n = g.first_sample;
-    for (uint32_t s = 0; s < g.samples; ++s, ++n) {
-        const float4 c = color[(size_t)s * g.pixels + pix];
-        acc = (n > 1u ? acc : mk(0.0f, 0.0f, 0.0f)) + mk(c.x, c.y, c.z);
+    if (t.comp) {
+        // Kahan-compensated sums (precision form); the first sample is 0 + L
+        // with zero compensation, as in the plain sum
+        f3 comp = mk(0.0f, 0.0f, 0.0f);
+        if (g.first_sample > 1u) {
+            const float4 k = t.comp[idx];
+            comp = mk(k.x, k.y, k.z);
+        }
+        for (uint32_t s = 0; s < g.samples; ++s, ++n) {
+            const float4 c = color[(size_t)s * g.pixels + pix];
+            const f3 y = mk(c.x, c.y, c.z) - comp;
+            const f3 sum = acc + y;
+            comp = (sum - acc) - y;
+            acc = sum;
+        }
+        t.comp[idx] = make_float4(comp.x, comp.y, comp.z, 0.0f);
+    } else {
+        for (uint32_t s = 0; s < g.samples; ++s, ++n) {
+            const float4 c = color[(size_t)s * g.pixels + pix];
+            acc = (n > 1u ? acc : mk(0.0f, 0.0f, 0.0f)) + mk(c.x, c.y, c.z);
+        }
     }
     n -= 1u;
     t.accum[idx] = make_float4(acc.x, acc.y, acc.z, 1.0f);
@@ -239,9 +269,6 @@ __global__ void finalize_records_kernel(ptk::Tile t, Group g, Queues q, ptk::Sin
         r->shadow_interior_visits = c.shadow_interior_visits;
         r->shadow_leaf_visits = c.shadow_leaf_visits;
         r->shadow_triangle_tests = c.shadow_triangle_tests;
-    r->shadow_interior_visits = c.shadow_interior_visits;
-    r->shadow_leaf_visits = c.shadow_leaf_visits;
-    r->shadow_triangle_tests = c.shadow_triangle_tests;
         r->rand_draws = c.rand_draws;
         r->hits = c.hits;
         r->sky_misses = c.sky_misses;
@@ -261,6 +288,52 @@ __global__ void pad_triangles_kernel(const pt_triangle_geometry* geo, uint64_t n
     tri4[3 * i + 0] = make_float4(v[0], v[1], v[2], 0.0f);
     tri4[3 * i + 1] = make_float4(v[3], v[4], v[5], 0.0f);
     tri4[3 * i + 2] = make_float4(v[6], v[7], v[8], 0.0f);
+}
+
+// FP32 attributes -> pt_half_attribute records (round to nearest even)
+PTD uint32_t pack_half2(float x, float y) {
+    return (uint32_t)__half_as_ushort(__float2half_rn(x)) | ((uint32_t)__half_as_ushort(__float2half_rn(y)) << 16);
+}
+__global__ void half_attributes_kernel(const pt_triangle_attribute* in, uint64_t n, uint2* out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const pt_triangle_attribute& a = in[i];
+    uint2* o = out + 8 * i;
+    o[0] = make_uint2(pack_half2(a.n0[0], a.n0[1]), pack_half2(a.n0[2], 0.0f));
+    o[1] = make_uint2(pack_half2(a.n1[0], a.n1[1]), pack_half2(a.n1[2], 0.0f));
+    o[2] = make_uint2(pack_half2(a.n2[0], a.n2[1]), pack_half2(a.n2[2], 0.0f));
+    o[3] = make_uint2(pack_half2(a.t0[0], a.t0[1]), pack_half2(a.t0[2], a.t0[3]));
+    o[4] = make_uint2(pack_half2(a.t1[0], a.t1[1]), pack_half2(a.t1[2], a.t1[3]));
+    o[5] = make_uint2(pack_half2(a.t2[0], a.t2[1]), pack_half2(a.t2[2], a.t2[3]));
+    o[6] = make_uint2(pack_half2(a.uv0[0], a.uv0[1]), pack_half2(a.uv1[0], a.uv1[1]));
+    o[7] = make_uint2(pack_half2(a.uv2[0], a.uv2[1]), a.material_index);
+}
+
+// RGBA32F skybox texels -> BF16 RGBA (round to nearest even)
+PTD uint32_t pack_bf162(float x, float y) {
+    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(x)) |
+           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(y)) << 16);
+}
+__global__ void bf16_sky_kernel(const float4* in, uint64_t n, uint2* out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = in[i];
+    out[i] = make_uint2(pack_bf162(p.x, p.y), pack_bf162(p.z, p.w));
+}
+
+// closest hit of given rays on the 8-wide BVH (hit-id parity of the precision form)
+__global__ void debug_intersect_wide_kernel(World w, Fast f, uint64_t n, const float* origins, const float* directions,
+                                            const float* t_max, int32_t* hit, float* hit_t) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    WideTraverser<false> tr;
+    uint2 stack[64];
+    tr.init(f, mk(origins[3 * i], origins[3 * i + 1], origins[3 * i + 2]),
+            mk(directions[3 * i], directions[3 * i + 1], directions[3 * i + 2]), t_max ? t_max[i] : kFltMax, -1);
+    while (!tr.step(w, f, stack, nullptr)) {
+    }
+    hit[i] = tr.hit;
+    hit_t[i] = tr.hit_t;
 }
 
 }  // namespace ptd
@@ -300,8 +373,12 @@ constexpr uint64_t kMaxPaths = 1ull << 25;  // paths in flight per group
 
 struct Wavefront {
     Buf o[2], d[2], T[2], hit, color, so, sd, sc, cnt, rec, rec_hits;
+    Buf lists;  // hit list, miss list (capacity entries each)
     Buf pairs, tri4;
+    Buf wide, attr_h, sky_h;  // precision form copies
     bool stale = true;
+    bool wide_ready = false, attr_h_ready = false, sky_h_ready = false;
+    uint64_t wide_count = 0;
     const void* layout_nodes = nullptr;  // world buffers the layouts were built from
     const void* layout_geo = nullptr;
     uint64_t capacity = 0;
@@ -321,13 +398,21 @@ int create(Wavefront** out) {
 void destroy(Wavefront* wf) {
     if (!wf) return;
     for (Buf* b : {&wf->o[0], &wf->o[1], &wf->d[0], &wf->d[1], &wf->T[0], &wf->T[1], &wf->hit, &wf->color, &wf->so,
-                   &wf->sd, &wf->sc, &wf->cnt, &wf->rec, &wf->rec_hits, &wf->pairs, &wf->tri4})
+                   &wf->sd, &wf->sc, &wf->cnt, &wf->rec, &wf->rec_hits, &wf->lists, &wf->pairs, &wf->tri4,
+                   &wf->wide, &wf->attr_h, &wf->sky_h})
         b->release();
     delete wf;
 }
 
 void world_changed(Wavefront* wf) {
-    if (wf) wf->stale = true;
+    if (wf) {
+        wf->stale = true;
+        wf->wide_ready = wf->attr_h_ready = false;
+    }
+}
+
+void sky_changed(Wavefront* wf) {
+    if (wf) wf->sky_h_ready = false;
 }
 
 namespace {
@@ -341,6 +426,26 @@ cudaError_t build_layouts(Wavefront* wf, const ptd::World& w, uint64_t nodes, ui
     wf->stale = false;
     wf->layout_nodes = w.nodes;
     wf->layout_geo = w.geo;
+    wf->wide_ready = wf->attr_h_ready = false;
+    return cudaSuccess;
+}
+
+// the 8-wide BVH: binary nodes back from the device, collapsed and quantised
+// on the host (pt_build_wide_bvh), uploaded
+cudaError_t build_wide(Wavefront* wf, const ptd::World& w, uint64_t nodes, cudaStream_t stream) {
+    std::vector<pt_bvh_node> host(nodes);
+    PTW_TRY(cudaMemcpyAsync(host.data(), w.nodes, nodes * sizeof(pt_bvh_node), cudaMemcpyDeviceToHost, stream));
+    PTW_TRY(cudaStreamSynchronize(stream));
+    uint64_t count = 0;
+    uint32_t depth = 0;
+    if (pt_build_wide_bvh(host.data(), nodes, nullptr, 0, &count, &depth) != PT_OK) return cudaErrorInvalidValue;
+    std::vector<pt_wide_node> wide(count);
+    if (pt_build_wide_bvh(host.data(), nodes, wide.data(), count, &count, &depth) != PT_OK) return cudaErrorInvalidValue;
+    PTW_TRY(wf->wide.reserve(count * sizeof(pt_wide_node)));
+    PTW_TRY(cudaMemcpyAsync(wf->wide.p, wide.data(), count * sizeof(pt_wide_node), cudaMemcpyHostToDevice, stream));
+    PTW_TRY(cudaStreamSynchronize(stream));  // the host vector goes out of scope
+    wf->wide_count = count;
+    wf->wide_ready = true;
     return cudaSuccess;
 }
 
@@ -350,6 +455,7 @@ cudaError_t reserve_paths(Wavefront* wf, uint64_t paths, bool record) {
                    &wf->sd, &wf->sc})
         PTW_TRY(x->reserve(b));
     PTW_TRY(wf->cnt.reserve(64));
+    PTW_TRY(wf->lists.reserve(paths * 8));
     if (record) {
         PTW_TRY(wf->rec.reserve(paths * sizeof(ptd::Counters)));
         PTW_TRY(wf->rec_hits.reserve(paths * PT_RECORD_MAX_BOUNCES * 4));
@@ -368,14 +474,14 @@ int occupancy(K kernel, int threads) {
 // one group of paths through raygen, max_bounces + 1 rounds of extend /
 // shade / shadow, and accumulate; kTri36 reads the reference's 36-byte
 // triangles instead of the padded copy
-template <bool kRec, bool kAlpha, bool kTri36, class TimerF>
+template <bool kRec, bool kAlpha, bool kTri36, bool kWide = false, class TimerF>
 cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const ptd::Queues& q,
                       const ptk::Tile& tile, const ptd::Group& g, ptk::Sinks sinks, cudaStream_t stream,
                       TimerF&& timer) {
     using namespace ptd;
-    const int ext_blocks = sms * occupancy(extend_kernel<kRec, kAlpha, kTri36>, kExtendThreads);
+    const int ext_blocks = sms * occupancy(extend_kernel<kRec, kAlpha, kTri36, kWide>, kExtendThreads);
     const int sha_blocks = sms * occupancy(shade_kernel<kRec, kAlpha>, kShadeThreads);
-    const int shd_blocks = sms * occupancy(shadow_kernel<kRec, kTri36>, kExtendThreads);
+    const int shd_blocks = sms * occupancy(shadow_kernel<kRec, kTri36, kWide>, kExtendThreads);
     PTW_TRY(timer(PT_KC_RAYGEN, [&] {
         raygen_kernel<kRec><<<(g.paths + 255u) / 256u, 256, 0, stream>>>(w, tile, g, q);
         return cudaGetLastError();
@@ -385,7 +491,7 @@ cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const pt
         bounce_reset_kernel<<<1, 1, 0, stream>>>(q.cnt, cur ^ 1);
         PTW_TRY(cudaGetLastError());
         PTW_TRY(timer(PT_KC_EXTEND, [&] {
-            extend_kernel<kRec, kAlpha, kTri36><<<ext_blocks, kExtendThreads, 0, stream>>>(w, f, q, cur, bounce);
+            extend_kernel<kRec, kAlpha, kTri36, kWide><<<ext_blocks, kExtendThreads, 0, stream>>>(w, f, q, cur, bounce);
             return cudaGetLastError();
         }));
         PTW_TRY(timer(PT_KC_SHADE, [&] {
@@ -394,7 +500,7 @@ cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const pt
         }));
         if constexpr (!kAlpha) {
             PTW_TRY(timer(PT_KC_SHADOW, [&] {
-                shadow_kernel<kRec, kTri36><<<shd_blocks, kExtendThreads, 0, stream>>>(w, f, q);
+                shadow_kernel<kRec, kTri36, kWide><<<shd_blocks, kExtendThreads, 0, stream>>>(w, f, q);
                 return cudaGetLastError();
             }));
         }
@@ -413,8 +519,17 @@ cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const pt
 
 }  // namespace
 
-cudaError_t trace(Wavefront* wf, const ptd::World& w, const ptk::Tile& tile, uint32_t first, uint32_t samples,
-                  ptk::Sinks sinks, cudaStream_t stream, const Timer& timer) {
+cudaError_t trace(Wavefront* wf, const ptd::World& w_in, const ptk::Tile& tile, uint32_t first, uint32_t samples,
+                  ptk::Sinks sinks, cudaStream_t stream, const Timer& timer, uint32_t precision) {
+    precision = effective_precision(w_in, precision, sinks.any());
+    ptd::World w = w_in;
+    if (precision & PT_PRECISION_HALF_ATTRIBUTES) {
+        if (!wf->attr_h_ready || !wf->sky_h_ready) return cudaErrorNotReady;  // prepare() first
+        w.attr_h = static_cast<const uint2*>(wf->attr_h.p);
+        w.sky_h = static_cast<const uint2*>(wf->sky_h.p);
+    }
+    const bool wide = (precision & PT_PRECISION_WIDE_BVH) != 0;
+    if (wide && !wf->wide_ready) return cudaErrorNotReady;
     const uint32_t vis_w = tile.tile_w < tile.image_w - tile.origin_x ? tile.tile_w : tile.image_w - tile.origin_x;
     const uint32_t vis_h = tile.tile_h < tile.image_h - tile.origin_y ? tile.tile_h : tile.image_h - tile.origin_y;
     const uint64_t pixels = (uint64_t)vis_w * vis_h;
@@ -439,11 +554,14 @@ cudaError_t trace(Wavefront* wf, const ptd::World& w, const ptk::Tile& tile, uin
     q.sd = static_cast<float4*>(wf->sd.p);
     q.sc = static_cast<float4*>(wf->sc.p);
     q.cnt = static_cast<uint32_t*>(wf->cnt.p);
+    q.hit_list = static_cast<uint32_t*>(wf->lists.p);
+    q.miss_list = q.hit_list + wf->capacity;
     q.rec = static_cast<ptd::Counters*>(wf->rec.p);
     q.rec_hits = static_cast<int32_t*>(wf->rec_hits.p);
     ptd::Fast f;
     f.pairs = reinterpret_cast<const float4*>(static_cast<const char*>(wf->pairs.p) + 32);
     f.tri4 = static_cast<const float4*>(wf->tri4.p);
+    f.wide = static_cast<const float4*>(wf->wide.p);
     for (uint32_t s0 = 0; s0 < samples; s0 += group) {
         ptd::Group g;
         g.vis_w = vis_w;
@@ -457,6 +575,8 @@ cudaError_t trace(Wavefront* wf, const ptd::World& w, const ptk::Tile& tile, uin
         if (record)
             e = w.any_alpha ? run_group<true, true, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer)
                             : run_group<true, false, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer);
+        else if (wide)
+            e = run_group<false, false, false, true>(wf->sms, w, f, q, tile, g, sinks, stream, timer);
         else
             e = w.any_alpha ? run_group<false, true, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer)
                             : run_group<false, false, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer);
@@ -465,9 +585,46 @@ cudaError_t trace(Wavefront* wf, const ptd::World& w, const ptk::Tile& tile, uin
     return cudaSuccess;
 }
 
-cudaError_t prepare(Wavefront* wf, const ptd::World& w, uint64_t nodes, uint64_t tris, cudaStream_t stream) {
-    if (!wf->stale && wf->layout_nodes == w.nodes && wf->layout_geo == w.geo) return cudaSuccess;
-    return build_layouts(wf, w, nodes, tris, stream);
+cudaError_t prepare(Wavefront* wf, const ptd::World& w, uint64_t nodes, uint64_t tris, uint32_t precision,
+                    cudaStream_t stream) {
+    if (wf->stale || wf->layout_nodes != w.nodes || wf->layout_geo != w.geo)
+        PTW_TRY(build_layouts(wf, w, nodes, tris, stream));
+    if ((precision & PT_PRECISION_WIDE_BVH) && !wf->wide_ready) PTW_TRY(build_wide(wf, w, nodes, stream));
+    if ((precision & PT_PRECISION_HALF_ATTRIBUTES) && !wf->attr_h_ready) {
+        PTW_TRY(wf->attr_h.reserve(tris * sizeof(pt_half_attribute)));
+        ptd::half_attributes_kernel<<<(unsigned)((tris + 255) / 256), 256, 0, stream>>>(w.attr, tris,
+                                                                                       static_cast<uint2*>(wf->attr_h.p));
+        PTW_TRY(cudaGetLastError());
+        wf->attr_h_ready = true;
+    }
+    if ((precision & PT_PRECISION_HALF_ATTRIBUTES) && !wf->sky_h_ready) {
+        const uint64_t texels = (uint64_t)w.sky_u.width * w.sky_u.height;
+        PTW_TRY(wf->sky_h.reserve(texels * 8));
+        ptd::bf16_sky_kernel<<<(unsigned)((texels + 255) / 256), 256, 0, stream>>>(w.sky, texels,
+                                                                                  static_cast<uint2*>(wf->sky_h.p));
+        PTW_TRY(cudaGetLastError());
+        wf->sky_h_ready = true;
+    }
+    return cudaSuccess;
+}
+
+uint32_t effective_precision(const ptd::World& w, uint32_t precision, bool record) {
+    if (w.any_alpha || record) precision &= ~PT_PRECISION_WIDE_BVH;
+    return precision;
+}
+
+cudaError_t debug_intersect_wide(Wavefront* wf, const ptd::World& w, uint64_t n, const float* origins,
+                                 const float* directions, const float* t_max, int32_t* hit, float* hit_t,
+                                 cudaStream_t stream) {
+    if (!wf->wide_ready) return cudaErrorNotReady;
+    ptd::Fast f;
+    f.pairs = reinterpret_cast<const float4*>(static_cast<const char*>(wf->pairs.p) + 32);
+    f.tri4 = static_cast<const float4*>(wf->tri4.p);
+    f.wide = static_cast<const float4*>(wf->wide.p);
+    if (n == 0) return cudaSuccess;
+    ptd::debug_intersect_wide_kernel<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(w, f, n, origins, directions,
+                                                                                      t_max, hit, hit_t);
+    return cudaGetLastError();
 }
 
 }  // namespace ptw
@@ -483,7 +640,8 @@ constexpr uint64_t kNoAllocPaths = PT_NOALLOC_MAX_PATHS;
 constexpr size_t kNoAllocQueueBytes = 11ull * 16ull * kNoAllocPaths;  // o, d, T (x2), hit, colour, shadow o/d/c
 constexpr size_t kNoAllocCountersOffset = kNoAllocQueueBytes;
 constexpr size_t kNoAllocLutOffset = kNoAllocCountersOffset + 256;
-static_assert(kNoAllocLutOffset + 1024 <= PT_NOALLOC_SCRATCH_BYTES, "static scratch too small");
+constexpr size_t kNoAllocListOffset = kNoAllocLutOffset + 1024;  // hit list, miss list
+static_assert(kNoAllocListOffset + 2 * 4 * kNoAllocPaths <= PT_NOALLOC_SCRATCH_BYTES, "static scratch too small");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[PT_NOALLOC_SCRATCH_BYTES];
 
@@ -603,6 +761,8 @@ extern "C" int pt_trace_noalloc(const pt_device_world* world, const pt_trace_par
     q.sd = arrays[9];
     q.sc = arrays[10];
     q.cnt = reinterpret_cast<uint32_t*>(base + kNoAllocCountersOffset);
+    q.hit_list = reinterpret_cast<uint32_t*>(base + kNoAllocListOffset);
+    q.miss_list = q.hit_list + kNoAllocPaths;
     q.rec = nullptr;
     q.rec_hits = nullptr;
 

@@ -1,0 +1,238 @@
+// wide_bvh.cpp - host side of the precision form (include/pt_precision.h):
+// the 8-wide BVH collapsed from the reference's binary BVH (world.rs:323-335,
+// 1430-1591) with outward-rounded 8-bit child boxes, and the FP16 attribute
+// conversion.
+//
+// Quantisation.  Per wide node and axis the frame origin is the minimum of
+// the children's box minima and the scale a power of two s = 2^e; a child's
+// lower bound becomes the largest q in [0, 255] with origin + q*s <= lo and
+// its upper bound the smallest q with origin + q*s >= hi, both evaluated in
+// FP32 exactly as the traversal kernel decodes them (q*s is exact, the one
+// addition rounds to nearest).  e is the smallest exponent for which every
+// child's upper bound fits in 8 bits.  Every decoded box therefore contains
+// its binary node's box, and since the slab test is monotone in the box
+// bounds, a wide box test accepts every ray the binary node's test accepts.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/pt_precision.h"
+
+namespace {
+
+constexpr int kMinExp = -126;  // scale stays a normal float
+constexpr int kMaxExp = 104;   // 2^(e + 23) stays finite (the kernel's exact decode)
+constexpr uint32_t kMaxDepth = 64;
+
+float decode(float origin, uint32_t q, float scale) {
+    const float qs = (float)q * scale;  // exact
+    return origin + qs;                 // one rounding, as in the kernel
+}
+
+double half_area(const pt_bvh_node& n) {
+    const double dx = (double)n.aabb_max[0] - n.aabb_min[0];
+    const double dy = (double)n.aabb_max[1] - n.aabb_min[1];
+    const double dz = (double)n.aabb_max[2] - n.aabb_min[2];
+    return dx * dy + dy * dz + dz * dx;
+}
+
+bool finite_box(const pt_bvh_node& n) {
+    for (int a = 0; a < 3; ++a)
+        if (!std::isfinite(n.aabb_min[a]) || !std::isfinite(n.aabb_max[a])) return false;
+    return true;
+}
+
+// quantise one axis of up to 8 child boxes; false if no exponent fits
+bool quantise_axis(float origin, const float* lo, const float* hi, int n, uint8_t* qlo, uint8_t* qhi, uint8_t* ebyte) {
+    double ext = 0.0;
+    for (int i = 0; i < n; ++i) ext = std::fmax(ext, (double)hi[i] - (double)origin);
+    int e = kMinExp;
+    if (ext > 0.0) {
+        int ex = 0;
+        std::frexp(ext / 255.0, &ex);  // ext / 255 < 2^ex
+        e = ex - 1;
+        if (e < kMinExp) e = kMinExp;
+    }
+    for (; e <= kMaxExp; ++e) {
+        const float s = std::ldexp(1.0f, e);
+        bool ok = true;
+        for (int i = 0; i < n && ok; ++i) {
+            double fl = std::floor(((double)lo[i] - (double)origin) / (double)s);
+            int q = fl < 0.0 ? 0 : (fl > 255.0 ? 255 : (int)fl);
+            while (q > 0 && decode(origin, (uint32_t)q, s) > lo[i]) --q;
+            while (q < 255 && decode(origin, (uint32_t)q + 1u, s) <= lo[i]) ++q;
+            if (decode(origin, (uint32_t)q, s) > lo[i]) ok = false;  // cannot happen: q = 0 decodes to origin
+            double ce = std::ceil(((double)hi[i] - (double)origin) / (double)s);
+            if (ce > 256.0) {
+                ok = false;
+                break;
+            }
+            int u = ce < 0.0 ? 0 : (int)ce;
+            while (u <= 255 && decode(origin, (uint32_t)u, s) < hi[i]) ++u;
+            if (u > 255) {
+                ok = false;
+                break;
+            }
+            while (u > 0 && decode(origin, (uint32_t)u - 1u, s) >= hi[i]) --u;
+            qlo[i] = (uint8_t)q;
+            qhi[i] = (uint8_t)u;
+        }
+        if (ok) {
+            *ebyte = (uint8_t)(e + 127);
+            return true;
+        }
+    }
+    return false;
+}
+
+struct Work {
+    uint32_t bnode;  // binary node the wide node is collapsed from
+    uint32_t wide;   // its index
+    uint32_t depth;
+};
+
+}  // namespace
+
+extern "C" int pt_build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, pt_wide_node* out, uint64_t capacity,
+                                 uint64_t* wide_count, uint32_t* wide_depth) {
+    if (!nodes || node_count == 0 || node_count > 0xffffffffull) return PT_ERR_INVALID_ARG;
+    std::vector<pt_wide_node> wide(1);
+    std::memset(wide.data(), 0, sizeof(pt_wide_node));
+    std::vector<Work> stack{{0u, 0u, 1u}};
+    uint32_t max_depth = 0;
+    const auto interior_ok = [&](uint32_t b) {
+        const pt_bvh_node& n = nodes[b];
+        return n.tri_count != 0 || (n.left_first >= 1 && (uint64_t)n.left_first + 1 < node_count);
+    };
+    while (!stack.empty()) {
+        const Work wk = stack.back();
+        stack.pop_back();
+        if (wk.depth > kMaxDepth) return PT_ERR_INVALID_ARG;  // deeper than any traversal stack, or cyclic
+        if (wk.depth > max_depth) max_depth = wk.depth;
+        const pt_bvh_node& b = nodes[wk.bnode];
+        if (!interior_ok(wk.bnode)) return PT_ERR_INVALID_ARG;
+        uint32_t kids[8];
+        int n = 0;
+        if (b.tri_count != 0) {
+            kids[n++] = wk.bnode;  // a leaf root: one leaf child
+        } else {
+            kids[n++] = b.left_first;
+            kids[n++] = b.left_first + 1;
+        }
+        while (n < 8) {
+            int best = -1;
+            double best_area = -1.0;
+            for (int i = 0; i < n; ++i) {
+                if (nodes[kids[i]].tri_count != 0) continue;
+                const double a = half_area(nodes[kids[i]]);
+                if (a > best_area) {
+                    best_area = a;
+                    best = i;
+                }
+            }
+            if (best < 0) break;
+            const uint32_t open = kids[best];
+            if (!interior_ok(open)) return PT_ERR_INVALID_ARG;
+            for (int i = n; i > best + 1; --i) kids[i] = kids[i - 1];
+            kids[best] = nodes[open].left_first;
+            kids[best + 1] = nodes[open].left_first + 1;
+            ++n;
+        }
+        float lo[3][8], hi[3][8];
+        for (int i = 0; i < n; ++i) {
+            const pt_bvh_node& c = nodes[kids[i]];
+            if (!finite_box(c)) return PT_ERR_INVALID_ARG;
+            if (c.tri_count > 0xffffu) return PT_ERR_INVALID_ARG;
+            for (int a = 0; a < 3; ++a) {
+                lo[a][i] = c.aabb_min[a];
+                hi[a][i] = c.aabb_max[a];
+            }
+        }
+        pt_wide_node node;
+        std::memset(&node, 0, sizeof node);
+        node.child_count = (uint8_t)n;
+        node.source_node = wk.bnode;
+        for (int a = 0; a < 3; ++a) {
+            float origin = lo[a][0];
+            for (int i = 1; i < n; ++i) origin = std::fmin(origin, lo[a][i]);
+            node.origin[a] = origin;
+            if (!quantise_axis(origin, lo[a], hi[a], n, node.lo[a], node.hi[a], &node.exponent[a]))
+                return PT_ERR_INVALID_ARG;
+        }
+        const uint32_t first_child = (uint32_t)wide.size();
+        uint32_t next = first_child;
+        for (int i = 0; i < n; ++i) {
+            const pt_bvh_node& c = nodes[kids[i]];
+            if (c.tri_count != 0) {
+                node.child[i] = c.left_first;
+                node.tri_count[i] = (uint16_t)c.tri_count;
+            } else {
+                node.child[i] = next++;
+                node.tri_count[i] = 0;
+            }
+        }
+        if ((uint64_t)next > node_count) return PT_ERR_INVALID_ARG;  // more wide nodes than binary ones: not a tree
+        wide[wk.wide] = node;
+        wide.resize(next);
+        // depth-first: the first interior child is expanded next, siblings stay contiguous
+        for (int i = n - 1; i >= 0; --i)
+            if (node.tri_count[i] == 0) stack.push_back({kids[i], node.child[i], wk.depth + 1});
+    }
+    if (wide_count) *wide_count = wide.size();
+    if (wide_depth) *wide_depth = max_depth;
+    if (!out) return PT_OK;
+    if (capacity < wide.size()) return PT_ERR_OUT_OF_LIMITS;
+    std::memcpy(out, wide.data(), wide.size() * sizeof(pt_wide_node));
+    return PT_OK;
+}
+
+namespace {
+
+// IEEE binary32 -> binary16, round to nearest even
+uint16_t to_half(float f) {
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    const uint32_t sign = (x >> 16) & 0x8000u;
+    const uint32_t ax = x & 0x7fffffffu;
+    if (ax >= 0x7f800000u) return (uint16_t)(sign | (ax > 0x7f800000u ? 0x7e00u : 0x7c00u));
+    if (ax >= 0x477ff000u) return (uint16_t)(sign | 0x7c00u);  // >= 65520 rounds to infinity
+    if (ax < 0x38800000u) {                                    // below 2^-14: subnormal or zero
+        if (ax <= 0x33000000u) return (uint16_t)sign;           // <= 2^-25 rounds to zero
+        const uint32_t e = ax >> 23, m = (ax & 0x7fffffu) | 0x800000u;
+        const uint32_t shift = 126u - e;  // units of 2^-24
+        uint32_t r = m >> shift;
+        const uint32_t rem = m & ((1u << shift) - 1u), halfway = 1u << (shift - 1u);
+        if (rem > halfway || (rem == halfway && (r & 1u))) ++r;
+        return (uint16_t)(sign | r);
+    }
+    uint32_t r = (ax >> 13) - ((127u - 15u) << 10);
+    const uint32_t rem = ax & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (r & 1u))) ++r;
+    return (uint16_t)(sign | r);
+}
+
+}  // namespace
+
+extern "C" void pt_half_attributes(const pt_triangle_attribute* in, uint64_t count, pt_half_attribute* out) {
+    for (uint64_t i = 0; i < count; ++i) {
+        const pt_triangle_attribute& a = in[i];
+        pt_half_attribute& h = out[i];
+        std::memset(&h, 0, sizeof h);
+        for (int k = 0; k < 3; ++k) {
+            h.n0[k] = to_half(a.n0[k]);
+            h.n1[k] = to_half(a.n1[k]);
+            h.n2[k] = to_half(a.n2[k]);
+        }
+        for (int k = 0; k < 4; ++k) {
+            h.t0[k] = to_half(a.t0[k]);
+            h.t1[k] = to_half(a.t1[k]);
+            h.t2[k] = to_half(a.t2[k]);
+        }
+        for (int k = 0; k < 2; ++k) {
+            h.uv0[k] = to_half(a.uv0[k]);
+            h.uv1[k] = to_half(a.uv1[k]);
+            h.uv2[k] = to_half(a.uv2[k]);
+        }
+        h.material_index = a.material_index;
+    }
+}
