@@ -35,6 +35,9 @@ import numpy as np  # noqa: E402
 WIDTH, HEIGHT, SPP, MAX_BOUNCES = 1920, 1080, 64, 8
 METRIC = "Mrays/s"
 KERNEL_NAMES = {"wavefront": 0, "plain": 1}
+# include/pt_precision.h: FP32 (the reference's buffers), 8-wide quantised BVH only, or the full
+# compressed form (wide BVH + FP16 attributes / BF16 skybox + Kahan sums)
+PRECISIONS = {"fp32": 0, "wide": 1, "compressed": 7}
 # DRAM bytes (read + write) per launch of the dominant kernel for this
 # workload, from the ncu capture summarised in profiles/ (None until captured)
 TRAFFIC_PER_LAUNCH: dict = {}
@@ -47,6 +50,7 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--kernel", choices=list(KERNEL_NAMES), default="wavefront")
+    p.add_argument("--precision", choices=list(PRECISIONS), default="fp32")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -270,6 +274,7 @@ def run_ours(args):
     emissive = updates.scene_uniforms.contents.emissive_triangles_count
     tracer = pt.PathTracer(updates, (WIDTH, HEIGHT), device=local_rank)
     tracer.set_kernel(KERNEL_NAMES[args.kernel])
+    tracer.set_precision(PRECISIONS[args.precision])
     tracer.set_max_bounces(MAX_BOUNCES)
 
     spp = args.spp
@@ -373,7 +378,8 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world_size, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": dict(workload_config(world, args.kernel), parallelism=f"replicas x{world_size}"),
+            "config": dict(workload_config(world, args.kernel), precision=args.precision,
+                           parallelism=f"replicas x{world_size}"),
             "rays_per_step": rays_per_step, "samples_per_s": paths_per_step * args.steps * world_size / (elapsed_ms / 1e3),
             "roofline": roofline, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,

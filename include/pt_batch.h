@@ -43,6 +43,10 @@ typedef struct pt_engine_config {
     uint32_t tile_size;         /* work-item tile side in pixels; 0 = 32 */
     uint32_t steps_per_refill;  /* node visits between traversal lane refills; 0 = 32 */
     uint32_t use_graphs;        /* 1 = replay waves from a captured CUDA graph (default), 0 = plain launches */
+    uint32_t precision;         /* PT_PRECISION_* bits of include/pt_precision.h; 0 = the reference's FP32
+                                   buffers.  With PT_PRECISION_HALF_ATTRIBUTES a cached scene keeps only
+                                   the FP16 attributes and BF16 skybox; with PT_PRECISION_WIDE_BVH an
+                                   opaque scene keeps only the 8-wide BVH */
 } pt_engine_config;
 
 int pte_create(const pt_engine_config* config, pt_engine** out);
@@ -82,7 +86,8 @@ int pte_wait_idle(pt_engine* engine, uint32_t timeout_ms);
 #define PT_JOB_RUNNING 1
 #define PT_JOB_DONE 2
 int pte_job_status(pt_engine* engine, uint64_t job_id, int* status, uint32_t* samples_done);
-/* PT_TILE_IMAGE or PT_TILE_ACCUMULATION of a finished job: width * height * 4 floats */
+/* PT_TILE_IMAGE, PT_TILE_ACCUMULATION or (Kahan engines) PT_TILE_COMPENSATION of a
+ * finished job: width * height * 4 floats */
 int pte_job_read(pt_engine* engine, uint64_t job_id, int which, float* host_rgba);
 /* free the job's buffers (a job continued by another keeps them until that one is released) */
 int pte_job_release(pt_engine* engine, uint64_t job_id);

@@ -16,9 +16,13 @@
  *                           binary node's test accepts.  Traversal arithmetic
  *                           stays FP32 and uses the reference's watertight
  *                           triangle test, so each ray's closest hit (triangle,
- *                           t, barycentrics) is the binary traversal's except
- *                           when two triangles have exactly equal t (the
- *                           first found wins, and the wide order differs).
+ *                           t, barycentrics) is the binary traversal's; exact-t
+ *                           ties go to the triangle the binary traversal
+ *                           reaches first (decided from the binary tree's
+ *                           parent links).  For a ray with a zero direction
+ *                           component the reference's slab test is not a
+ *                           bound (0 * inf); the wide test then returns the
+ *                           same hit or a nearer one, never a farther one.
  *   PT_PRECISION_HALF_ATTRIBUTES  shading normals, tangents and UVs stored as
  *                           FP16 (64 B per triangle instead of 112 B) and
  *                           skybox texels as BF16 (8 B instead of 16 B).
@@ -51,7 +55,7 @@ extern "C" {
  * with the product exact and one FP32 round-to-nearest addition; every
  * decoded box contains the binary node it stands for.  tri_count[i] == 0
  * marks an interior child (child[i] = its wide node index); otherwise the
- * child is a leaf of the binary BVH with triangles
+ * child is a binary leaf, or a merged binary subtree, with triangles
  * [child[i], child[i] + tri_count[i]). */
 typedef struct pt_wide_node {
     float origin[3];
@@ -77,12 +81,14 @@ typedef struct pt_half_attribute {
 /* Collapse a binary BVH (the reference's layout, root at 0) into 8-wide
  * nodes: each wide node starts from a binary interior node's two children
  * and repeatedly opens its interior child of largest surface area until it
- * has 8 children or only leaves.  Runs on the host.  `out` may be NULL to
- * query the count.  PT_ERR_INVALID_ARG for a malformed tree, non-finite
- * boxes or a leaf of more than 65535 triangles; PT_ERR_OUT_OF_LIMITS if
- * `capacity` is too small. */
-int pt_build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, pt_wide_node* out, uint64_t capacity,
-                      uint64_t* wide_count, uint32_t* wide_depth);
+ * has 8 children or only leaves.  A binary subtree of at most
+ * max_leaf_triangles triangles (0: none) becomes one leaf child over its
+ * contiguous triangle range.  Runs on the host.  `out` may be NULL to query
+ * the count.  PT_ERR_INVALID_ARG for a malformed tree, non-finite boxes or
+ * a leaf of more than 65535 triangles; PT_ERR_OUT_OF_LIMITS if `capacity`
+ * is too small. */
+int pt_build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, uint32_t max_leaf_triangles,
+                      pt_wide_node* out, uint64_t capacity, uint64_t* wide_count, uint32_t* wide_depth);
 
 /* FP32 attributes -> FP16 (host-side reference of the device conversion). */
 void pt_half_attributes(const pt_triangle_attribute* in, uint64_t count, pt_half_attribute* out);

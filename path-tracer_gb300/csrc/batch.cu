@@ -18,8 +18,13 @@
 #include <thread>
 #include <vector>
 
+#include <type_traits>
+
 #include "../../include/pt_batch.h"
+#include "../../include/pt_precision.h"
+#include "pt_links.h"
 #include "pt_wave.cuh"
+#include "pt_wavefront.h"
 
 namespace ptb {
 
@@ -36,6 +41,7 @@ struct JobDev {
     pt_camera camera;
     float4* accum;
     float4* image;
+    float4* comp;  // Kahan compensation (precision form), else null
 };
 
 struct ItemDev {
@@ -128,12 +134,13 @@ __global__ void reset_kernel(uint32_t* cnt, int next) {
     cnt[6] = 0u;
 }
 
-template <bool kAlpha>
-__global__ void __launch_bounds__(kExtendThreads) extend_kernel(const SceneDev* scenes, WaveBufs b, int cur,
+template <bool kAlpha, bool kWide>
+__global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : 1) extend_kernel(const SceneDev* scenes, WaveBufs b, int cur,
                                                                 uint32_t steps_per_refill) {
+    static_assert(!(kAlpha && kWide), "the wide form runs opaque scenes only");
     const Stage st = stage_of(b.q, cur);
     const uint32_t count = *st.count;
-    Traverser<false, kAlpha, false> tr;
+    typename std::conditional<kWide, WideTraverser<false>, Traverser<false, kAlpha, false>>::type tr;
     uint2 stack[64];
     uint32_t istack[1];
     const SceneDev* sc = scenes;
@@ -219,10 +226,11 @@ __global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kern
     }
 }
 
-__global__ void __launch_bounds__(kExtendThreads) shadow_kernel(const SceneDev* scenes, WaveBufs b,
+template <bool kWide>
+__global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : 1) shadow_kernel(const SceneDev* scenes, WaveBufs b,
                                                                 uint32_t steps_per_refill) {
     const uint32_t count = b.q.cnt[2];
-    Traverser<false, false, true> tr;
+    typename std::conditional<kWide, WideTraverser<true>, Traverser<false, false, true>>::type tr;
     uint2 stack[64];
     uint32_t istack[1];
     const SceneDev* sc = scenes;
@@ -267,9 +275,26 @@ __global__ void __launch_bounds__(256) accumulate_kernel(const Ctrl* ctrl, const
                 acc = mk(a.x, a.y, a.z);
             }
             uint32_t n = it.first_sample;
-            for (uint32_t s = 0; s < it.samples; ++s, ++n) {
-                const float4 c = b.q.color[off + s * px_count + pix];
-                acc = (n > 1u ? acc : mk(0.0f, 0.0f, 0.0f)) + mk(c.x, c.y, c.z);
+            if (job.comp) {
+                // Kahan-compensated sums; the first sample is 0 + L with zero compensation
+                f3 comp = mk(0.0f, 0.0f, 0.0f);
+                if (it.first_sample > 1u) {
+                    const float4 k = job.comp[idx];
+                    comp = mk(k.x, k.y, k.z);
+                }
+                for (uint32_t s = 0; s < it.samples; ++s, ++n) {
+                    const float4 c = b.q.color[off + s * px_count + pix];
+                    const f3 y = mk(c.x, c.y, c.z) - comp;
+                    const f3 sum = acc + y;
+                    comp = (sum - acc) - y;
+                    acc = sum;
+                }
+                job.comp[idx] = make_float4(comp.x, comp.y, comp.z, 0.0f);
+            } else {
+                for (uint32_t s = 0; s < it.samples; ++s, ++n) {
+                    const float4 c = b.q.color[off + s * px_count + pix];
+                    acc = (n > 1u ? acc : mk(0.0f, 0.0f, 0.0f)) + mk(c.x, c.y, c.z);
+                }
             }
             n -= 1u;
             job.accum[idx] = make_float4(acc.x, acc.y, acc.z, 1.0f);
@@ -326,6 +351,7 @@ struct Scene {
     int job_refs = 0;     // accumulations using it
     uint64_t last_use = 0;
     Buf geo, attr, mat, nodes, srgb, linear, sky, sky_alias, scene_alias, lut, pairs, tri4;
+    Buf wide, links, attr_h, sky_h;  // precision form (links: parent per node, leaf per triangle)
 };
 
 struct Accumulation {
@@ -336,7 +362,7 @@ struct Accumulation {
     bool busy = false;
     uint64_t bytes = 0;
     int job_refs = 0;
-    Buf accum, image;
+    Buf accum, image, comp;
     std::deque<uint64_t> waiting;  // jobs queued behind the running pass
 };
 
@@ -507,7 +533,7 @@ int occupancy(K kernel, int threads) {
 }
 
 // the launches of one wave (captured into a graph, or issued directly)
-template <bool kAlpha>
+template <bool kAlpha, bool kWideBvh>
 cudaError_t issue_wave(pt_engine* e) {
     const cudaStream_t s = e->stream;
     const ItemDev* ring = e->d_ring.as<const ItemDev>();
@@ -517,15 +543,16 @@ cudaError_t issue_wave(pt_engine* e) {
     const int per_wave_blocks = e->sms * 8;
     plan_kernel<<<1, 32, 0, s>>>(ctrl, ring, e->ring_cap, e->cfg.wave_paths, e->max_items, e->wb);
     raygen_kernel<<<per_wave_blocks, 256, 0, s>>>(ctrl, ring, jobs, e->wb);
-    const int ext = e->sms * occupancy(extend_kernel<kAlpha>, kExtendThreads);
+    constexpr bool kWide = kWideBvh && !kAlpha;
+    const int ext = e->sms * occupancy(extend_kernel<kAlpha, kWide>, kExtendThreads);
     const int sha = e->sms * occupancy(shade_kernel<kAlpha>, kShadeThreads);
-    const int shd = e->sms * occupancy(shadow_kernel, kExtendThreads);
+    const int shd = e->sms * occupancy(shadow_kernel<kWide>, kExtendThreads);
     int cur = 0;
     for (uint32_t bounce = 0; bounce < kRounds; ++bounce) {
         reset_kernel<<<1, 1, 0, s>>>(e->wb.q.cnt, cur ^ 1);
-        extend_kernel<kAlpha><<<ext, kExtendThreads, 0, s>>>(scenes, e->wb, cur, e->cfg.steps_per_refill);
+        extend_kernel<kAlpha, kWide><<<ext, kExtendThreads, 0, s>>>(scenes, e->wb, cur, e->cfg.steps_per_refill);
         shade_kernel<kAlpha><<<sha, kShadeThreads, 0, s>>>(scenes, jobs, e->wb, cur, bounce);
-        if constexpr (!kAlpha) shadow_kernel<<<shd, kExtendThreads, 0, s>>>(scenes, e->wb, e->cfg.steps_per_refill);
+        if constexpr (!kAlpha) shadow_kernel<kWide><<<shd, kExtendThreads, 0, s>>>(scenes, e->wb, e->cfg.steps_per_refill);
         cur ^= 1;
     }
     accumulate_kernel<<<per_wave_blocks, 256, 0, s>>>(ctrl, ring, jobs, e->wb, e->d_done.as<uint32_t>());
@@ -534,13 +561,19 @@ cudaError_t issue_wave(pt_engine* e) {
     return cudaGetLastError();
 }
 
+cudaError_t issue_any_wave(pt_engine* e, bool alpha) {
+    const bool wide = (e->cfg.precision & PT_PRECISION_WIDE_BVH) != 0;
+    if (alpha) return issue_wave<true, false>(e);
+    return wide ? issue_wave<false, true>(e) : issue_wave<false, false>(e);
+}
+
 int launch_wave(pt_engine* e, bool alpha) {
     const int gi = alpha ? 1 : 0;
     if (e->cfg.use_graphs && !e->graph[gi]) {
         cudaGraph_t g = nullptr;
         int rc = e->cuda(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
         if (rc) return rc;
-        const cudaError_t le = alpha ? issue_wave<true>(e) : issue_wave<false>(e);
+        const cudaError_t le = issue_any_wave(e, alpha);
         const cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
         if ((rc = e->cuda(le, "wave capture"))) return rc;
         if ((rc = e->cuda(ce, "graph capture"))) return rc;
@@ -554,7 +587,7 @@ int launch_wave(pt_engine* e, bool alpha) {
     if (e->cfg.use_graphs)
         rc = e->cuda(cudaGraphLaunch(e->graph[gi], e->stream), "graph launch");
     else
-        rc = e->cuda(alpha ? issue_wave<true>(e) : issue_wave<false>(e), "wave launch");
+        rc = e->cuda(issue_any_wave(e, alpha), "wave launch");
     if (rc) return rc;
     cudaEventRecord(f.stop, e->stream);
     e->flights.push_back(f);
@@ -585,6 +618,7 @@ int start_job(pt_engine* e, Job& j) {
     jd.camera = j.camera;
     jd.accum = a.accum.as<float4>();
     jd.image = a.image.as<float4>();
+    jd.comp = a.comp.p ? a.comp.as<float4>() : nullptr;
     int rc = e->cuda(cudaMemcpyAsync(e->d_jobs.as<JobDev>() + a.slot, &jd, sizeof jd, cudaMemcpyHostToDevice, e->stream),
                      "job record");
     if (rc) return rc;
@@ -630,6 +664,7 @@ void free_accumulation(pt_engine* e, Accumulation& a) {
     e->used -= a.bytes;
     a.accum.release();
     a.image.release();
+    a.comp.release();
     e->slots[a.slot].reset();
     auto it = e->scenes.find(a.scene);
     if (it != e->scenes.end()) it->second->job_refs -= 1;
@@ -691,10 +726,20 @@ int pump(pt_engine* e) {
     return PT_OK;
 }
 
+// which derived copies a cached scene keeps: the binary BVH always (waves
+// with non-opaque jobs traverse it), the wide BVH for opaque scenes of a wide
+// engine, and FP16 attributes / BF16 skybox in place of the FP32 ones
+struct SceneForm {
+    bool wide, half;
+};
+SceneForm scene_form(const pt_engine* e, bool any_alpha);
+
 int upload_scene(pt_engine* e, Scene& s, const pt_world_updates* u) {
     const pt_scene_upload* sc = u->scene;
     const pt_skybox_upload* sk = u->skybox;
     const size_t layer = (size_t)PT_ATLAS_SIZE * PT_ATLAS_SIZE * 4;
+    const SceneForm form = scene_form(e, s.any_alpha);
+    const uint64_t texels = (uint64_t)sk->uniforms.width * sk->uniforms.height;
     auto put = [&](Buf& b, const void* src, size_t n, const char* what) {
         int rc = e->cuda(b.alloc(n), what);
         if (!rc && n) rc = e->cuda(cudaMemcpyAsync(b.p, src, n, cudaMemcpyHostToDevice, e->stream), what);
@@ -706,7 +751,36 @@ int upload_scene(pt_engine* e, Scene& s, const pt_world_updates* u) {
     if (!rc) rc = put(s.nodes, sc->bvh_nodes, sc->node_count * 32, "BVH");
     if (!rc) rc = put(s.srgb, sc->srgb_texture_atlases, sc->srgb_atlas_count * layer, "atlases");
     if (!rc) rc = put(s.linear, sc->linear_texture_atlases, sc->linear_atlas_count * layer, "atlases");
-    if (!rc) rc = put(s.sky, sk->rgba, (size_t)sk->uniforms.width * sk->uniforms.height * 16, "skybox");
+    if (!rc) rc = put(s.sky, sk->rgba, texels * 16, "skybox");
+    if (!rc && form.half) {
+        // narrow copies on the device; the FP32 ones are dropped once converted
+        rc = e->cuda(s.attr_h.alloc(sc->triangle_count * sizeof(pt_half_attribute)), "FP16 attributes");
+        if (!rc) rc = e->cuda(ptw::convert_half_attributes(s.attr.as<pt_triangle_attribute>(), sc->triangle_count,
+                                                           s.attr_h.as<uint2>(), e->stream), "FP16 attributes");
+        if (!rc) rc = e->cuda(s.sky_h.alloc(texels * 8), "BF16 skybox");
+        if (!rc) rc = e->cuda(ptw::convert_bf16_sky(s.sky.as<float4>(), texels, s.sky_h.as<uint2>(), e->stream),
+                              "BF16 skybox");
+        if (!rc) rc = e->cuda(cudaStreamSynchronize(e->stream), "narrow copies");
+        if (!rc) {
+            s.attr.release();
+            s.sky.release();
+        }
+    }
+    if (!rc && form.wide) {
+        uint64_t count = 0;
+        uint32_t depth = 0;
+        if (pt_build_wide_bvh(sc->bvh_nodes, sc->node_count, kWideLeafMerge, nullptr, 0, &count, &depth) != PT_OK)
+            return e->fail(PT_ERR_INVALID_ARG, "the BVH cannot be collapsed into 8-wide nodes");
+        std::vector<pt_wide_node> wide(count);
+        pt_build_wide_bvh(sc->bvh_nodes, sc->node_count, kWideLeafMerge, wide.data(), count, &count, &depth);
+        std::vector<uint32_t> links(sc->node_count + sc->triangle_count);
+        if (!ptw::build_bvh_links(sc->bvh_nodes, sc->node_count, sc->triangle_count, links.data(),
+                                  links.data() + sc->node_count))
+            return e->fail(PT_ERR_INVALID_ARG, "BVH child or triangle range out of bounds");
+        rc = put(s.wide, wide.data(), count * sizeof(pt_wide_node), "wide BVH");
+        if (!rc) rc = put(s.links, links.data(), links.size() * 4, "BVH links");
+        if (!rc) rc = e->cuda(cudaStreamSynchronize(e->stream), "wide BVH");  // the host copies go out of scope
+    }
     if (!rc) rc = put(s.sky_alias, sk->alias_table, sk->alias_count * 12, "skybox aliases");
     if (!rc) rc = put(s.scene_alias, u->scene_alias_table, u->scene_alias_count * 16, "scene aliases");
     float lut[256];
@@ -729,14 +803,16 @@ int upload_scene(pt_engine* e, Scene& s, const pt_world_updates* u) {
     SceneDev d{};
     World& w = d.w;
     w.geo = s.geo.as<pt_triangle_geometry>();
-    w.attr = s.attr.as<pt_triangle_attribute>();
+    w.attr = s.attr.p ? s.attr.as<pt_triangle_attribute>() : nullptr;
+    w.attr_h = s.attr_h.p ? s.attr_h.as<uint2>() : nullptr;
     w.mat = s.mat.as<pt_material>();
     w.nodes = s.nodes.as<pt_bvh_node>();
     w.srgb = sc->srgb_atlas_count ? s.srgb.as<uint8_t>() : nullptr;
     w.linear = sc->linear_atlas_count ? s.linear.as<uint8_t>() : nullptr;
     w.srgb_count = sc->srgb_atlas_count;
     w.linear_count = sc->linear_atlas_count;
-    w.sky = s.sky.as<float4>();
+    w.sky = s.sky.p ? s.sky.as<float4>() : nullptr;
+    w.sky_h = s.sky_h.p ? s.sky_h.as<uint2>() : nullptr;
     w.sky_alias = s.sky_alias.as<pt_skybox_alias_entry>();
     w.scene_alias = s.scene_alias.as<pt_scene_alias_entry>();
     w.sky_u = *u->skybox_uniforms;
@@ -745,10 +821,20 @@ int upload_scene(pt_engine* e, Scene& s, const pt_world_updates* u) {
     w.any_alpha = s.any_alpha ? 1 : 0;
     d.f.pairs = reinterpret_cast<const float4*>(static_cast<const char*>(s.pairs.p) + 32);
     d.f.tri4 = s.tri4.as<float4>();
+    d.f.wide = s.wide.p ? s.wide.as<float4>() : nullptr;
+    d.f.parent = s.links.p ? s.links.as<uint32_t>() : nullptr;
+    d.f.leaf_of = s.links.p ? s.links.as<uint32_t>() + sc->node_count : nullptr;
     rc = e->cuda(cudaMemcpyAsync(e->d_scenes.as<SceneDev>() + s.slot, &d, sizeof d, cudaMemcpyHostToDevice, e->stream),
                  "scene record");
     if (!rc) rc = e->cuda(cudaStreamSynchronize(e->stream), "scene upload");
     return rc;
+}
+
+SceneForm scene_form(const pt_engine* e, bool any_alpha) {
+    SceneForm f;
+    f.wide = (e->cfg.precision & PT_PRECISION_WIDE_BVH) != 0 && !any_alpha;
+    f.half = (e->cfg.precision & PT_PRECISION_HALF_ATTRIBUTES) != 0;
+    return f;
 }
 
 bool evict_one(pt_engine* e) {
@@ -780,6 +866,8 @@ int pte_create(const pt_engine_config* cfg, pt_engine** out) {
     int rc = PT_OK;
     if (e->cfg.tile_size > 256 || e->cfg.wave_paths < (1u << 12) || e->cfg.wave_paths > (1u << 28))
         rc = e->fail(PT_ERR_INVALID_ARG, "tile_size must be at most 256 and wave_paths in [4096, 2^28]");
+    if (!rc && (e->cfg.precision & ~PT_PRECISION_COMPRESSED))
+        rc = e->fail(PT_ERR_INVALID_ARG, "unknown precision bits");
     if (!rc) rc = e->cuda(cudaSetDevice(e->cfg.device), "cudaSetDevice");
     if (!rc) rc = e->cuda(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "stream");
     if (!rc) rc = e->cuda(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, e->cfg.device), "SM count");
@@ -905,10 +993,17 @@ int pte_scene_add(pt_engine* e, const pt_world_updates* u, uint64_t* scene_id) {
         *scene_id = h;
         return PT_OK;
     }
-    const uint64_t bytes = sc->triangle_count * (36 + 112 + 48) + sc->material_count * 224 + sc->node_count * 64 + 512 +
-                           (sc->srgb_atlas_count + sc->linear_atlas_count) * layer +
-                           (uint64_t)sk->uniforms.width * sk->uniforms.height * 16 + sk->alias_count * 12 +
-                           u->scene_alias_count * 16 + 1024;
+    bool any_alpha = false;
+    for (uint64_t i = 0; i < sc->material_count; ++i) any_alpha |= sc->materials[i].alpha_mode != PT_ALPHA_MODE_OPAQUE;
+    const SceneForm form = scene_form(e, any_alpha);
+    const uint64_t texels = (uint64_t)sk->uniforms.width * sk->uniforms.height;
+    uint64_t bytes = sc->triangle_count * (36 + 48) + sc->material_count * 224 + 512 +
+                     (sc->srgb_atlas_count + sc->linear_atlas_count) * layer + sk->alias_count * 12 +
+                     u->scene_alias_count * 16 + 1024;
+    bytes += form.half ? sc->triangle_count * 64 + texels * 8 : sc->triangle_count * 112 + texels * 16;
+    bytes += sc->node_count * 64 + 256;             // binary nodes + child-pair copy
+    bytes += form.wide ? sc->node_count * (64 + 4) + sc->triangle_count * 4 : 0;  // wide nodes (at most one per
+                                                                                   // two binary nodes) + links
     while (e->used + bytes > e->budget && evict_one(e)) {
     }
     if (e->used + bytes > e->budget) return hbm_fail(e->error, "the scene", bytes, e->used, e->budget);
@@ -932,7 +1027,7 @@ int pte_scene_add(pt_engine* e, const pt_world_updates* u, uint64_t* scene_id) {
     s->bytes = bytes;
     s->caller_refs = 1;
     s->last_use = e->use_clock;
-    for (uint64_t i = 0; i < sc->material_count; ++i) s->any_alpha |= sc->materials[i].alpha_mode != PT_ALPHA_MODE_OPAQUE;
+    s->any_alpha = any_alpha;
     int rc = upload_scene(e, *s, u);
     if (rc) return rc;
     e->scene_slots[slot] = h;
@@ -978,7 +1073,8 @@ int pte_submit(pt_engine* e, const pt_job_desc* d, uint64_t* job_id) {
                 break;
             }
         if (slot == kMaxSlots) return e->fail(PT_ERR_OUT_OF_LIMITS, "too many live jobs");
-        const uint64_t bytes = (uint64_t)d->width * d->height * 32;
+        const bool kahan = (e->cfg.precision & PT_PRECISION_KAHAN) != 0;
+        const uint64_t bytes = (uint64_t)d->width * d->height * (kahan ? 48 : 32);
         while (e->used + bytes > e->budget && evict_one(e)) {
         }
         if (e->used + bytes > e->budget) return hbm_fail(e->error, "the job's accumulation", bytes, e->used, e->budget);
@@ -989,8 +1085,10 @@ int pte_submit(pt_engine* e, const pt_job_desc* d, uint64_t* job_id) {
         a->height = d->height;
         a->max_bounces = d->max_bounces;
         a->bytes = bytes;
-        int rc = e->cuda(a->accum.alloc(bytes / 2), "accumulation buffer");
-        if (!rc) rc = e->cuda(a->image.alloc(bytes / 2), "image buffer");
+        const size_t plane = (size_t)d->width * d->height * 16;
+        int rc = e->cuda(a->accum.alloc(plane), "accumulation buffer");
+        if (!rc) rc = e->cuda(a->image.alloc(plane), "image buffer");
+        if (!rc && kahan) rc = e->cuda(a->comp.alloc(plane), "Kahan compensation");
         if (rc) return rc;
         e->used += bytes;
         e->slots[slot] = a;
@@ -1060,13 +1158,18 @@ int pte_job_status(pt_engine* e, uint64_t id, int* status, uint32_t* samples_don
 }
 
 int pte_job_read(pt_engine* e, uint64_t id, int which, float* host) {
-    if (!e || !host || (which != PT_TILE_IMAGE && which != PT_TILE_ACCUMULATION)) return PT_ERR_INVALID_ARG;
+    if (!e || !host || (which != PT_TILE_IMAGE && which != PT_TILE_ACCUMULATION && which != PT_TILE_COMPENSATION))
+        return PT_ERR_INVALID_ARG;
     cudaSetDevice(e->cfg.device);
     auto it = e->jobs.find(id);
     if (it == e->jobs.end() || !it->second.acc) return e->fail(PT_ERR_INVALID_ARG, "unknown job");
     if (it->second.status != PT_JOB_DONE) return e->fail(PT_ERR_STATE, "job not finished");
     Accumulation& a = *it->second.acc;
-    const Buf& b = which == PT_TILE_IMAGE ? a.image : a.accum;
+    if (which == PT_TILE_COMPENSATION && !a.comp.p) {
+        memset(host, 0, (size_t)a.width * a.height * 16);
+        return PT_OK;
+    }
+    const Buf& b = which == PT_TILE_IMAGE ? a.image : (which == PT_TILE_ACCUMULATION ? a.accum : a.comp);
     int rc = e->cuda(cudaMemcpyAsync(host, b.p, (size_t)a.width * a.height * 16, cudaMemcpyDeviceToHost, e->stream), "job readback");
     if (!rc) rc = e->cuda(cudaStreamSynchronize(e->stream), "job readback");
     return rc;

@@ -12,7 +12,10 @@ struct Fast {
     const float4* pairs;  // node i at pairs[2i], pairs[2i+1]
     const float4* tri4;   // triangle i at tri4[3i .. 3i+2]
     const float4* wide = nullptr;  // pt_wide_node i at wide[8i .. 8i+7] (precision form)
+    const uint32_t* parent = nullptr;   // binary node -> its parent (root: 0xffffffff)
+    const uint32_t* leaf_of = nullptr;  // triangle -> the binary leaf holding it
 };
+
 
 struct Queues {
     float4* o[2];
@@ -75,6 +78,19 @@ PTD Stage stage_of(const Queues& q, int cur) {
 // idle lanes of a traversal warp take new rays once fewer than this many are busy
 #ifndef PT_REFILL_BELOW
 #define PT_REFILL_BELOW 32
+#endif
+// binary subtrees of at most this many triangles become one leaf of the 8-wide BVH
+#ifndef PT_WIDE_LEAF_MERGE
+#define PT_WIDE_LEAF_MERGE 0
+#endif
+// 1: a step of the 8-wide traversal tests one triangle of a leaf; 0: the whole leaf
+#ifndef PT_WIDE_TRI_PER_STEP
+#define PT_WIDE_TRI_PER_STEP 1
+#endif
+constexpr uint32_t kWideLeafMerge = PT_WIDE_LEAF_MERGE;
+// resident blocks per SM the 8-wide traversal kernels are compiled for
+#ifndef PT_WIDE_MIN_BLOCKS
+#define PT_WIDE_MIN_BLOCKS 6
 #endif
 // 1: a traversal step tests one triangle of a leaf; 0: a whole leaf
 #ifndef PT_TRI_PER_STEP
@@ -305,6 +321,44 @@ PTD void sort8(uint32_t (&k)[8]) {
 #undef PT_CE
 }
 
+// Whether the reference's binary traversal (trace.slang:786-884) reaches
+// triangle a before triangle b on this ray: in one leaf the lower index
+// first; otherwise at their lowest common ancestor the child the traversal
+// enters first (the nearer accepted child box, ties to the right).  Used
+// only to break exact-t ties the way the reference does (its `t < hit_t`
+// keeps the first triangle found).
+PTD bool binary_first(const Fast& f, f3 o, f3 d, uint32_t a, uint32_t b) {
+    uint32_t la = __ldg(f.leaf_of + a), lb = __ldg(f.leaf_of + b);
+    if (la == lb) return a < b;
+    const auto depth = [&](uint32_t n) {
+        uint32_t k = 0;
+        while (n != 0u && k < 64u) {
+            n = __ldg(f.parent + n);
+            ++k;
+        }
+        return k;
+    };
+    uint32_t da = depth(la), db = depth(lb);
+    for (; da > db; --da) la = __ldg(f.parent + la);
+    for (; db > da; --db) lb = __ldg(f.parent + lb);
+    for (uint32_t k = 0; k < 64u; ++k) {
+        const uint32_t pa = __ldg(f.parent + la), pb = __ldg(f.parent + lb);
+        if (pa == pb) break;
+        la = pa;
+        lb = pb;
+    }
+    // la, lb: the two children of the common ancestor, la on a's side
+    const uint32_t left = la < lb ? la : lb;
+    const f3 rcp = 1.0f / d, nod = -o * rcp;
+    const float4* p = f.pairs + 2 * (size_t)left;
+    const float inf = __int_as_float(0x7f800000);
+    const float dl = box_test(__ldg(p), __ldg(p + 1), nod, rcp, inf);
+    const float dr = box_test(__ldg(p + 2), __ldg(p + 3), nod, rcp, inf);
+    const bool hl = dl >= 0.0f, hr = dr >= 0.0f;
+    const bool go_left = hl && (!hr || dl < dr);
+    return (la == left) == go_left;
+}
+
 // One ray's traversal of the 8-wide BVH of the precision form
 // (include/pt_precision.h), with the same step()/result interface as
 // Traverser.  A visit decodes the node's child boxes exactly as the host
@@ -369,6 +423,8 @@ struct WideTraverser {
         uint32_t k[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
+            k[i] = 0xffffffffu;
+            if ((uint32_t)i >= count) continue;
             // q as the float 2^23 + q, then (2^23 + q) * s - 2^23 * s = q * s exactly
             const unsigned sel = 0x7440u | (unsigned)(i & 3);
             const int wd = i >> 2;
@@ -386,11 +442,13 @@ struct WideTraverser {
             const float t1z = fma_(bmaxz, rcp.z, nod_hi.z);
             const float t_near = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
             const float t_far = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
-            const bool h = (uint32_t)i < count && t_near <= t_far && t_far > 0.0f && t_near < hit_t;
-            if constexpr (kShadow)
-                k[i] = h ? (uint32_t)i : 0xffffffffu;
-            else
-                k[i] = h ? ((__float_as_uint(fmaxf(0.0f, t_near)) & ~7u) | (uint32_t)i) : 0xffffffffu;
+            const bool h = t_near <= t_far && t_far > 0.0f && t_near < hit_t;
+            if (h) {
+                if constexpr (kShadow)
+                    k[i] = (uint32_t)i;
+                else
+                    k[i] = (__float_as_uint(fmaxf(0.0f, t_near)) & ~7u) | (uint32_t)i;
+            }
         }
         if constexpr (!kShadow) sort8(k);
         uint32_t l = 0u, cnt = 0u;
@@ -421,6 +479,11 @@ struct WideTraverser {
                 hv = v;
                 hw = wb;
             }
+        } else if (!kShadow && t == hit_t && hit >= 0 && binary_first(f, o, d, tri, (uint32_t)hit)) {
+            // an exact tie: keep the triangle the binary traversal finds first
+            hit = (int32_t)tri;
+            hv = v;
+            hw = wb;
         }
         return false;
     }
@@ -454,12 +517,20 @@ struct WideTraverser {
             lf = child;
             tri_left = tc;
         }
+#if PT_WIDE_TRI_PER_STEP
         const uint32_t tri = lf;
         lf += 1u;
         tri_left -= 1u;
         bool skip = false;
         if constexpr (kShadow) skip = (int32_t)tri == light_tri;
         return !skip && test_triangle(w, f, tri);
+#else
+        for (; tri_left > 0u; --tri_left, ++lf) {
+            if (kShadow && (int32_t)lf == light_tri) continue;
+            if (test_triangle(w, f, lf)) return true;
+        }
+        return false;
+#endif
     }
 };
 

@@ -47,6 +47,11 @@ uint32_t effective_precision(const ptd::World& w, uint32_t precision, bool recor
 cudaError_t trace(Wavefront* wf, const ptd::World& w, const ptk::Tile& tile, uint32_t first_sample,
                   uint32_t samples, ptk::Sinks sinks, cudaStream_t stream, const Timer& timer, uint32_t precision);
 
+// the narrow copies of the precision form, on `stream`: FP32 attributes ->
+// pt_half_attribute records (8 uint2 each), RGBA32F texels -> BF16 RGBA
+cudaError_t convert_half_attributes(const pt_triangle_attribute* in, uint64_t n, uint2* out, cudaStream_t stream);
+cudaError_t convert_bf16_sky(const float4* in, uint64_t n, uint2* out, cudaStream_t stream);
+
 // closest hit of given rays through the 8-wide BVH (prepare with
 // PT_PRECISION_WIDE_BVH first); device arrays
 cudaError_t debug_intersect_wide(Wavefront* wf, const ptd::World& w, uint64_t n, const float* origins,

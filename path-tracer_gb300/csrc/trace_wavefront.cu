@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/pt_precision.h"
+#include "pt_links.h"
 #include "pt_wave.cuh"
 #include "pt_wavefront.h"
 
@@ -83,7 +84,7 @@ __global__ void bounce_reset_kernel(uint32_t* cnt, int next) {
 // are filed under hits or misses for the shading kernel.  kWide traverses the
 // 8-wide BVH of the precision form instead of the binary one.
 template <bool kRec, bool kAlpha, bool kTri36 = false, bool kWide = false>
-__global__ void __launch_bounds__(kExtendThreads, PT_EXTEND_MIN_BLOCKS) extend_kernel(World w, Fast f, Queues q, int cur, uint32_t bounce) {
+__global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : PT_EXTEND_MIN_BLOCKS) extend_kernel(World w, Fast f, Queues q, int cur, uint32_t bounce) {
     static_assert(!(kWide && (kRec || kAlpha)), "the wide form keeps no records and runs opaque scenes only");
     const Stage st = stage_of(q, cur);
     const uint32_t count = *st.count;
@@ -181,7 +182,7 @@ __global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kern
 // Persistent shadow kernel (opaque scenes): any-hit traversal of every queued
 // shadow ray with the same lane refill; unoccluded rays add their light.
 template <bool kRec, bool kTri36 = false, bool kWide = false>
-__global__ void __launch_bounds__(kExtendThreads, PT_EXTEND_MIN_BLOCKS) shadow_kernel(World w, Fast f, Queues q) {
+__global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : PT_EXTEND_MIN_BLOCKS) shadow_kernel(World w, Fast f, Queues q) {
     static_assert(!(kWide && kRec), "the wide form keeps no records");
     const uint32_t count = q.cnt[2];
     typename std::conditional<kWide, WideTraverser<true, kTri36>, Traverser<kRec, false, true, kTri36>>::type tr;
@@ -375,10 +376,11 @@ struct Wavefront {
     Buf o[2], d[2], T[2], hit, color, so, sd, sc, cnt, rec, rec_hits;
     Buf lists;  // hit list, miss list (capacity entries each)
     Buf pairs, tri4;
-    Buf wide, attr_h, sky_h;  // precision form copies
+    Buf wide, links, attr_h, sky_h;  // precision form copies (links: parent per node, leaf per triangle)
     bool stale = true;
     bool wide_ready = false, attr_h_ready = false, sky_h_ready = false;
     uint64_t wide_count = 0;
+    uint64_t links_nodes = 0;  // node count of the links array (leaf_of follows the parents)
     const void* layout_nodes = nullptr;  // world buffers the layouts were built from
     const void* layout_geo = nullptr;
     uint64_t capacity = 0;
@@ -399,7 +401,7 @@ void destroy(Wavefront* wf) {
     if (!wf) return;
     for (Buf* b : {&wf->o[0], &wf->o[1], &wf->d[0], &wf->d[1], &wf->T[0], &wf->T[1], &wf->hit, &wf->color, &wf->so,
                    &wf->sd, &wf->sc, &wf->cnt, &wf->rec, &wf->rec_hits, &wf->lists, &wf->pairs, &wf->tri4,
-                   &wf->wide, &wf->attr_h, &wf->sky_h})
+                   &wf->wide, &wf->links, &wf->attr_h, &wf->sky_h})
         b->release();
     delete wf;
 }
@@ -432,18 +434,25 @@ cudaError_t build_layouts(Wavefront* wf, const ptd::World& w, uint64_t nodes, ui
 
 // the 8-wide BVH: binary nodes back from the device, collapsed and quantised
 // on the host (pt_build_wide_bvh), uploaded
-cudaError_t build_wide(Wavefront* wf, const ptd::World& w, uint64_t nodes, cudaStream_t stream) {
+cudaError_t build_wide(Wavefront* wf, const ptd::World& w, uint64_t nodes, uint64_t tris, cudaStream_t stream) {
     std::vector<pt_bvh_node> host(nodes);
     PTW_TRY(cudaMemcpyAsync(host.data(), w.nodes, nodes * sizeof(pt_bvh_node), cudaMemcpyDeviceToHost, stream));
     PTW_TRY(cudaStreamSynchronize(stream));
     uint64_t count = 0;
     uint32_t depth = 0;
-    if (pt_build_wide_bvh(host.data(), nodes, nullptr, 0, &count, &depth) != PT_OK) return cudaErrorInvalidValue;
+    if (pt_build_wide_bvh(host.data(), nodes, ptd::kWideLeafMerge, nullptr, 0, &count, &depth) != PT_OK)
+        return cudaErrorInvalidValue;
     std::vector<pt_wide_node> wide(count);
-    if (pt_build_wide_bvh(host.data(), nodes, wide.data(), count, &count, &depth) != PT_OK) return cudaErrorInvalidValue;
+    if (pt_build_wide_bvh(host.data(), nodes, ptd::kWideLeafMerge, wide.data(), count, &count, &depth) != PT_OK)
+        return cudaErrorInvalidValue;
+    std::vector<uint32_t> links(nodes + tris);
+    if (!ptw::build_bvh_links(host.data(), nodes, tris, links.data(), links.data() + nodes)) return cudaErrorInvalidValue;
     PTW_TRY(wf->wide.reserve(count * sizeof(pt_wide_node)));
     PTW_TRY(cudaMemcpyAsync(wf->wide.p, wide.data(), count * sizeof(pt_wide_node), cudaMemcpyHostToDevice, stream));
-    PTW_TRY(cudaStreamSynchronize(stream));  // the host vector goes out of scope
+    PTW_TRY(wf->links.reserve(links.size() * 4));
+    PTW_TRY(cudaMemcpyAsync(wf->links.p, links.data(), links.size() * 4, cudaMemcpyHostToDevice, stream));
+    PTW_TRY(cudaStreamSynchronize(stream));  // the host vectors go out of scope
+    wf->links_nodes = nodes;
     wf->wide_count = count;
     wf->wide_ready = true;
     return cudaSuccess;
@@ -562,6 +571,8 @@ cudaError_t trace(Wavefront* wf, const ptd::World& w_in, const ptk::Tile& tile, 
     f.pairs = reinterpret_cast<const float4*>(static_cast<const char*>(wf->pairs.p) + 32);
     f.tri4 = static_cast<const float4*>(wf->tri4.p);
     f.wide = static_cast<const float4*>(wf->wide.p);
+    f.parent = static_cast<const uint32_t*>(wf->links.p);
+    f.leaf_of = f.parent ? f.parent + wf->links_nodes : nullptr;
     for (uint32_t s0 = 0; s0 < samples; s0 += group) {
         ptd::Group g;
         g.vis_w = vis_w;
@@ -589,23 +600,31 @@ cudaError_t prepare(Wavefront* wf, const ptd::World& w, uint64_t nodes, uint64_t
                     cudaStream_t stream) {
     if (wf->stale || wf->layout_nodes != w.nodes || wf->layout_geo != w.geo)
         PTW_TRY(build_layouts(wf, w, nodes, tris, stream));
-    if ((precision & PT_PRECISION_WIDE_BVH) && !wf->wide_ready) PTW_TRY(build_wide(wf, w, nodes, stream));
+    if ((precision & PT_PRECISION_WIDE_BVH) && !wf->wide_ready) PTW_TRY(build_wide(wf, w, nodes, tris, stream));
     if ((precision & PT_PRECISION_HALF_ATTRIBUTES) && !wf->attr_h_ready) {
         PTW_TRY(wf->attr_h.reserve(tris * sizeof(pt_half_attribute)));
-        ptd::half_attributes_kernel<<<(unsigned)((tris + 255) / 256), 256, 0, stream>>>(w.attr, tris,
-                                                                                       static_cast<uint2*>(wf->attr_h.p));
-        PTW_TRY(cudaGetLastError());
+        PTW_TRY(convert_half_attributes(w.attr, tris, static_cast<uint2*>(wf->attr_h.p), stream));
         wf->attr_h_ready = true;
     }
     if ((precision & PT_PRECISION_HALF_ATTRIBUTES) && !wf->sky_h_ready) {
         const uint64_t texels = (uint64_t)w.sky_u.width * w.sky_u.height;
         PTW_TRY(wf->sky_h.reserve(texels * 8));
-        ptd::bf16_sky_kernel<<<(unsigned)((texels + 255) / 256), 256, 0, stream>>>(w.sky, texels,
-                                                                                  static_cast<uint2*>(wf->sky_h.p));
-        PTW_TRY(cudaGetLastError());
+        PTW_TRY(convert_bf16_sky(w.sky, texels, static_cast<uint2*>(wf->sky_h.p), stream));
         wf->sky_h_ready = true;
     }
     return cudaSuccess;
+}
+
+cudaError_t convert_half_attributes(const pt_triangle_attribute* in, uint64_t n, uint2* out, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    ptd::half_attributes_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(in, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t convert_bf16_sky(const float4* in, uint64_t n, uint2* out, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    ptd::bf16_sky_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(in, n, out);
+    return cudaGetLastError();
 }
 
 uint32_t effective_precision(const ptd::World& w, uint32_t precision, bool record) {
@@ -621,6 +640,8 @@ cudaError_t debug_intersect_wide(Wavefront* wf, const ptd::World& w, uint64_t n,
     f.pairs = reinterpret_cast<const float4*>(static_cast<const char*>(wf->pairs.p) + 32);
     f.tri4 = static_cast<const float4*>(wf->tri4.p);
     f.wide = static_cast<const float4*>(wf->wide.p);
+    f.parent = static_cast<const uint32_t*>(wf->links.p);
+    f.leaf_of = f.parent + wf->links_nodes;
     if (n == 0) return cudaSuccess;
     ptd::debug_intersect_wide_kernel<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(w, f, n, origins, directions,
                                                                                       t_max, hit, hit_t);

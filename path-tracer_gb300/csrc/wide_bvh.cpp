@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/pt_precision.h"
+#include "pt_links.h"
 
 namespace {
 
@@ -93,9 +94,41 @@ struct Work {
 
 }  // namespace
 
-extern "C" int pt_build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, pt_wide_node* out, uint64_t capacity,
-                                 uint64_t* wide_count, uint32_t* wide_depth) {
+extern "C" int pt_build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, uint32_t max_leaf_triangles,
+                                 pt_wide_node* out, uint64_t capacity, uint64_t* wide_count, uint32_t* wide_depth) {
     if (!nodes || node_count == 0 || node_count > 0xffffffffull) return PT_ERR_INVALID_ARG;
+    // triangle range of every binary subtree (children follow their parent in
+    // the reference's layout, so one backward pass suffices); a subtree of at
+    // most max_leaf_triangles triangles in one contiguous range becomes a
+    // single leaf child
+    std::vector<uint32_t> sub_first, sub_count;
+    if (max_leaf_triangles > 0) {
+        sub_first.assign(node_count, 0);
+        sub_count.assign(node_count, 0xffffffffu);  // not mergeable
+        for (uint64_t k = node_count; k-- > 0;) {
+            const pt_bvh_node& n = nodes[k];
+            if (n.tri_count != 0) {
+                sub_first[k] = n.left_first;
+                sub_count[k] = n.tri_count;
+                continue;
+            }
+            const uint64_t l = n.left_first, r = l + 1;
+            if (l <= k || r >= node_count) continue;
+            if (sub_count[l] == 0xffffffffu || sub_count[r] == 0xffffffffu) continue;
+            if (sub_first[l] + sub_count[l] == sub_first[r]) {
+                sub_first[k] = sub_first[l];
+            } else if (sub_first[r] + sub_count[r] == sub_first[l]) {
+                sub_first[k] = sub_first[r];
+            } else {
+                continue;
+            }
+            const uint64_t total = (uint64_t)sub_count[l] + sub_count[r];
+            sub_count[k] = total > 0xffffu ? 0xffffffffu : (uint32_t)total;
+        }
+    }
+    const auto as_leaf = [&](uint32_t b) {
+        return nodes[b].tri_count != 0 || (max_leaf_triangles > 0 && sub_count[b] <= max_leaf_triangles);
+    };
     std::vector<pt_wide_node> wide(1);
     std::memset(wide.data(), 0, sizeof(pt_wide_node));
     std::vector<Work> stack{{0u, 0u, 1u}};
@@ -123,7 +156,7 @@ extern "C" int pt_build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, 
             int best = -1;
             double best_area = -1.0;
             for (int i = 0; i < n; ++i) {
-                if (nodes[kids[i]].tri_count != 0) continue;
+                if (as_leaf(kids[i])) continue;
                 const double a = half_area(nodes[kids[i]]);
                 if (a > best_area) {
                     best_area = a;
@@ -166,6 +199,9 @@ extern "C" int pt_build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, 
             if (c.tri_count != 0) {
                 node.child[i] = c.left_first;
                 node.tri_count[i] = (uint16_t)c.tri_count;
+            } else if (as_leaf(kids[i])) {
+                node.child[i] = sub_first[kids[i]];
+                node.tri_count[i] = (uint16_t)sub_count[kids[i]];
             } else {
                 node.child[i] = next++;
                 node.tri_count[i] = 0;
@@ -235,4 +271,22 @@ extern "C" void pt_half_attributes(const pt_triangle_attribute* in, uint64_t cou
         }
         h.material_index = a.material_index;
     }
+}
+
+bool ptw::build_bvh_links(const pt_bvh_node* nodes, uint64_t node_count, uint64_t tri_count, uint32_t* parent,
+                          uint32_t* leaf_of) {
+    for (uint64_t i = 0; i < node_count; ++i) parent[i] = 0xffffffffu;
+    for (uint64_t t = 0; t < tri_count; ++t) leaf_of[t] = 0xffffffffu;
+    for (uint64_t i = 0; i < node_count; ++i) {
+        const pt_bvh_node& n = nodes[i];
+        if (n.tri_count == 0) {
+            if ((uint64_t)n.left_first + 1 >= node_count) return false;
+            parent[n.left_first] = (uint32_t)i;
+            parent[n.left_first + 1] = (uint32_t)i;
+        } else {
+            if ((uint64_t)n.left_first + n.tri_count > tri_count) return false;
+            for (uint32_t k = 0; k < n.tri_count; ++k) leaf_of[n.left_first + k] = (uint32_t)i;
+        }
+    }
+    return true;
 }

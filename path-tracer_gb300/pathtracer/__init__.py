@@ -55,6 +55,14 @@ class World:
         cls._check_static(lib, lib.ptw_scene_cornell_box(C.byref(h)), "ptw_scene_cornell_box")
         return cls(h.value)
 
+    @classmethod
+    def cornell_box_textured(cls, seed: int = 1) -> "World":
+        """The Cornell room as eight meshes, four with procedural 1024^2 textures (precision workload)."""
+        lib = load()
+        h = C.c_void_p()
+        cls._check_static(lib, lib.ptw_scene_cornell_box_textured(seed, C.byref(h)), "ptw_scene_cornell_box_textured")
+        return cls(h.value)
+
     @staticmethod
     def procedural_defaults() -> abi.ProceduralParams:
         p = abi.ProceduralParams()
@@ -202,6 +210,38 @@ def alias_table(weights) -> np.ndarray:
     return np.frombuffer(bytes(out), dtype=dt)[:n].copy()
 
 
+WIDE_NODE_DTYPE = np.dtype([("origin", "<f4", 3), ("exponent", "u1", 3), ("child_count", "u1"),
+                            ("lo", "u1", (3, 8)), ("hi", "u1", (3, 8)), ("child", "<u4", 8),
+                            ("tri_count", "<u2", 8), ("source_node", "<u4"), ("pad", "<u4", 3)])
+
+
+def build_wide_bvh(nodes: np.ndarray, max_leaf_triangles: int = 0):
+    """8-wide quantised BVH of the precision form from binary nodes ((m, 8) uint32 as World.bvh_nodes())
+    -> (structured array of WIDE_NODE_DTYPE, depth); subtrees of at most max_leaf_triangles become leaves."""
+    lib = load()
+    b = np.ascontiguousarray(nodes, dtype=np.uint32).reshape(-1, 8)
+    bp = b.ctypes.data_as(C.POINTER(abi.BvhNode))
+    count, depth = C.c_uint64(), C.c_uint32()
+    rc = lib.pt_build_wide_bvh(bp, b.shape[0], max_leaf_triangles, None, 0, C.byref(count), C.byref(depth))
+    if rc:
+        raise PathTracerError(rc, "pt_build_wide_bvh rejected the tree")
+    out = np.zeros(count.value, dtype=WIDE_NODE_DTYPE)
+    rc = lib.pt_build_wide_bvh(bp, b.shape[0], max_leaf_triangles, out.ctypes.data, count.value, C.byref(count),
+                               C.byref(depth))
+    if rc:
+        raise PathTracerError(rc, "pt_build_wide_bvh failed")
+    return out, depth.value
+
+
+def half_attributes(attributes: np.ndarray) -> np.ndarray:
+    """FP16 attribute records (64 B each, as uint16 / uint32 fields) of FP32 TriangleAttribute records."""
+    a = np.ascontiguousarray(attributes)
+    n = a.size
+    out = np.zeros(n * 64, dtype=np.uint8)
+    load().pt_half_attributes(a.ctypes.data_as(C.POINTER(abi.TriangleAttribute)), n, out.ctypes.data)
+    return out.reshape(n, 64)
+
+
 def build_bvh(triangles: np.ndarray):
     """Binned SAH BVH of world.rs:1430-1591 over (n, 9) float32 triangles -> (nodes (m, 8) uint32, order)."""
     t = np.ascontiguousarray(triangles, dtype=np.float32).reshape(-1, 9)
@@ -275,6 +315,16 @@ class PathTracer:
     def set_kernel(self, kernel: int) -> None:
         self._check(self._lib.pt_set_kernel(self._h, kernel))
 
+    def set_precision(self, flags: int) -> None:
+        """PT_PRECISION_* bits (wide BVH, FP16/BF16 attributes, Kahan); resets the accumulation."""
+        self._check(self._lib.pt_set_precision(self._h, flags))
+
+    def precision(self) -> int:
+        return self._lib.pt_precision(self._h)
+
+    def precision_active(self) -> int:
+        return self._lib.pt_precision_active(self._h)
+
     def trace(self, sample_count: int) -> int:
         traced = C.c_uint32()
         self._check(self._lib.pt_trace(self._h, sample_count, C.byref(traced)))
@@ -333,17 +383,20 @@ class PathTracer:
     def launch_count(self) -> int:
         return self._lib.pt_launch_count(self._h)
 
-    def debug_intersect(self, origins, directions, t_max=None):
+    def debug_intersect(self, origins, directions, t_max=None, records: bool = True):
+        """Closest hits of opaque rays -> (hit, t, records or None).  Without records and with
+        PT_PRECISION_WIDE_BVH selected the rays traverse the 8-wide BVH."""
         o = np.ascontiguousarray(origins, dtype=np.float32).reshape(-1, 3)
         d = np.ascontiguousarray(directions, dtype=np.float32).reshape(-1, 3)
         n = o.shape[0]
         tm = np.full(n, np.finfo(np.float32).max, dtype=np.float32) if t_max is None else np.ascontiguousarray(t_max, np.float32)
         hit = np.empty(n, dtype=np.int32)
         ht = np.empty(n, dtype=np.float32)
-        recs = (abi.PathRecord * max(1, n))()
+        recs = (abi.PathRecord * max(1, n))() if records else None
         self._check(self._lib.pt_debug_intersect(self._h, n, o.ctypes.data, d.ctypes.data, tm.ctypes.data,
-                                                 hit.ctypes.data, ht.ctypes.data, C.addressof(recs)))
-        return hit, ht, records_to_numpy(recs, n)
+                                                 hit.ctypes.data, ht.ctypes.data,
+                                                 C.addressof(recs) if records else None))
+        return hit, ht, (records_to_numpy(recs, n) if records else None)
 
 
 RECORD_DTYPE = np.dtype([("visit_hash", "<u8"), ("hit", "<i4", (abi.PT_RECORD_MAX_BOUNCES,)),

@@ -37,6 +37,13 @@ PT_KERNEL_WAVEFRONT = 0
 PT_KERNEL_PLAIN = 1
 PT_TILE_IMAGE = 0
 PT_TILE_ACCUMULATION = 1
+PT_TILE_COMPENSATION = 2
+# include/pt_precision.h
+PT_PRECISION_FP32 = 0
+PT_PRECISION_WIDE_BVH = 1
+PT_PRECISION_HALF_ATTRIBUTES = 2
+PT_PRECISION_KAHAN = 4
+PT_PRECISION_COMPRESSED = 7
 PT_KERNEL_CLASS_COUNT = 6
 KERNEL_CLASSES = ["raygen", "extend", "shade", "shadow", "accumulate", "plain"]
 PT_RECORD_MAX_BOUNCES = 17
@@ -158,18 +165,33 @@ class DeviceWorld(C.Structure):
                 ("any_non_opaque", c_i32)]
 
 
+class WideNode(C.Structure):
+    """pt_wide_node: one 8-wide node of the precision form, 128 B."""
+    _fields_ = [("origin", c_f * 3), ("exponent", C.c_uint8 * 3), ("child_count", C.c_uint8),
+                ("lo", (C.c_uint8 * 8) * 3), ("hi", (C.c_uint8 * 8) * 3), ("child", c_u32 * 8),
+                ("tri_count", C.c_uint16 * 8), ("source_node", c_u32), ("pad", c_u32 * 3)]
+
+
+class HalfAttribute(C.Structure):
+    """pt_half_attribute: FP16 shading attributes, 64 B."""
+    _fields_ = [("n0", C.c_uint16 * 4), ("n1", C.c_uint16 * 4), ("n2", C.c_uint16 * 4), ("t0", C.c_uint16 * 4),
+                ("t1", C.c_uint16 * 4), ("t2", C.c_uint16 * 4), ("uv0", C.c_uint16 * 2), ("uv1", C.c_uint16 * 2),
+                ("uv2", C.c_uint16 * 2), ("material_index", c_u32)]
+
+
 PT_NOALLOC_MAX_PATHS = 262144
 PT_NOALLOC_SCRATCH_BYTES = 48 << 20
 
 STRUCT_SIZES = {
     TriangleGeometry: 36, TriangleAttribute: 112, BvhNode: 32, Material: 224, Camera: 64,
     SceneUniforms: 16, SceneAliasEntry: 16, SkyboxUniforms: 16, SkyboxAliasEntry: 12,
-    TraceParameters: 32, PathRecord: 144,
+    TraceParameters: 32, PathRecord: 144, WideNode: 128, HalfAttribute: 64,
 }
 
 P = C.POINTER
 _vp = C.c_void_p
-# name: (restype, argtypes) of every entry point declared in include/pt.h and include/pt_world.h
+# name: (restype, argtypes) of every entry point declared in include/pt.h, include/pt_precision.h
+# and include/pt_world.h
 SIGNATURES = {
     # pt.h
     "pt_create": (C.c_int, [C.c_int, P(WorldUpdates), c_u32, c_u32, P(_vp)]),
@@ -195,6 +217,12 @@ SIGNATURES = {
     "pt_debug_intersect": (C.c_int, [_vp, c_u64, _vp, _vp, _vp, _vp, _vp, _vp]),
     "pt_trace_noalloc": (C.c_int, [P(DeviceWorld), P(TraceParameters), c_u32, c_u32, c_u32, _vp, _vp, _vp,
                                    C.c_char_p, C.c_size_t]),
+    # pt_precision.h
+    "pt_build_wide_bvh": (C.c_int, [P(BvhNode), c_u64, c_u32, _vp, c_u64, P(c_u64), P(c_u32)]),
+    "pt_half_attributes": (None, [P(TriangleAttribute), c_u64, _vp]),
+    "pt_set_precision": (C.c_int, [_vp, c_u32]),
+    "pt_precision": (c_u32, [_vp]),
+    "pt_precision_active": (c_u32, [_vp]),
     # pt_world.h
     "ptw_create": (C.c_int, [P(_vp)]),
     "ptw_destroy": (None, [_vp]),
@@ -223,6 +251,7 @@ SIGNATURES = {
     "ptw_alias_table": (c_u64, [_vp, c_u64, _vp]),
     "ptw_build_bvh": (c_u64, [_vp, c_u64, _vp, _vp]),
     "ptw_scene_cornell_box": (C.c_int, [P(_vp)]),
+    "ptw_scene_cornell_box_textured": (C.c_int, [c_u64, P(_vp)]),
     "ptw_procedural_defaults": (None, [P(ProceduralParams)]),
     "ptw_scene_procedural": (C.c_int, [P(ProceduralParams), P(_vp)]),
 }
@@ -262,7 +291,7 @@ PT_JOB_DONE = 2
 
 class EngineConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("hbm_budget_bytes", c_u64), ("wave_paths", c_u32), ("tile_size", c_u32),
-                ("steps_per_refill", c_u32), ("use_graphs", c_u32)]
+                ("steps_per_refill", c_u32), ("use_graphs", c_u32), ("precision", c_u32)]
 
 
 class JobDesc(C.Structure):

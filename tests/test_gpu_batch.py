@@ -166,3 +166,26 @@ def test_autotune_picks_a_candidate(scenes):
     eng.wait_idle(timeout_ms=300000)
     assert eng.status(j)[0] == abi.PT_JOB_DONE
     eng.close()
+
+
+def test_compressed_engine_equals_alone(scenes):
+    """The precision form in the engine (8-wide BVH, FP16 attributes, BF16 sky, Kahan) gives each job
+    the bits pt_trace gives it alone in the same form."""
+    eng = Engine(wave_paths=1 << 15, tile_size=16, precision=abi.PT_PRECISION_COMPRESSED)
+    ids = {name: eng.add_scene(scenes.full[name]) for name in scenes.full}
+    cams = [scenes.camera(n, w, h, yaw) for n, w, h, _, _, yaw in JOBS[:3]]
+    jobs = [eng.submit(ids[n], cam, w, h, spp, b) for (n, w, h, spp, b, _), cam in zip(JOBS[:3], cams)]
+    eng.wait_idle(timeout_ms=300000)
+    for (n, w, h, spp, b, _), cam, jid in zip(JOBS[:3], cams, jobs):
+        tr = pt.PathTracer(scenes.updates_with_camera(n, cam), (w, h))
+        tr.set_precision(abi.PT_PRECISION_COMPRESSED)
+        tr.set_max_bounces(b)
+        tr.set_tile((w, h), (0, 0), (w, h))
+        done = 0
+        while done < spp:
+            done += tr.trace(spp - done)
+        for which in (abi.PT_TILE_ACCUMULATION, abi.PT_TILE_IMAGE, abi.PT_TILE_COMPENSATION):
+            np.testing.assert_array_equal(eng.read(jid, w, h, which).view(np.uint32),
+                                          tr.read_tile(which).view(np.uint32))
+        tr.close()
+    eng.close()

@@ -184,3 +184,21 @@ def test_counted_totals_match_records(cornell):
     for k in abi.COUNT_FIELDS:
         assert totals[k] == int(recs[k].sum()), k
     tr.close()
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_textured_cornell_tile_bit_exact(kernel):
+    """The precision workload's scene in FP32: procedural 1024^2 sRGB textures on four of eight meshes."""
+    w = pt.World.cornell_box_textured(1)
+    w.set_aspect_ratio(1.0)
+    u = w.take_updates()
+    ow = oracle.world_from_updates(u)
+    tr = pt.PathTracer(u, (64, 64))
+    tr.set_kernel(kernel)
+    tr.set_max_bounces(8)
+    tr.set_tile((256, 256), (96, 128), (64, 64))
+    gpu = tr.trace_recorded(4)
+    px = pixels_of((96, 128), (64, 64), (256, 256))
+    _, ref = oracle.trace_paths(ow, (256, 256), 8, px, 1, 4, records=True)
+    assert_records_equal(gpu, ref)
+    tr.close()

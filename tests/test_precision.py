@@ -1,0 +1,158 @@
+"""Precision form, host side (include/pt_precision.h): the 8-wide BVH collapsed
+from the reference's binary tree must contain every binary child box after
+decoding (so no ray the binary traversal follows is culled), reach every
+binary leaf exactly once, and quantise tightly; the FP16 attribute records
+must round to nearest even like numpy's float16 conversion."""
+import numpy as np
+import pytest
+
+import pathtracer as pt
+
+
+def decode(origin, q, ebyte):
+    """origin + q * 2^(e - 127) in float32: the product is exact, the sum rounds once (as in the kernel)."""
+    s = np.ldexp(np.float32(1.0), ebyte.astype(np.int32) - 127).astype(np.float32)
+    return (np.float32(origin) + q.astype(np.float32) * s).astype(np.float32)
+
+
+def subtree_ranges(nodes: np.ndarray) -> dict:
+    """(first triangle, count) of every binary subtree -> its node (children follow their parent)."""
+    first = np.zeros(nodes.shape[0], np.int64)
+    count = np.zeros(nodes.shape[0], np.int64)
+    for k in range(nodes.shape[0] - 1, -1, -1):
+        lf, tc = int(nodes[k, 3]), int(nodes[k, 7])
+        if tc:
+            first[k], count[k] = lf, tc
+        else:
+            first[k], count[k] = min(first[lf], first[lf + 1]), count[lf] + count[lf + 1]
+    out = {}
+    for k in range(nodes.shape[0]):  # the topmost node of a range wins
+        out.setdefault((int(first[k]), int(count[k])), k)
+    return out
+
+
+def check_wide(nodes: np.ndarray, tri_count: int, merge: int = 0):
+    wide, depth = pt.build_wide_bvh(nodes, merge)
+    assert 1 <= depth <= 64
+    assert 0 < wide.size <= nodes.shape[0]
+    bmin = nodes[:, 0:3].view(np.float32)
+    bmax = nodes[:, 4:7].view(np.float32)
+    count = nodes[:, 7]
+    node_of_range = subtree_ranges(nodes)
+    seen_children = np.zeros(wide.size, dtype=np.int64)
+    ranges = []
+    for wi, w in enumerate(wide):
+        n = int(w["child_count"])
+        assert 1 <= n <= 8
+        for i in range(n):
+            c, tc = int(w["child"][i]), int(w["tri_count"][i])
+            if tc:
+                b = node_of_range[(c, tc)]
+                assert count[b] > 0 or tc <= merge  # a binary leaf, or a merged small subtree
+                ranges.append((c, tc))
+            else:
+                assert wi < c < wide.size  # children after parents: acyclic
+                seen_children[c] += 1
+                b = int(wide[c]["source_node"])
+                assert count[b] == 0
+            for a in range(3):
+                lo = decode(w["origin"][a], np.array([w["lo"][a][i]]), np.array([w["exponent"][a]]))[0]
+                hi = decode(w["origin"][a], np.array([w["hi"][a][i]]), np.array([w["exponent"][a]]))[0]
+                assert lo <= bmin[b, a] and hi >= bmax[b, a], (wi, i, a)
+                # tight: one quantum less would no longer contain the box
+                ql, qh = int(w["lo"][a][i]), int(w["hi"][a][i])
+                if ql < 255:
+                    assert decode(w["origin"][a], np.array([ql + 1]), np.array([w["exponent"][a]]))[0] > bmin[b, a]
+                if qh > 0:
+                    assert decode(w["origin"][a], np.array([qh - 1]), np.array([w["exponent"][a]]))[0] < bmax[b, a]
+    assert seen_children[0] == 0 and np.all(seen_children[1:] == 1)  # a tree
+    ranges.sort()
+    pos = 0
+    for first, n in ranges:  # the leaves tile [0, triangles) exactly once
+        assert first == pos
+        pos += n
+    assert pos == tri_count
+    return wide
+
+
+def test_wide_bvh_cornell():
+    w = pt.World.cornell_box()
+    wide = check_wide(w.bvh_nodes(), w.triangle_count())
+    assert wide.size >= 1
+
+
+def test_wide_bvh_procedural():
+    w = pt.World.procedural(grid_x=48, grid_z=24, boxes=40, spheres=4, sphere_subdivision=2, emissive_triangles=8,
+                            skybox_width=16, skybox_height=8)
+    nodes = w.bvh_nodes()
+    wide = check_wide(nodes, w.triangle_count())
+    # the collapse opens up to 8 children: far fewer wide nodes than binary interior nodes
+    assert wide["child_count"][0] == 8
+    assert wide.size < 0.5 * np.count_nonzero(nodes[:, 7] == 0)
+
+
+def test_wide_bvh_random_soups():
+    rng = np.random.default_rng(3)
+    for n in (1, 2, 3, 17, 500):
+        c = rng.uniform(-100, 100, (n, 1, 3))
+        tris = (c + rng.normal(0, 1.5, (n, 3, 3))).astype(np.float32).reshape(n, 9)
+        nodes, _ = pt.build_bvh(tris)
+        check_wide(nodes, n)
+
+
+@pytest.mark.parametrize("merge", [2, 4, 8])
+def test_wide_bvh_merged_leaves(merge):
+    w = pt.World.procedural(grid_x=48, grid_z=24, boxes=40, spheres=4, sphere_subdivision=2, emissive_triangles=8,
+                            skybox_width=16, skybox_height=8)
+    nodes = w.bvh_nodes()
+    plain = check_wide(nodes, w.triangle_count())
+    merged = check_wide(nodes, w.triangle_count(), merge)
+    # binary leaves already hold up to 2 triangles, so merging pays from 4 on
+    assert merged.size < plain.size if merge >= 4 else merged.size == plain.size
+    assert merged["tri_count"].max() <= max(merge, int(nodes[:, 7].max()))
+
+
+def test_wide_bvh_rejects_bad_trees():
+    nodes = pt.World.cornell_box().bvh_nodes().copy()
+    bad = nodes.copy()
+    bad[0, 3] = nodes.shape[0] + 5  # root children out of range
+    with pytest.raises(pt.PathTracerError):
+        pt.build_wide_bvh(bad)
+    cyc = nodes.copy()
+    interior = np.nonzero(cyc[1:, 7] == 0)[0]
+    if interior.size:
+        i = int(interior[0]) + 1
+        cyc[i, 3] = 1  # points back up towards the root: not a tree
+        with pytest.raises(pt.PathTracerError):
+            pt.build_wide_bvh(cyc)
+
+
+def test_half_attributes_round_to_nearest_even():
+    rng = np.random.default_rng(5)
+    n = 4096
+    vals = rng.normal(0, 1, (n, 27)).astype(np.float32)
+    special = np.array([65504.0, 65519.996, 65520.0, 1e6, 2.0 ** -24, 2.0 ** -25, 1.5 * 2.0 ** -25, 2.0 ** -14,
+                        2.0 ** -14 * (1 - 2.0 ** -11), -0.0, 1.0 + 2.0 ** -11, 1.0 + 3 * 2.0 ** -11, 1e-8,
+                        -65520.0, 3.0e-5], dtype=np.float32)
+    vals.reshape(-1)[: special.size] = special
+    vals[:, 18:27:4] = np.where(rng.random((n, 3)) < 0.5, -1.0, 1.0)  # tangent handedness (w)
+    mat = rng.integers(0, 1000, n, dtype=np.uint32)
+    buf = np.zeros((n, 28), dtype=np.uint32)
+    buf[:, 0] = mat
+    buf[:, 1:] = vals.view(np.uint32)
+    attrs = buf.copy()
+    half = pt.half_attributes(attrs.view(np.dtype((np.void, 112))).reshape(n))
+    h16 = half.view(np.uint16).reshape(n, 32)
+    f = vals
+
+    def exp16(a):
+        with np.errstate(over="ignore"):
+            return np.asarray(a, dtype=np.float32).astype(np.float16).view(np.uint16)
+    # normals n0..n2: xyz then 0
+    for k in range(3):
+        np.testing.assert_array_equal(h16[:, 4 * k:4 * k + 3], exp16(f[:, 3 * k:3 * k + 3]))
+        assert np.all(h16[:, 4 * k + 3] == 0)
+    # uvs at float offsets 9..14 -> halves 24..29; tangents at 15..26 -> halves 12..23
+    np.testing.assert_array_equal(h16[:, 24:30], exp16(f[:, 9:15]))
+    np.testing.assert_array_equal(h16[:, 12:24], exp16(f[:, 15:27]))
+    np.testing.assert_array_equal(half.view(np.uint32).reshape(n, 16)[:, 15], mat)
