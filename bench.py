@@ -57,6 +57,8 @@ def parse_args():
     p.add_argument("--spp", type=int, default=SPP, help="samples per pixel of one step")
     p.add_argument("--profile-run", action="store_true",
                    help="only the timed steps (no counting pass, e2e or CPU baseline): for ncu captures")
+    p.add_argument("--no-latency", action="store_true",
+                   help="skip the request-latency measurement (batched engine vs the plain path)")
     p.add_argument("--image", type=int, nargs=2, metavar=("W", "H"), default=None,
                    help="image size (default 1920 1080); smaller sizes are for ncu captures, not bench lines")
     args = p.parse_args()
@@ -159,6 +161,61 @@ class ClockSampler:
         os.unlink(self.file.name)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def latency_report(updates, precision: int, rate: float = 20.0, seconds: float = 3.0) -> dict:
+    """p50/p99/p999 request latency (arrival -> result ready) of 512x512, 16-spp, max_bounces-8
+    requests on this scene arriving as a seeded Poisson stream: through the batched engine
+    (continuous batching, the requested precision form) and through the plain path (one
+    request at a time, one pt_trace call of 16 samples, the plain kernel, the host waiting; its
+    queueing is replayed from the measured service times)."""
+    import pathtracer as pt
+    from pathtracer import abi
+    from pathtracer.engine import Engine
+    from pathtracer.serving import percentiles, request_stream
+    size, spp, depth = 512, 16, 8
+    reqs = request_stream(rate, seconds, ["bench"], seed=3, progressive_fraction=0.0, fixed=(size, size, spp, depth))
+    cam = abi.Camera.from_buffer_copy(updates.camera.contents)
+    eng = Engine(precision=precision)
+    sid = eng.add_scene(updates)
+    warm = eng.submit(sid, cam, size, size, spp, depth)  # graph capture, layouts
+    eng.wait_idle(timeout_ms=0)
+    eng.release(warm)
+    lat, arrival_of, i = [], {}, 0
+    t0 = time.perf_counter()
+    while i < len(reqs) or arrival_of:
+        now = time.perf_counter() - t0
+        while i < len(reqs) and reqs[i].arrival <= now:
+            arrival_of[eng.submit(sid, cam, size, size, spp, depth)] = reqs[i].arrival
+            i += 1
+        for jid in eng.poll(timeout_ms=1):
+            lat.append((time.perf_counter() - t0 - arrival_of.pop(jid)) * 1e3)
+            eng.release(jid)
+    eng.close()
+    tr = pt.PathTracer(updates, (size, size))
+    tr.set_kernel(abi.PT_KERNEL_PLAIN)
+    tr.set_max_bounces(depth)
+    tr.set_tile((size, size), (0, 0), (size, size))
+    tr.trace(spp)
+    tr.synchronize()
+    free_at, plat = 0.0, []
+    for r in reqs:
+        u = abi.WorldUpdates()
+        u.camera = C.pointer(cam)
+        u.reset_accumulation = 1
+        s0 = time.perf_counter()
+        tr.apply_updates(u)
+        tr.set_tile((size, size), (0, 0), (size, size))
+        tr.trace(spp)
+        tr.synchronize()
+        service = time.perf_counter() - s0
+        start = max(r.arrival, free_at)
+        free_at = start + service
+        plat.append((free_at - r.arrival) * 1e3)
+    tr.close()
+    return {"workload": f"{size}x{size}, {spp} spp, max_bounces {depth}, Poisson {rate:g} req/s for {seconds:g} s "
+                        f"on this scene (seed 3)",
+            "engine_ms": percentiles(lat), "plain_ms": percentiles(plat)}
 
 
 def pinned_updates(updates):
@@ -368,6 +425,10 @@ def run_ours(args):
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
         e2e_value = rays_per_step * e2e_steps * world_size / float(t.item()) / 1e6
 
+    latency = None
+    if rank == 0 and world_size == 1 and not args.no_latency:
+        latency = latency_report(updates, PRECISIONS[args.precision])
+
     cpu = None
     if rank == 0 and world_size == 1 and not args.no_cpu_baseline:
         v, threads, desc, _ = oracle_sample(updates, args.cpu_seconds)
@@ -384,7 +445,7 @@ def run_ours(args):
             "roofline": roofline, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": WIDTH * HEIGHT * 4},
-            "gpu_launches": launches, "clocks": clocks.summary(),
+            "gpu_launches": launches, "clocks": clocks.summary(), "latency": latency,
             "kernel_ms": {k: v for k, v in times.milliseconds.items() if times.launches[k]},
         }
         print(json.dumps(line), flush=True)

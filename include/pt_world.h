@@ -57,6 +57,14 @@ int ptw_add_mesh(ptw_world* world, const ptw_mesh* mesh);
 /* sRGB / linear RGBA8 atlas layers (PT_ATLAS_SIZE^2 * 4 bytes each); returns the layer index */
 int ptw_add_atlas_layer(ptw_world* world, int srgb, const uint8_t* rgba8, int32_t* layer);
 
+/* glTF 2.0 import (.glb, or .gltf with external or base64 buffers): adds the
+ * default scene's triangle primitives and their materials, walking the node
+ * tree as the reference's Scene::new does (world.rs:1078-1337; materials
+ * world.rs:1992-2155).  Call before ptw_build.  Textured materials are
+ * refused (the import decodes no images).  On failure `error` (if given)
+ * receives the reason. */
+int ptw_load_gltf(ptw_world* world, const char* path, char* error, size_t error_size);
+
 /* Builds the BVH over all added meshes, reorders triangles to BVH order and
  * sets the auto camera (the tail of Scene::new, world.rs:1339-1357).  Errors
  * with PT_ERR_INVALID_ARG if the scene has no triangles. */

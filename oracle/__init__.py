@@ -23,7 +23,7 @@ from pathtracer import RECORD_DTYPE, records_to_numpy  # noqa: E402
 
 LIB_PATH = ROOT / "oracle" / "_build" / "liboracle.so"
 
-FMATH = {"sin": 0, "cos": 1, "acos": 2, "atan2": 3, "pow": 4, "log2": 5, "exp2": 6}
+FMATH = {"sin": 0, "cos": 1, "acos": 2, "atan2": 3, "pow": 4, "log2": 5, "exp2": 6, "sincos_sin": 7, "sincos_cos": 8}
 
 
 class OracleWorld(C.Structure):

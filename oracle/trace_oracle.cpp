@@ -992,6 +992,18 @@ void oracle_fmath(int which, const float* x, const float* y, float* out, uint64_
             case 4: out[i] = ptm::powf_(x[i], y[i]); break;
             case 5: out[i] = ptm::log2f_(x[i]); break;
             case 6: out[i] = ptm::exp2f_(x[i]); break;
+            case 7: {  // sin through the shared-reduction sincos of the kernels
+                float sn, cs;
+                ptm::sincosf_(x[i], &sn, &cs);
+                out[i] = sn;
+                break;
+            }
+            case 8: {
+                float sn, cs;
+                ptm::sincosf_(x[i], &sn, &cs);
+                out[i] = cs;
+                break;
+            }
             default: out[i] = 0.0f; break;
         }
     }

@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : 1
     __shared__ FilerSlots<kExtendThreads> filer_slots;
     ResultFiler filer = filer_slots.of_warp(lane_id());
     lane_refill_loop(
-        &b.q.cnt[3], count, steps_per_refill, kRefillBelow,
+        &b.q.cnt[3], count, kWide ? (uint32_t)kWideStepsPerRefill : steps_per_refill, kRefillBelow,
         [&](uint32_t i) {
             slot = i;
             const float4 o4 = st.o[i], d4 = st.d[i];
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : 1
     uint32_t path = 0;
     float4 contribution = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     lane_refill_loop(
-        &b.q.cnt[4], count, steps_per_refill, kRefillBelow,
+        &b.q.cnt[4], count, kWide ? (uint32_t)kWideStepsPerRefill : steps_per_refill, kRefillBelow,
         [&](uint32_t i) {
             const float4 o4 = b.q.so[i], d4 = b.q.sd[i];
             contribution = b.q.sc[i];

@@ -1,0 +1,705 @@
+// gltf.cpp - glTF 2.0 scene import into the world builder (the reference's
+// Scene::new glTF path, world.rs:1078-1337, materials world.rs:1992-2155).
+//
+// Reads .glb (binary container) and .gltf (JSON with external or base64
+// buffers): the default scene's node tree (matrix or TRS transforms, walked
+// with the same LIFO stack as the reference so triangles arrive in the same
+// order), triangle primitives (POSITION, NORMAL, TANGENT, TEXCOORD_0,
+// indices of any integer width, normalised integer texture coordinates) and
+// materials (pbrMetallicRoughness, emissive factor and strength, IOR,
+// KHR_materials_specular, alpha mode and cutoff, OpenPBR_* extras).  Per
+// primitive the positions are transformed by the node matrix, normals by its
+// inverse transpose and tangents by the matrix; ptw_add_mesh then applies
+// the reference's normalisation and tangent rules.  Textured materials are
+// refused: the reference decodes PNG/JPEG images into its atlases, which
+// this import does not do.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/pt_world.h"
+
+namespace {
+
+// ------------------------------------------------------------------ JSON
+struct Json {
+    enum Kind { Null, Bool, Number, String, Array, Object } kind = Null;
+    bool b = false;
+    double num = 0.0;
+    std::string str;
+    std::vector<Json> arr;
+    std::vector<std::pair<std::string, Json>> obj;
+
+    const Json* get(const char* key) const {
+        if (kind != Object) return nullptr;
+        for (const auto& kv : obj)
+            if (kv.first == key) return &kv.second;
+        return nullptr;
+    }
+    double number(const char* key, double dflt) const {
+        const Json* j = get(key);
+        return j && j->kind == Number ? j->num : dflt;
+    }
+    long integer(const char* key, long dflt) const {
+        const Json* j = get(key);
+        return j && j->kind == Number ? (long)j->num : dflt;
+    }
+    std::string string(const char* key, const char* dflt) const {
+        const Json* j = get(key);
+        return j && j->kind == String ? j->str : std::string(dflt);
+    }
+};
+
+struct JsonParser {
+    const char* p;
+    const char* end;
+    std::string error;
+    int depth = 0;
+
+    void ws() {
+        while (p < end && (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r')) ++p;
+    }
+    bool fail(const char* what) {
+        if (error.empty()) error = what;
+        return false;
+    }
+    bool parse(Json& out) {
+        ws();
+        if (p >= end) return fail("unexpected end of JSON");
+        if (++depth > 256) return fail("JSON nested too deeply");
+        bool ok;
+        switch (*p) {
+            case '{': ok = object(out); break;
+            case '[': ok = array(out); break;
+            case '"': out.kind = Json::String; ok = string(out.str); break;
+            case 't': ok = literal("true", out, Json::Bool, true); break;
+            case 'f': ok = literal("false", out, Json::Bool, false); break;
+            case 'n': ok = literal("null", out, Json::Null, false); break;
+            default: ok = number(out); break;
+        }
+        --depth;
+        return ok;
+    }
+    bool literal(const char* word, Json& out, Json::Kind kind, bool value) {
+        const size_t n = strlen(word);
+        if ((size_t)(end - p) < n || strncmp(p, word, n) != 0) return fail("bad JSON literal");
+        p += n;
+        out.kind = kind;
+        out.b = value;
+        return true;
+    }
+    bool number(Json& out) {
+        const char* s = p;
+        if (p < end && (*p == '-' || *p == '+')) ++p;
+        while (p < end && ((*p >= '0' && *p <= '9') || *p == '.' || *p == 'e' || *p == 'E' || *p == '-' || *p == '+'))
+            ++p;
+        if (p == s) return fail("bad JSON value");
+        out.kind = Json::Number;
+        out.num = std::strtod(std::string(s, p).c_str(), nullptr);
+        return true;
+    }
+    static void utf8(std::string& s, unsigned cp) {
+        if (cp < 0x80) {
+            s += (char)cp;
+        } else if (cp < 0x800) {
+            s += (char)(0xC0 | (cp >> 6));
+            s += (char)(0x80 | (cp & 0x3F));
+        } else if (cp < 0x10000) {
+            s += (char)(0xE0 | (cp >> 12));
+            s += (char)(0x80 | ((cp >> 6) & 0x3F));
+            s += (char)(0x80 | (cp & 0x3F));
+        } else {
+            s += (char)(0xF0 | (cp >> 18));
+            s += (char)(0x80 | ((cp >> 12) & 0x3F));
+            s += (char)(0x80 | ((cp >> 6) & 0x3F));
+            s += (char)(0x80 | (cp & 0x3F));
+        }
+    }
+    bool hex4(unsigned& v) {
+        if (end - p < 4) return fail("bad JSON escape");
+        v = 0;
+        for (int i = 0; i < 4; ++i) {
+            const char c = *p++;
+            v <<= 4;
+            if (c >= '0' && c <= '9') v |= (unsigned)(c - '0');
+            else if (c >= 'a' && c <= 'f') v |= (unsigned)(c - 'a' + 10);
+            else if (c >= 'A' && c <= 'F') v |= (unsigned)(c - 'A' + 10);
+            else return fail("bad JSON escape");
+        }
+        return true;
+    }
+    bool string(std::string& s) {
+        ++p;  // opening quote
+        while (p < end && *p != '"') {
+            if (*p == '\\') {
+                ++p;
+                if (p >= end) break;
+                const char c = *p++;
+                switch (c) {
+                    case 'n': s += '\n'; break;
+                    case 't': s += '\t'; break;
+                    case 'r': s += '\r'; break;
+                    case 'b': s += '\b'; break;
+                    case 'f': s += '\f'; break;
+                    case 'u': {
+                        unsigned cp;
+                        if (!hex4(cp)) return false;
+                        if (cp >= 0xD800 && cp < 0xDC00 && end - p >= 6 && p[0] == '\\' && p[1] == 'u') {
+                            p += 2;
+                            unsigned lo;
+                            if (!hex4(lo)) return false;
+                            cp = 0x10000 + ((cp - 0xD800) << 10) + (lo - 0xDC00);
+                        }
+                        utf8(s, cp);
+                        break;
+                    }
+                    default: s += c; break;
+                }
+            } else {
+                s += *p++;
+            }
+        }
+        if (p >= end) return fail("unterminated JSON string");
+        ++p;
+        return true;
+    }
+    bool array(Json& out) {
+        out.kind = Json::Array;
+        ++p;
+        ws();
+        if (p < end && *p == ']') {
+            ++p;
+            return true;
+        }
+        for (;;) {
+            out.arr.emplace_back();
+            if (!parse(out.arr.back())) return false;
+            ws();
+            if (p < end && *p == ',') {
+                ++p;
+                continue;
+            }
+            if (p < end && *p == ']') {
+                ++p;
+                return true;
+            }
+            return fail("expected , or ] in JSON array");
+        }
+    }
+    bool object(Json& out) {
+        out.kind = Json::Object;
+        ++p;
+        ws();
+        if (p < end && *p == '}') {
+            ++p;
+            return true;
+        }
+        for (;;) {
+            ws();
+            if (p >= end || *p != '"') return fail("expected a key in JSON object");
+            std::string key;
+            if (!string(key)) return false;
+            ws();
+            if (p >= end || *p != ':') return fail("expected : in JSON object");
+            ++p;
+            out.obj.emplace_back(std::move(key), Json());
+            if (!parse(out.obj.back().second)) return false;
+            ws();
+            if (p < end && *p == ',') {
+                ++p;
+                continue;
+            }
+            if (p < end && *p == '}') {
+                ++p;
+                return true;
+            }
+            return fail("expected , or } in JSON object");
+        }
+    }
+};
+
+// ------------------------------------------------------------------ math
+struct M4 {
+    float m[16];  // column-major: column c at m[4c .. 4c+3]
+};
+M4 identity() {
+    M4 r{};
+    r.m[0] = r.m[5] = r.m[10] = r.m[15] = 1.0f;
+    return r;
+}
+// a * b, each result column = a.x * b.c.x + a.y * b.c.y + a.z * b.c.z + a.w * b.c.w
+M4 mul(const M4& a, const M4& b) {
+    M4 r;
+    for (int c = 0; c < 4; ++c)
+        for (int row = 0; row < 4; ++row)
+            r.m[4 * c + row] = ((a.m[row] * b.m[4 * c] + a.m[4 + row] * b.m[4 * c + 1]) + a.m[8 + row] * b.m[4 * c + 2]) +
+                               a.m[12 + row] * b.m[4 * c + 3];
+    return r;
+}
+M4 from_trs(const float t[3], const float q[4], const float s[3]) {
+    const float x = q[0], y = q[1], z = q[2], w = q[3];
+    const float x2 = x + x, y2 = y + y, z2 = z + z;
+    const float xx = x * x2, xy = x * y2, xz = x * z2, yy = y * y2, yz = y * z2, zz = z * z2;
+    const float wx = w * x2, wy = w * y2, wz = w * z2;
+    M4 r{};
+    // rotation columns scaled by s, translation in the last column
+    const float c0[3] = {1.0f - (yy + zz), xy + wz, xz - wy};
+    const float c1[3] = {xy - wz, 1.0f - (xx + zz), yz + wx};
+    const float c2[3] = {xz + wy, yz - wx, 1.0f - (xx + yy)};
+    for (int i = 0; i < 3; ++i) {
+        r.m[i] = c0[i] * s[0];
+        r.m[4 + i] = c1[i] * s[1];
+        r.m[8 + i] = c2[i] * s[2];
+        r.m[12 + i] = t[i];
+    }
+    r.m[15] = 1.0f;
+    return r;
+}
+// inverse transpose of the upper 3x3 (normals), in double
+void normal_matrix(const M4& a, double n[9]) {
+    const double m00 = a.m[0], m10 = a.m[1], m20 = a.m[2];
+    const double m01 = a.m[4], m11 = a.m[5], m21 = a.m[6];
+    const double m02 = a.m[8], m12 = a.m[9], m22 = a.m[10];
+    const double c00 = m11 * m22 - m12 * m21, c01 = m12 * m20 - m10 * m22, c02 = m10 * m21 - m11 * m20;
+    const double det = m00 * c00 + m01 * c01 + m02 * c02;
+    const double id = det != 0.0 ? 1.0 / det : 0.0;
+    // inverse transpose = cofactor matrix / det (row-major here: n[3*row + col])
+    n[0] = c00 * id;
+    n[1] = c01 * id;
+    n[2] = c02 * id;
+    n[3] = (m02 * m21 - m01 * m22) * id;
+    n[4] = (m00 * m22 - m02 * m20) * id;
+    n[5] = (m01 * m20 - m00 * m21) * id;
+    n[6] = (m01 * m12 - m02 * m11) * id;
+    n[7] = (m02 * m10 - m00 * m12) * id;
+    n[8] = (m00 * m11 - m01 * m10) * id;
+}
+
+// ------------------------------------------------------------------ glTF
+struct Loader {
+    ptw_world* world;
+    std::string dir;
+    Json doc;
+    std::vector<std::vector<uint8_t>> buffers;
+    std::map<long, uint32_t> material_cache;  // glTF material index -> world material
+    std::string error;
+
+    bool fail(const std::string& msg) {
+        if (error.empty()) error = msg;
+        return false;
+    }
+
+    static bool read_file(const std::string& path, std::vector<uint8_t>& out) {
+        std::ifstream f(path, std::ios::binary);
+        if (!f) return false;
+        f.seekg(0, std::ios::end);
+        const std::streamoff n = f.tellg();
+        if (n < 0) return false;
+        f.seekg(0);
+        out.resize((size_t)n);
+        if (n) f.read(reinterpret_cast<char*>(out.data()), n);
+        return (bool)f;
+    }
+
+    static bool base64(const std::string& s, std::vector<uint8_t>& out) {
+        auto val = [](char c) -> int {
+            if (c >= 'A' && c <= 'Z') return c - 'A';
+            if (c >= 'a' && c <= 'z') return c - 'a' + 26;
+            if (c >= '0' && c <= '9') return c - '0' + 52;
+            if (c == '+') return 62;
+            if (c == '/') return 63;
+            return -1;
+        };
+        uint32_t acc = 0;
+        int bits = 0;
+        for (char c : s) {
+            if (c == '=') break;
+            const int v = val(c);
+            if (v < 0) return false;
+            acc = (acc << 6) | (uint32_t)v;
+            bits += 6;
+            if (bits >= 8) {
+                bits -= 8;
+                out.push_back((uint8_t)((acc >> bits) & 0xFF));
+            }
+        }
+        return true;
+    }
+
+    bool open(const std::string& path) {
+        std::vector<uint8_t> file;
+        if (!read_file(path, file)) return fail("cannot read " + path);
+        const size_t slash = path.find_last_of('/');
+        dir = slash == std::string::npos ? "" : path.substr(0, slash + 1);
+        std::vector<uint8_t> bin;
+        const char* json_begin;
+        size_t json_size;
+        if (file.size() >= 12 && memcmp(file.data(), "glTF", 4) == 0) {
+            uint32_t version, length;
+            memcpy(&version, file.data() + 4, 4);
+            memcpy(&length, file.data() + 8, 4);
+            if (version != 2) return fail("only glTF 2.0 binaries are supported");
+            if (length > file.size()) return fail("truncated .glb");
+            size_t off = 12;
+            json_begin = nullptr;
+            json_size = 0;
+            while (off + 8 <= length) {
+                uint32_t clen, ctype;
+                memcpy(&clen, file.data() + off, 4);
+                memcpy(&ctype, file.data() + off + 4, 4);
+                off += 8;
+                if (off + clen > length) return fail("truncated .glb chunk");
+                if (ctype == 0x4E4F534Au && !json_begin) {  // "JSON"
+                    json_begin = reinterpret_cast<const char*>(file.data() + off);
+                    json_size = clen;
+                } else if (ctype == 0x004E4942u && bin.empty()) {  // "BIN\0"
+                    bin.assign(file.data() + off, file.data() + off + clen);
+                }
+                off += (clen + 3u) & ~3u;
+            }
+            if (!json_begin) return fail(".glb without a JSON chunk");
+        } else {
+            json_begin = reinterpret_cast<const char*>(file.data());
+            json_size = file.size();
+        }
+        JsonParser jp{json_begin, json_begin + json_size, {}};
+        if (!jp.parse(doc) || doc.kind != Json::Object) return fail("bad glTF JSON: " + jp.error);
+        const Json* asset = doc.get("asset");
+        if (!asset || asset->string("version", "").rfind("2", 0) != 0) return fail("not a glTF 2.0 asset");
+        if (const Json* req = doc.get("extensionsRequired"))
+            for (const Json& e : req->arr)
+                if (e.str != "KHR_materials_emissive_strength" && e.str != "KHR_materials_ior" &&
+                    e.str != "KHR_materials_specular")
+                    return fail("required glTF extension not supported: " + e.str);
+        if (const Json* bufs = doc.get("buffers")) {
+            for (size_t i = 0; i < bufs->arr.size(); ++i) {
+                const Json& b = bufs->arr[i];
+                std::vector<uint8_t> data;
+                const Json* uri = b.get("uri");
+                if (!uri) {
+                    if (i != 0 || bin.empty()) return fail("buffer without uri and no .glb BIN chunk");
+                    data = bin;
+                } else if (uri->str.rfind("data:", 0) == 0) {
+                    const size_t comma = uri->str.find(',');
+                    if (comma == std::string::npos || uri->str.find(";base64") == std::string::npos ||
+                        !base64(uri->str.substr(comma + 1), data))
+                        return fail("unsupported data URI in buffer " + std::to_string(i));
+                } else if (!read_file(dir + uri->str, data)) {
+                    return fail("cannot read buffer " + uri->str);
+                }
+                const long need = b.integer("byteLength", 0);
+                if (need < 0 || (size_t)need > data.size()) return fail("buffer shorter than its byteLength");
+                buffers.push_back(std::move(data));
+            }
+        }
+        return true;
+    }
+
+    // accessor i as float components (count x ncomp), normalised integers mapped to [0, 1] / [-1, 1]
+    bool read_floats(long index, int want_comps, std::vector<float>& out, size_t* count) {
+        const Json* accs = doc.get("accessors");
+        if (!accs || index < 0 || (size_t)index >= accs->arr.size()) return fail("accessor out of range");
+        const Json& a = accs->arr[(size_t)index];
+        if (a.get("sparse")) return fail("sparse accessors are not supported");
+        const std::string type = a.string("type", "");
+        const int comps = type == "SCALAR" ? 1 : type == "VEC2" ? 2 : type == "VEC3" ? 3 : type == "VEC4" ? 4 : 0;
+        if (comps != want_comps) return fail("accessor has type " + type);
+        const long ctype = a.integer("componentType", 0);
+        const bool norm = a.get("normalized") && a.get("normalized")->b;
+        const size_t n = (size_t)a.integer("count", 0);
+        const int csize = ctype == 5126 || ctype == 5125 ? 4 : ctype == 5123 || ctype == 5122 ? 2 : 1;
+        out.assign(n * comps, 0.0f);
+        *count = n;
+        if (!a.get("bufferView")) return true;  // all zeros
+        const uint8_t* base;
+        size_t stride, avail;
+        if (!view(a.integer("bufferView", -1), a.integer("byteOffset", 0), (size_t)csize * comps, &base, &stride, &avail))
+            return false;
+        if (n && (n - 1) * stride + (size_t)csize * comps > avail) return fail("accessor runs past its buffer view");
+        for (size_t i = 0; i < n; ++i)
+            for (int c = 0; c < comps; ++c) {
+                const uint8_t* e = base + i * stride + (size_t)c * csize;
+                float v;
+                switch (ctype) {
+                    case 5126: memcpy(&v, e, 4); break;
+                    case 5121: v = norm ? (float)e[0] / 255.0f : (float)e[0]; break;
+                    case 5120: {
+                        const int8_t s = (int8_t)e[0];
+                        v = norm ? std::fmax((float)s / 127.0f, -1.0f) : (float)s;
+                        break;
+                    }
+                    case 5123: {
+                        uint16_t u;
+                        memcpy(&u, e, 2);
+                        v = norm ? (float)u / 65535.0f : (float)u;
+                        break;
+                    }
+                    case 5122: {
+                        int16_t s;
+                        memcpy(&s, e, 2);
+                        v = norm ? std::fmax((float)s / 32767.0f, -1.0f) : (float)s;
+                        break;
+                    }
+                    default: return fail("unsupported accessor component type");
+                }
+                out[i * comps + c] = v;
+            }
+        return true;
+    }
+
+    bool read_indices(long index, std::vector<uint32_t>& out) {
+        const Json* accs = doc.get("accessors");
+        if (!accs || index < 0 || (size_t)index >= accs->arr.size()) return fail("accessor out of range");
+        const Json& a = accs->arr[(size_t)index];
+        if (a.get("sparse")) return fail("sparse accessors are not supported");
+        const long ctype = a.integer("componentType", 0);
+        const int csize = ctype == 5125 ? 4 : ctype == 5123 ? 2 : ctype == 5121 ? 1 : 0;
+        if (!csize || a.string("type", "") != "SCALAR") return fail("index accessor must be unsigned SCALAR");
+        const size_t n = (size_t)a.integer("count", 0);
+        out.assign(n, 0u);
+        if (!a.get("bufferView")) return true;
+        const uint8_t* base;
+        size_t stride, avail;
+        if (!view(a.integer("bufferView", -1), a.integer("byteOffset", 0), (size_t)csize, &base, &stride, &avail))
+            return false;
+        if (n && (n - 1) * stride + (size_t)csize > avail) return fail("index accessor runs past its buffer view");
+        for (size_t i = 0; i < n; ++i) {
+            const uint8_t* e = base + i * stride;
+            if (csize == 4) memcpy(&out[i], e, 4);
+            else if (csize == 2) {
+                uint16_t u;
+                memcpy(&u, e, 2);
+                out[i] = u;
+            } else {
+                out[i] = e[0];
+            }
+        }
+        return true;
+    }
+
+    bool view(long index, long offset, size_t elem, const uint8_t** base, size_t* stride, size_t* avail) {
+        const Json* views = doc.get("bufferViews");
+        if (!views || index < 0 || (size_t)index >= views->arr.size()) return fail("buffer view out of range");
+        const Json& v = views->arr[(size_t)index];
+        const long b = v.integer("buffer", -1);
+        if (b < 0 || (size_t)b >= buffers.size()) return fail("buffer out of range");
+        const long voff = v.integer("byteOffset", 0), vlen = v.integer("byteLength", 0);
+        if (voff < 0 || vlen < 0 || offset < 0 || (size_t)(voff + vlen) > buffers[(size_t)b].size() || offset > vlen)
+            return fail("buffer view out of range");
+        *base = buffers[(size_t)b].data() + voff + offset;
+        const long st = v.integer("byteStride", 0);
+        *stride = st > 0 ? (size_t)st : elem;
+        *avail = (size_t)(vlen - offset);
+        return true;
+    }
+
+    bool has_texture(const Json* t) const { return t && t->kind == Json::Object; }
+
+    // GpuMaterial::new, world.rs:1992-2155
+    bool material(const Json* m, uint32_t* out) {
+        pt_material g;
+        ptw_default_material(&g);
+        const Json empty;
+        const Json& mat = m ? *m : empty;
+        const Json* pbr = mat.get("pbrMetallicRoughness");
+        const Json& p = pbr ? *pbr : empty;
+        if (has_texture(p.get("baseColorTexture")) || has_texture(p.get("metallicRoughnessTexture")) ||
+            has_texture(mat.get("normalTexture")) || has_texture(mat.get("emissiveTexture")))
+            return fail("textured glTF materials are not supported (no image decoding)");
+        const Json* bcf = p.get("baseColorFactor");
+        for (int i = 0; i < 4; ++i)
+            g.base_color[i] = bcf && bcf->arr.size() == 4 ? (float)bcf->arr[i].num : 1.0f;
+        g.base_weight = 1.0f;
+        g.base_metalness = (float)p.number("metallicFactor", 1.0);
+        g.base_diffuse_roughness = (float)p.number("roughnessFactor", 1.0);
+        g.emission_weight = 1.0f;
+        const Json* ef = mat.get("emissiveFactor");
+        for (int i = 0; i < 3; ++i)
+            g.emission_color_and_luminance[i] = ef && ef->arr.size() == 3 ? (float)ef->arr[i].num : 0.0f;
+        g.emission_color_and_luminance[3] = 1.0f;
+        g.specular_color_and_weight[0] = g.specular_color_and_weight[1] = g.specular_color_and_weight[2] = 1.0f;
+        g.specular_color_and_weight[3] = 1.0f;
+        g.specular_roughness = 0.3f;
+        g.specular_roughness_anisotropy = 0.0f;
+        g.specular_haze = 0.0f;
+        g.specular_haze_spread = 0.3f;
+        g.specular_ior = 1.5f;
+        g.specular_retroreflectivity = 0.0f;
+        g.normal_scale = 1.0f;
+        if (const Json* ext = mat.get("extensions")) {
+            if (const Json* es = ext->get("KHR_materials_emissive_strength"))
+                g.emission_color_and_luminance[3] = (float)es->number("emissiveStrength", 1.0);
+            if (const Json* ior = ext->get("KHR_materials_ior")) g.specular_ior = (float)ior->number("ior", 1.5);
+            if (const Json* sp = ext->get("KHR_materials_specular")) {
+                if (has_texture(sp->get("specularTexture")) || has_texture(sp->get("specularColorTexture")))
+                    return fail("textured glTF materials are not supported (no image decoding)");
+                g.specular_color_and_weight[3] = (float)sp->number("specularFactor", 1.0);
+                if (const Json* sc = sp->get("specularColorFactor"))
+                    for (int i = 0; i < 3 && i < (int)sc->arr.size(); ++i)
+                        g.specular_color_and_weight[i] = (float)sc->arr[i].num;
+            }
+        }
+        const std::string mode = mat.string("alphaMode", "OPAQUE");
+        g.alpha_mode = mode == "MASK" ? PT_ALPHA_MODE_MASK : mode == "BLEND" ? PT_ALPHA_MODE_BLEND : PT_ALPHA_MODE_OPAQUE;
+        g.alpha_cutoff = (float)mat.number("alphaCutoff", 0.5);
+        if (const Json* extras = mat.get("extras")) {
+            // OpenPBR values in [0, 1]; out-of-range values are ignored as in the reference
+            const auto apply = [&](const char* key, float* target) {
+                const Json* v = extras->get(key);
+                if (v && v->kind == Json::Number) {
+                    const float f = (float)v->num;
+                    if (f >= 0.0f && f <= 1.0f) *target = f;
+                }
+            };
+            apply("OpenPBR_base_weight", &g.base_weight);
+            apply("OpenPBR_emission_weight", &g.emission_weight);
+            apply("OpenPBR_specular_roughness", &g.specular_roughness);
+            apply("OpenPBR_specular_roughness_anisotropy", &g.specular_roughness_anisotropy);
+            apply("OpenPBR_specular_haze", &g.specular_haze);
+            apply("OpenPBR_specular_haze_spread", &g.specular_haze_spread);
+            apply("OpenPBR_specular_retroreflectivity", &g.specular_retroreflectivity);
+        }
+        // no texture: layer -1 and a zero UV transform
+        for (float* uv : {g.base_color_uv, g.normal_uv, g.metallic_roughness_uv, g.emission_uv, g.specular_weight_uv,
+                          g.specular_color_uv})
+            uv[0] = uv[1] = uv[2] = uv[3] = 0.0f;
+        return ptw_add_material(world, &g, out) == PT_OK || fail(ptw_last_error(world));
+    }
+
+    bool primitive(const Json& prim, const M4& model, const double nm[9]) {
+        if (prim.integer("mode", 4) != 4) return true;  // only triangles, as the reference
+        const Json* attrs = prim.get("attributes");
+        if (!attrs || !attrs->get("POSITION")) return true;  // no positions: skipped
+        std::vector<float> pos, nor, tan, uv;
+        size_t nv = 0, n2 = 0;
+        if (!read_floats(attrs->integer("POSITION", -1), 3, pos, &nv)) return false;
+        std::vector<uint32_t> idx;
+        if (prim.get("indices")) {
+            if (!read_indices(prim.integer("indices", -1), idx)) return false;
+            for (uint32_t i : idx)
+                if (i >= nv) return fail("index out of range");
+        }
+        const bool has_n = attrs->get("NORMAL") != nullptr;
+        const bool has_t = has_n && attrs->get("TANGENT") != nullptr;
+        const bool has_uv = attrs->get("TEXCOORD_0") != nullptr;
+        if (has_n && (!read_floats(attrs->integer("NORMAL", -1), 3, nor, &n2) || n2 != nv))
+            return error.empty() ? fail("NORMAL count differs from POSITION") : false;
+        if (has_t && (!read_floats(attrs->integer("TANGENT", -1), 4, tan, &n2) || n2 != nv))
+            return error.empty() ? fail("TANGENT count differs from POSITION") : false;
+        if (has_uv && (!read_floats(attrs->integer("TEXCOORD_0", -1), 2, uv, &n2) || n2 != nv))
+            return error.empty() ? fail("TEXCOORD_0 count differs from POSITION") : false;
+        // transform_point3 / transform_vector3 with the node matrix
+        for (size_t i = 0; i < nv; ++i) {
+            const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+            for (int r = 0; r < 3; ++r)
+                pos[3 * i + r] = ((model.m[r] * x + model.m[4 + r] * y) + model.m[8 + r] * z) + model.m[12 + r];
+        }
+        bool placeholder = false;
+        for (size_t i = 0; has_t && i < nv; ++i) {
+            const float* t = &tan[4 * i];
+            if (t[0] == 1.0f && t[1] == 0.0f && t[2] == 0.0f && t[3] == 1.0f) placeholder = true;
+        }
+        for (size_t i = 0; has_n && i < nv; ++i) {
+            const double x = nor[3 * i], y = nor[3 * i + 1], z = nor[3 * i + 2];
+            for (int r = 0; r < 3; ++r) nor[3 * i + r] = (float)(nm[3 * r] * x + nm[3 * r + 1] * y + nm[3 * r + 2] * z);
+        }
+        for (size_t i = 0; has_t && i < nv; ++i) {
+            const float x = tan[4 * i], y = tan[4 * i + 1], z = tan[4 * i + 2];
+            for (int r = 0; r < 3; ++r) tan[4 * i + r] = (model.m[r] * x + model.m[4 + r] * y) + model.m[8 + r] * z;
+        }
+        uint32_t mi;
+        const Json* mats = doc.get("materials");
+        const long mat_index = prim.integer("material", -1);
+        if (mat_index >= 0) {
+            auto it = material_cache.find(mat_index);
+            if (it != material_cache.end()) {
+                mi = it->second;
+            } else {
+                if (!mats || (size_t)mat_index >= mats->arr.size()) return fail("material out of range");
+                if (!material(&mats->arr[(size_t)mat_index], &mi)) return false;
+                material_cache[mat_index] = mi;
+            }
+        } else if (!material(nullptr, &mi)) {
+            return false;
+        }
+        ptw_mesh mesh;
+        mesh.positions = pos.data();
+        mesh.normals = has_n ? nor.data() : nullptr;
+        mesh.uvs = has_uv ? uv.data() : nullptr;
+        mesh.tangents = has_t && !placeholder ? tan.data() : nullptr;
+        mesh.vertex_count = (uint32_t)nv;
+        mesh.indices = idx.empty() ? nullptr : idx.data();
+        mesh.index_count = (uint32_t)idx.size();
+        mesh.material_index = mi;
+        if (idx.empty() && nv % 3 != 0) return fail("non-indexed primitive with a vertex count not a multiple of 3");
+        return ptw_add_mesh(world, &mesh) == PT_OK || fail(ptw_last_error(world));
+    }
+
+    bool load() {
+        const Json* nodes = doc.get("nodes");
+        const Json* meshes = doc.get("meshes");
+        std::vector<long> roots;
+        const Json* scenes = doc.get("scenes");
+        const long scene = doc.integer("scene", scenes && !scenes->arr.empty() ? 0 : -1);
+        if (scene >= 0 && scenes && (size_t)scene < scenes->arr.size()) {
+            if (const Json* sn = scenes->arr[(size_t)scene].get("nodes"))
+                for (const Json& n : sn->arr) roots.push_back((long)n.num);
+        } else if (nodes) {
+            for (size_t i = 0; i < nodes->arr.size(); ++i) roots.push_back((long)i);
+        }
+        // the reference's LIFO node stack: the last root first, children pushed in order
+        std::vector<std::pair<long, M4>> stack;
+        for (long r : roots) stack.emplace_back(r, identity());
+        size_t visited = 0;
+        while (!stack.empty()) {
+            const auto [ni, parent] = stack.back();
+            stack.pop_back();
+            if (!nodes || ni < 0 || (size_t)ni >= nodes->arr.size()) return fail("node out of range");
+            if (++visited > 4 * nodes->arr.size() + 16) return fail("node graph is not a tree");
+            const Json& node = nodes->arr[(size_t)ni];
+            M4 local = identity();
+            if (const Json* mtx = node.get("matrix")) {
+                if (mtx->arr.size() != 16) return fail("node matrix must have 16 numbers");
+                for (int i = 0; i < 16; ++i) local.m[i] = (float)mtx->arr[i].num;
+            } else {
+                float t[3] = {0, 0, 0}, q[4] = {0, 0, 0, 1}, s[3] = {1, 1, 1};
+                if (const Json* v = node.get("translation"))
+                    for (int i = 0; i < 3 && i < (int)v->arr.size(); ++i) t[i] = (float)v->arr[i].num;
+                if (const Json* v = node.get("rotation"))
+                    for (int i = 0; i < 4 && i < (int)v->arr.size(); ++i) q[i] = (float)v->arr[i].num;
+                if (const Json* v = node.get("scale"))
+                    for (int i = 0; i < 3 && i < (int)v->arr.size(); ++i) s[i] = (float)v->arr[i].num;
+                local = from_trs(t, q, s);
+            }
+            const M4 model = mul(parent, local);
+            if (node.get("mesh")) {
+                const long mi = node.integer("mesh", -1);
+                if (!meshes || mi < 0 || (size_t)mi >= meshes->arr.size()) return fail("mesh out of range");
+                double nm[9];
+                normal_matrix(model, nm);
+                if (const Json* prims = meshes->arr[(size_t)mi].get("primitives"))
+                    for (const Json& prim : prims->arr)
+                        if (!primitive(prim, model, nm)) return false;
+            }
+            if (const Json* ch = node.get("children"))
+                for (const Json& c : ch->arr) stack.emplace_back((long)c.num, model);
+        }
+        return true;
+    }
+};
+
+}  // namespace
+
+extern "C" int ptw_load_gltf(ptw_world* world, const char* path, char* error, size_t error_size) {
+    if (!world || !path) return PT_ERR_INVALID_ARG;
+    Loader l;
+    l.world = world;
+    const bool ok = l.open(path) && l.load();
+    if (!ok && error && error_size) snprintf(error, error_size, "%s", l.error.c_str());
+    return ok ? PT_OK : PT_ERR_INVALID_ARG;
+}

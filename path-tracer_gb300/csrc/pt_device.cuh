@@ -263,15 +263,29 @@ PTD float ggx_lambda(f3 v, f2 a) {
     return fma_(0.5f, sqrtf(1.0f + (a.x * a.x * v.x * v.x + a.y * a.y * v.y * v.y) / (v.z * v.z)), -0.5f);
 }
 
-// sample_VNDF, trace.slang:356-364
-PTD f3 sample_vndf(f3 wo, f2 a, float r, float two_pi_r) {
+// sample_VNDF, trace.slang:356-364, with sin / cos of 2 pi r given
+PTD f3 sample_vndf_sc(f3 wo, f2 a, float r, float sin_2pr, float cos_2pr) {
     const f3 ww = normalize(mk(wo.x * a.x, wo.y * a.y, wo.z));
     const float z = fma_(1.0f - r, 1.0f + ww.z, -ww.z);
     const float sin_theta = sqrtf(saturate(fma_(-z, z, 1.0f)));
-    const float x = sin_theta * ptm::cosf_(two_pi_r);
-    const float y = sin_theta * ptm::sinf_(two_pi_r);
+    const float x = sin_theta * cos_2pr;
+    const float y = sin_theta * sin_2pr;
     const f3 h = mk(x, y, z) + ww;
     return normalize(mk(h.x * a.x, h.y * a.y, h.z));
+}
+// 1: sin and cos of one argument share one reduction (same bits either way)
+#ifndef PT_SHARED_SINCOS
+#define PT_SHARED_SINCOS 1
+#endif
+PTD f3 sample_vndf(f3 wo, f2 a, float r, float two_pi_r) {
+    float sn, cs;
+#if PT_SHARED_SINCOS
+    ptm::sincosf_(two_pi_r, &sn, &cs);
+#else
+    sn = ptm::sinf_(two_pi_r);
+    cs = ptm::cosf_(two_pi_r);
+#endif
+    return sample_vndf_sc(wo, a, r, sn, cs);
 }
 
 // alpha_anisotropic, trace.slang:369-375
@@ -478,7 +492,9 @@ PTD LightSample sample_light(const World& w, f3 origin, Rng<kRec>& rng, Counters
         const float shs = mix(a * a, b * b, rng());
         const float cos_theta = 1.0f - 2.0f * shs;
         const float sin_theta = 2.0f * sqrtf(fmaxf(0.0f, shs * (1.0f - shs)));
-        r.direction = mk(sin_theta * ptm::cosf_(phi), north ? cos_theta : -cos_theta, sin_theta * ptm::sinf_(phi));
+        float sin_phi, cos_phi;
+        ptm::sincosf_(phi, &sin_phi, &cos_phi);
+        r.direction = mk(sin_theta * cos_phi, north ? cos_theta : -cos_theta, sin_theta * sin_phi);
         r.distance = kFltMax;
         r.pdf = skybox_light_pdf(w, r.direction, p1);
         r.emission = evaluate_skybox(w, r.direction);

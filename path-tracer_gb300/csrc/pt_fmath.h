@@ -177,6 +177,19 @@ PT_HD float cosf_(float x) {
     }
 }
 
+// sin and cos of one argument with one reduction: bitwise sinf_(x), cosf_(x)
+PT_HD void sincosf_(float x, float* sn, float* cs) {
+    int q;
+    const float r = reduce_pio2(x, &q);
+    const float s = sin_kernel(r), c = cos_kernel(r);
+    switch (q) {
+        case 0: *sn = s; *cs = c; break;
+        case 1: *sn = c; *cs = -s; break;
+        case 2: *sn = -s; *cs = -c; break;
+        default: *sn = -c; *cs = s; break;
+    }
+}
+
 // asin(z) for |z| <= 1/2 (Taylor to z^25)
 PT_HD float asin_kernel(float z) {
     const float z2 = z * z;

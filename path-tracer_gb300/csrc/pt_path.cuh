@@ -339,19 +339,26 @@ PTD bool shade_hit(const World& w, uint32_t bounce, uint32_t max_bounces, PathSt
     // BSDF sampling, trace.slang:1212-1260
     const float two_pi_r = kTwoPi * rng();
     const float r1 = rng();
+    float sin_2pr, cos_2pr;  // every branch below uses both
+#if PT_SHARED_SINCOS
+    ptm::sincosf_(two_pi_r, &sin_2pr, &cos_2pr);
+#else
+    sin_2pr = ptm::sinf_(two_pi_r);
+    cos_2pr = ptm::cosf_(two_pi_r);
+#endif
     f3 wi;
     if (rng() < b.p_ggx) {
-        wi = reflect(-wo, sample_vndf(wo, b.alpha, r1, two_pi_r));
+        wi = reflect(-wo, sample_vndf_sc(wo, b.alpha, r1, sin_2pr, cos_2pr));
     } else if (r1 < b.p_u) {
         const float u1 = r1 / b.p_u;
         const float sin_theta = sqrtf(1.0f - u1 * u1);
-        wi = mk(sin_theta * ptm::cosf_(two_pi_r), sin_theta * ptm::sinf_(two_pi_r), u1);
+        wi = mk(sin_theta * cos_2pr, sin_theta * sin_2pr, u1);
     } else {
         const float u1 = (r1 - b.p_u) / b.p_c;
         const float R = sqrtf(u1);
-        const float y = R * ptm::sinf_(two_pi_r);
+        const float y = R * sin_2pr;
         const float s = fma_(0.5f, rsqrt_(fma_(b.ld, b.ld, 1.0f)), 0.5f);
-        const float x = -mix(sqrtf(fma_(-y, y, 1.0f)), R * ptm::cosf_(two_pi_r), s);
+        const float x = -mix(sqrtf(fma_(-y, y, 1.0f)), R * cos_2pr, s);
         const f3 wh = mk(x, y, sqrtf(fmaxf(1.0f - (x * x + y * y), 0.0f)));
         const f3 wu = mk(b.la * wh.x + b.lb * wh.z, b.lc * wh.y, b.ld * wh.x + wh.z);
         wi = normalize(wu.x * b.bx + wu.y * b.by + wu.z * mk(0.0f, 0.0f, 1.0f));

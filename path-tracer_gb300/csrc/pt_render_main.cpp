@@ -7,8 +7,9 @@
 // at most 16 samples per trace call (headless.rs:207-285), each finished tile
 // tone mapped (display.wgsl) and the RGB8 image saved.
 //
-// Scenes: "cornell" (36-triangle Cornell box) or "procedural[:SEED]" (the
-// ~2.1M-triangle procedural scene); glTF files are not read by this build.
+// Scenes: a glTF 2.0 file (.glb or .gltf, untextured materials; the
+// reference's default is its box.glb asset), "cornell" (36-triangle Cornell
+// box) or "procedural[:SEED]" (the ~2.1M-triangle procedural scene).
 // Skyboxes: "black", "procedural" (gradient + sun) or a Radiance .hdr file.
 // Output: .png (or .ppm); JPEG and WebP encoders are not part of this build.
 #include <algorithm>
@@ -341,7 +342,11 @@ int main(int argc, char** argv) {
         p.skybox_width = p.skybox_height = 0;  // the --skybox flag decides the sky
         rc = ptw_scene_procedural(&p, &world);
     } else {
-        return fail("scene", "cannot read scene " + opt.scene + ": only the built-in scenes `cornell` and `procedural[:SEED]` are available");
+        char err[512] = {0};
+        rc = ptw_create(&world);
+        if (!rc) rc = ptw_load_gltf(world, opt.scene.c_str(), err, sizeof err);
+        if (rc) return fail("scene", "cannot read scene " + opt.scene + ": " + err);
+        rc = ptw_build(world);
     }
     if (rc) return fail("scene", "scene construction failed");
     if (opt.skybox == "procedural") {

@@ -4,6 +4,8 @@
 // warp-aggregated queue appends.
 #pragma once
 
+#include <type_traits>
+
 #include "pt_path.cuh"
 
 namespace ptd {
@@ -85,12 +87,12 @@ PTD Stage stage_of(const Queues& q, int cur) {
 #endif
 // 1: a step of the 8-wide traversal tests one triangle of a leaf; 0: the whole leaf
 #ifndef PT_WIDE_TRI_PER_STEP
-#define PT_WIDE_TRI_PER_STEP 1
+#define PT_WIDE_TRI_PER_STEP 0
 #endif
 constexpr uint32_t kWideLeafMerge = PT_WIDE_LEAF_MERGE;
 // resident blocks per SM the 8-wide traversal kernels are compiled for
 #ifndef PT_WIDE_MIN_BLOCKS
-#define PT_WIDE_MIN_BLOCKS 6
+#define PT_WIDE_MIN_BLOCKS 8
 #endif
 // 1: a traversal step tests one triangle of a leaf; 0: a whole leaf
 #ifndef PT_TRI_PER_STEP
@@ -370,9 +372,55 @@ PTD bool binary_first(const Fast& f, f3 o, f3 d, uint32_t a, uint32_t b) {
 // rest of its list), one entry per level.  Triangles are tested one per step
 // with the reference's watertight test, so a hit's (t, v, w) are the binary
 // traversal's for the same triangle.  Opaque scenes only.
+// One axis of a wide node in the ray's frame.  A child bound q (8 bits) is
+// placed into the float v = 1 + q 2^-15 with one byte permute, and its slab
+// distance is t = fma(v, a15, c): a15 = 2^(e+15) rcp and c = B - a15 with
+// B = fma(origin, rcp, -o rcp), so t = B + q 2^e rcp up to rounding.  The
+// near bound (the box minimum when rcp >= 0, else the maximum) uses
+// c - eps, the far bound c + eps, with eps = 2^-19 (|B| + |a15| + |o rcp|):
+// more than the sum of the rounding errors of this form, of the
+// reference's slab test on the binary box (trace.slang:597-609), and of the
+// box decode (each at most a few units of 2^-24 of those magnitudes).  So the
+// wide interval contains the interval the reference computes for every
+// binary node under the child, and a box the reference accepts is accepted.
+// An axis the ray does not move along (rcp = 0 here) constrains nothing.
+struct AxisFrame {
+    float a15, c_near, c_far;
+    uint32_t near0, near1, far0, far1;  // bound bytes of children 0-3 / 4-7
+};
+PTD AxisFrame axis_frame(float origin, uint32_t ebyte, float rcp_a, float nod_a, uint32_t lo0, uint32_t lo1,
+                         uint32_t hi0, uint32_t hi1) {
+    AxisFrame f;
+    const bool neg = rcp_a < 0.0f;
+    f.near0 = neg ? hi0 : lo0;
+    f.near1 = neg ? hi1 : lo1;
+    f.far0 = neg ? lo0 : hi0;
+    f.far1 = neg ? lo1 : hi1;
+    if (rcp_a == 0.0f) {
+        const float inf = __int_as_float(0x7f800000);
+        f.a15 = 0.0f;
+        f.c_near = -inf;
+        f.c_far = inf;
+        return f;
+    }
+    const float s15 = __uint_as_float((ebyte + 15u) << 23);  // 2^(e + 15)
+    f.a15 = s15 * rcp_a;
+    const float b = fmaf(origin, rcp_a, nod_a);
+    const float c0 = b - f.a15;
+    const float eps = (fabsf(b) + fabsf(f.a15) + fabsf(nod_a)) * 0x1p-19f;
+    f.c_near = c0 - eps;
+    f.c_far = c0 + eps;
+    return f;
+}
+// v = 1 + q 2^-15 for the bound byte of child i (bytes: 0, q, 0x80, 0x3F)
+template <int i>
+PTD float bound_v(uint32_t w0, uint32_t w1) {
+    return __uint_as_float(__byte_perm(i < 4 ? w0 : w1, 0x3F800000u, 0x7604u | ((unsigned)(i & 3) << 4)));
+}
+
 template <bool kShadow, bool kTri36 = false>
 struct WideTraverser {
-    f3 o, d, rcp, nod_lo, nod_hi;
+    f3 o, d, rcp, nod;
     Shear s;
     float hit_t, hv, hw;
     int32_t hit, light_tri;
@@ -385,14 +433,13 @@ struct WideTraverser {
         d = dir;
         rcp = 1.0f / d;
         s = make_shear(d, rcp);
-        const f3 nod = -o * rcp;
-        nod_lo = nod;
-        nod_hi = nod;
-        // an axis the ray does not move along: t0 = -inf, t1 = +inf
+        nod = -o * rcp;
+        // an axis the ray does not move along: the slab test's 0 * inf is not a
+        // bound, so the axis is left unconstrained
         const float inf = __int_as_float(0x7f800000);
-        if (fabsf(rcp.x) == inf) { rcp.x = 0.0f; nod_lo.x = -inf; nod_hi.x = inf; }
-        if (fabsf(rcp.y) == inf) { rcp.y = 0.0f; nod_lo.y = -inf; nod_hi.y = inf; }
-        if (fabsf(rcp.z) == inf) { rcp.z = 0.0f; nod_lo.z = -inf; nod_hi.z = inf; }
+        if (fabsf(rcp.x) == inf) { rcp.x = 0.0f; nod.x = 0.0f; }
+        if (fabsf(rcp.y) == inf) { rcp.y = 0.0f; nod.y = 0.0f; }
+        if (fabsf(rcp.z) == inf) { rcp.z = 0.0f; nod.z = 0.0f; }
         hit_t = t_max;
         hv = hw = 0.0f;
         hit = -1;
@@ -410,46 +457,40 @@ struct WideTraverser {
         const float4 h0 = __ldg(p), h1 = __ldg(p + 1), h2 = __ldg(p + 2), h3 = __ldg(p + 3);
         const uint32_t meta = __float_as_uint(h0.w);
         const uint32_t count = meta >> 24;
-        const float sx = __uint_as_float((meta & 0xffu) << 23);
-        const float sy = __uint_as_float(((meta >> 8) & 0xffu) << 23);
-        const float sz = __uint_as_float(((meta >> 16) & 0xffu) << 23);
-        const float cx = sx * 8388608.0f, cy = sy * 8388608.0f, cz = sz * 8388608.0f;  // 2^23 * s, exact
-        const uint32_t lox[2] = {__float_as_uint(h1.x), __float_as_uint(h1.y)};
-        const uint32_t loy[2] = {__float_as_uint(h1.z), __float_as_uint(h1.w)};
-        const uint32_t loz[2] = {__float_as_uint(h2.x), __float_as_uint(h2.y)};
-        const uint32_t hix[2] = {__float_as_uint(h2.z), __float_as_uint(h2.w)};
-        const uint32_t hiy[2] = {__float_as_uint(h3.x), __float_as_uint(h3.y)};
-        const uint32_t hiz[2] = {__float_as_uint(h3.z), __float_as_uint(h3.w)};
+        const AxisFrame X = axis_frame(h0.x, meta & 0xffu, rcp.x, nod.x, __float_as_uint(h1.x), __float_as_uint(h1.y),
+                                       __float_as_uint(h2.z), __float_as_uint(h2.w));
+        const AxisFrame Y = axis_frame(h0.y, (meta >> 8) & 0xffu, rcp.y, nod.y, __float_as_uint(h1.z),
+                                       __float_as_uint(h1.w), __float_as_uint(h3.x), __float_as_uint(h3.y));
+        const AxisFrame Z = axis_frame(h0.z, (meta >> 16) & 0xffu, rcp.z, nod.z, __float_as_uint(h2.x),
+                                       __float_as_uint(h2.y), __float_as_uint(h3.z), __float_as_uint(h3.w));
         uint32_t k[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
+        const auto child = [&](auto ic) {
+            constexpr int i = decltype(ic)::value;
             k[i] = 0xffffffffu;
-            if ((uint32_t)i >= count) continue;
-            // q as the float 2^23 + q, then (2^23 + q) * s - 2^23 * s = q * s exactly
-            const unsigned sel = 0x7440u | (unsigned)(i & 3);
-            const int wd = i >> 2;
-            const float qlx = fmaf(__uint_as_float(__byte_perm(lox[wd], 0x4B000000u, sel)), sx, -cx);
-            const float qly = fmaf(__uint_as_float(__byte_perm(loy[wd], 0x4B000000u, sel)), sy, -cy);
-            const float qlz = fmaf(__uint_as_float(__byte_perm(loz[wd], 0x4B000000u, sel)), sz, -cz);
-            const float qhx = fmaf(__uint_as_float(__byte_perm(hix[wd], 0x4B000000u, sel)), sx, -cx);
-            const float qhy = fmaf(__uint_as_float(__byte_perm(hiy[wd], 0x4B000000u, sel)), sy, -cy);
-            const float qhz = fmaf(__uint_as_float(__byte_perm(hiz[wd], 0x4B000000u, sel)), sz, -cz);
-            const float bminx = __fadd_rn(h0.x, qlx), bminy = __fadd_rn(h0.y, qly), bminz = __fadd_rn(h0.z, qlz);
-            const float bmaxx = __fadd_rn(h0.x, qhx), bmaxy = __fadd_rn(h0.y, qhy), bmaxz = __fadd_rn(h0.z, qhz);
-            const float t0x = fma_(bminx, rcp.x, nod_lo.x), t0y = fma_(bminy, rcp.y, nod_lo.y);
-            const float t0z = fma_(bminz, rcp.z, nod_lo.z);
-            const float t1x = fma_(bmaxx, rcp.x, nod_hi.x), t1y = fma_(bmaxy, rcp.y, nod_hi.y);
-            const float t1z = fma_(bmaxz, rcp.z, nod_hi.z);
-            const float t_near = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
-            const float t_far = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
-            const bool h = t_near <= t_far && t_far > 0.0f && t_near < hit_t;
-            if (h) {
+            if ((uint32_t)i >= count) return;
+            const float nx = fmaf(bound_v<i>(X.near0, X.near1), X.a15, X.c_near);
+            const float ny = fmaf(bound_v<i>(Y.near0, Y.near1), Y.a15, Y.c_near);
+            const float nz = fmaf(bound_v<i>(Z.near0, Z.near1), Z.a15, Z.c_near);
+            const float fx = fmaf(bound_v<i>(X.far0, X.far1), X.a15, X.c_far);
+            const float fy = fmaf(bound_v<i>(Y.far0, Y.far1), Y.a15, Y.c_far);
+            const float fz = fmaf(bound_v<i>(Z.far0, Z.far1), Z.a15, Z.c_far);
+            const float t_near = fmaxf(fmaxf(nx, ny), nz);
+            const float t_far = fminf(fminf(fx, fy), fz);
+            if (t_near <= t_far && t_far > 0.0f && t_near < hit_t) {
                 if constexpr (kShadow)
                     k[i] = (uint32_t)i;
                 else
                     k[i] = (__float_as_uint(fmaxf(0.0f, t_near)) & ~7u) | (uint32_t)i;
             }
-        }
+        };
+        child(std::integral_constant<int, 0>());
+        child(std::integral_constant<int, 1>());
+        child(std::integral_constant<int, 2>());
+        child(std::integral_constant<int, 3>());
+        child(std::integral_constant<int, 4>());
+        child(std::integral_constant<int, 5>());
+        child(std::integral_constant<int, 6>());
+        child(std::integral_constant<int, 7>());
         if constexpr (!kShadow) sort8(k);
         uint32_t l = 0u, cnt = 0u;
 #pragma unroll
@@ -535,6 +576,11 @@ struct WideTraverser {
 };
 
 constexpr int kStepsPerRefill = PT_STEPS_PER_REFILL;
+// steps between refills of the 8-wide traversal (its steps are longer)
+#ifndef PT_WIDE_STEPS_PER_REFILL
+#define PT_WIDE_STEPS_PER_REFILL 16
+#endif
+constexpr int kWideStepsPerRefill = PT_WIDE_STEPS_PER_REFILL;
 constexpr unsigned kRefillBelow = PT_REFILL_BELOW;
 
 PTD unsigned lane_id() {

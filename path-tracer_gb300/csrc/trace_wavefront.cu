@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
     __shared__ FilerSlots<kExtendThreads> filer_slots;
     ResultFiler filer = filer_slots.of_warp(lane_id());
     lane_refill_loop(
-        &q.cnt[3], count, kStepsPerRefill, kRefillBelow,
+        &q.cnt[3], count, kWide ? kWideStepsPerRefill : kStepsPerRefill, kRefillBelow,
         [&](uint32_t i) {
             slot = i;
             const float4 o4 = st.o[i], d4 = st.d[i];
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
     uint32_t path = 0;
     float4 contribution = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     lane_refill_loop(
-        &q.cnt[4], count, kStepsPerRefill, kRefillBelow,
+        &q.cnt[4], count, kWide ? kWideStepsPerRefill : kStepsPerRefill, kRefillBelow,
         [&](uint32_t i) {
             const float4 o4 = q.so[i], d4 = q.sd[i];
             contribution = q.sc[i];

@@ -56,6 +56,19 @@ class World:
         return cls(h.value)
 
     @classmethod
+    def from_gltf(cls, path, build: bool = True) -> "World":
+        """A world holding a glTF 2.0 scene (.glb / .gltf); built (BVH, camera) unless build=False."""
+        w = cls.empty()
+        err = C.create_string_buffer(512)
+        rc = w._lib.ptw_load_gltf(w._h, str(path).encode(), err, len(err))
+        if rc != abi.PT_OK:
+            w.close()
+            raise PathTracerError(rc, f"glTF import of {path}: {err.value.decode()}")
+        if build:
+            w.build()
+        return w
+
+    @classmethod
     def cornell_box_textured(cls, seed: int = 1) -> "World":
         """The Cornell room as eight meshes, four with procedural 1024^2 textures (precision workload)."""
         lib = load()

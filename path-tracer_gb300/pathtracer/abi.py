@@ -231,6 +231,7 @@ SIGNATURES = {
     "ptw_add_material": (C.c_int, [_vp, P(Material), P(c_u32)]),
     "ptw_add_mesh": (C.c_int, [_vp, P(Mesh)]),
     "ptw_add_atlas_layer": (C.c_int, [_vp, C.c_int, _vp, P(c_i32)]),
+    "ptw_load_gltf": (C.c_int, [_vp, C.c_char_p, C.c_char_p, C.c_size_t]),
     "ptw_build": (C.c_int, [_vp]),
     "ptw_set_skybox_rgba": (C.c_int, [_vp, _vp, c_u32, c_u32]),
     "ptw_set_procedural_skybox": (C.c_int, [_vp, c_u32, c_u32]),

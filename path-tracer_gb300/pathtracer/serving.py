@@ -218,6 +218,9 @@ def main(argv=None) -> None:
     p.add_argument("--progressive", type=float, default=0.1)
     p.add_argument("--budget-gb", type=float, default=150.0)
     p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--precision", choices=["fp32", "wide", "compressed"], default="fp32",
+                   help="engine form: the reference's FP32 buffers, the 8-wide BVH, or the compressed form "
+                        "(8-wide BVH + FP16 attributes / BF16 skybox + Kahan sums)")
     p.add_argument("--compare", type=int, default=0,
                    help="instead of serving: render this many requests of the mix back to back with the plain "
                         "kernel, the wavefront kernel (one job per call) and the batched engine")
@@ -226,12 +229,15 @@ def main(argv=None) -> None:
     t = time.perf_counter()
     worlds = {n: build_scene(n) for n in names}
     build_s = time.perf_counter() - t
-    eng = Engine(hbm_budget_bytes=int(args.budget_gb * (1 << 30)))
+    precision = {"fp32": abi.PT_PRECISION_FP32, "wide": abi.PT_PRECISION_WIDE_BVH,
+                 "compressed": abi.PT_PRECISION_COMPRESSED}[args.precision]
+    eng = Engine(hbm_budget_bytes=int(args.budget_gb * (1 << 30)), precision=precision)
     server = Server(eng, worlds)
     fixed = tuple(int(x) for x in args.fixed.split(",")) if args.fixed else None
     if args.compare:
         reqs = request_stream(1000.0, args.compare / 1000.0 * 2.0 + 1.0, names, args.seed, 0.0, fixed)[:args.compare]
-        out = {"requests": len(reqs), "triangles": {n: worlds[n].triangle_count() for n in names}}
+        out = {"requests": len(reqs), "engine_precision": args.precision,
+               "triangles": {n: worlds[n].triangle_count() for n in names}}
         for mode in ("engine", "wavefront", "plain"):
             out[mode] = closed_loop(server, reqs, mode)
         out["engine_over_plain"] = out["engine"]["samples_per_s"] / out["plain"]["samples_per_s"]
@@ -247,7 +253,7 @@ def main(argv=None) -> None:
         "rejected": res.rejected, "latency_ms": percentiles(res.latencies_ms),
         "latency_512x512x16_ms": percentiles(res.latencies_512_16_ms),
         "samples_per_s": res.paths / res.wall_s, "wall_s": res.wall_s, "gpu_ms": st["gpu_ms"],
-        "waves": st["waves"], "scene_build_s": build_s,
+        "waves": st["waves"], "scene_build_s": build_s, "engine_precision": args.precision,
         "triangles": {n: worlds[n].triangle_count() for n in names},
     }))
     eng.close()

@@ -66,3 +66,13 @@ def test_log2_exp2():
     want = np.exp2(t.astype(np.float64))
     ok = want > 2.0 ** -126
     assert ulp_error(got[ok], want[ok]).max() <= 2.0
+
+
+def test_sincos_equals_sin_and_cos():
+    """The kernels take sin and cos of one argument through one shared reduction; the bits must be
+    those of the separate functions the oracle uses."""
+    rng = np.random.default_rng(9)
+    x = np.concatenate([rng.uniform(-10, 10, 200000), rng.uniform(0, 2 * np.pi, 200000),
+                        np.array([0.0, -0.0, np.pi / 4, np.pi / 2, np.pi, 2 * np.pi])]).astype(np.float32)
+    np.testing.assert_array_equal(oracle.fmath("sincos_sin", x).view(np.uint32), oracle.fmath("sin", x).view(np.uint32))
+    np.testing.assert_array_equal(oracle.fmath("sincos_cos", x).view(np.uint32), oracle.fmath("cos", x).view(np.uint32))

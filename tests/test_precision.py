@@ -156,3 +156,86 @@ def test_half_attributes_round_to_nearest_even():
     np.testing.assert_array_equal(h16[:, 24:30], exp16(f[:, 9:15]))
     np.testing.assert_array_equal(h16[:, 12:24], exp16(f[:, 15:27]))
     np.testing.assert_array_equal(half.view(np.uint32).reshape(n, 16)[:, 15], mat)
+
+
+def fma32(a, b, c):
+    """float32 fma: the exact product and sum rounded once (through float64; the rare double
+    rounding is far inside the slack checked below)."""
+    return (a.astype(np.float64) * b.astype(np.float64) + c.astype(np.float64)).astype(np.float32)
+
+
+def reference_accept(lo, hi, rcp, nod, hit_t):
+    """The binary traversal's slab test (trace.slang:597-609) in float32."""
+    t0 = fma32(lo, rcp, nod)
+    t1 = fma32(hi, rcp, nod)
+    with np.errstate(invalid="ignore"):
+        near = np.fmax(np.fmax(np.fmin(t0[..., 0], t1[..., 0]), np.fmin(t0[..., 1], t1[..., 1])),
+                       np.fmin(t0[..., 2], t1[..., 2]))
+        far = np.fmin(np.fmin(np.fmax(t0[..., 0], t1[..., 0]), np.fmax(t0[..., 1], t1[..., 1])),
+                      np.fmax(t0[..., 2], t1[..., 2]))
+    return (near <= far) & (far > 0) & (near < hit_t)
+
+
+def wide_accept(origin, ebyte, qlo, qhi, rcp, nod, hit_t):
+    """The 8-wide kernel's test: t = fma(1 + q 2^-15, 2^(e+15) rcp, B - a15 -/+ eps) per bound."""
+    a15 = (np.ldexp(np.float32(1), ebyte.astype(np.int32) - 127 + 15).astype(np.float32) * rcp).astype(np.float32)
+    b = fma32(origin, rcp, nod)
+    c0 = (b - a15).astype(np.float32)
+    eps = ((np.abs(b) + np.abs(a15) + np.abs(nod)).astype(np.float32) * np.float32(2.0 ** -19)).astype(np.float32)
+    neg = rcp < 0
+    qn = np.where(neg, qhi, qlo).astype(np.float32)
+    qf = np.where(neg, qlo, qhi).astype(np.float32)
+    vn = (1 + qn * np.float32(2.0 ** -15)).astype(np.float32)
+    vf = (1 + qf * np.float32(2.0 ** -15)).astype(np.float32)
+    tn = fma32(vn, a15, (c0 - eps).astype(np.float32))
+    tf = fma32(vf, a15, (c0 + eps).astype(np.float32))
+    near = np.max(tn, axis=-1)
+    far = np.min(tf, axis=-1)
+    return (near <= far) & (far > 0) & (near < hit_t)
+
+
+def test_wide_box_test_accepts_whatever_the_binary_test_accepts():
+    """For every child of every wide node and many rays (random, and aimed at box corners and
+    edges, where rounding decides), the kernel's slab test on the quantised box accepts every
+    ray the reference's slab test accepts on the binary node the child stands for."""
+    w = pt.World.procedural(grid_x=48, grid_z=24, boxes=40, spheres=4, sphere_subdivision=2, emissive_triangles=8,
+                            skybox_width=16, skybox_height=8)
+    nodes = w.bvh_nodes()
+    wide, _ = pt.build_wide_bvh(nodes)
+    node_of_range = subtree_ranges(nodes)
+    rows = []  # (wide node, child slot, binary node)
+    for wi, wn in enumerate(wide):
+        for i in range(int(wn["child_count"])):
+            c, tc = int(wn["child"][i]), int(wn["tri_count"][i])
+            rows.append((wi, i, node_of_range[(c, tc)] if tc else int(wide[c]["source_node"])))
+    rows = np.array(rows)
+    bmin = nodes[rows[:, 2], 0:3].view(np.float32)
+    bmax = nodes[rows[:, 2], 4:7].view(np.float32)
+    origin = wide["origin"][rows[:, 0]].astype(np.float32)
+    ebyte = wide["exponent"][rows[:, 0]]
+    qlo = wide["lo"][rows[:, 0], :, rows[:, 1]]
+    qhi = wide["hi"][rows[:, 0], :, rows[:, 1]]
+    rng = np.random.default_rng(17)
+    lo_all, hi_all = bmin.min(axis=0), bmax.max(axis=0)
+    misses = 0
+    for trial in range(24):
+        n = rows.shape[0]
+        o = rng.uniform(lo_all - 5, hi_all + 5, (n, 3)).astype(np.float32)
+        if trial % 3 == 0:
+            d = rng.normal(size=(n, 3))
+        else:  # towards a corner (trial 1 mod 3) or an edge midpoint of the binary box
+            pick = rng.integers(0, 2, (n, 3)).astype(bool)
+            target = np.where(pick, bmin, bmax).astype(np.float64)
+            if trial % 3 == 2:
+                k = rng.integers(0, 3, n)
+                target[np.arange(n), k] = 0.5 * (bmin[np.arange(n), k] + bmax[np.arange(n), k])
+            d = target - o
+        d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+        with np.errstate(divide="ignore"):
+            rcp = (np.float32(1) / d).astype(np.float32)
+        nod = (-o * rcp).astype(np.float32)
+        hit_t = np.where(rng.random(n) < 0.5, np.float32(np.inf), rng.uniform(0.1, 60, n)).astype(np.float32)
+        ref = reference_accept(bmin, bmax, rcp, nod, hit_t)
+        wid = wide_accept(origin, ebyte, qlo, qhi, rcp, nod, hit_t)
+        misses += int(np.count_nonzero(ref & ~wid))
+    assert misses == 0
