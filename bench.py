@@ -180,6 +180,7 @@ def latency_report(updates, precision: int, rate: float = 20.0, seconds: float =
     sid = eng.add_scene(updates)
     warm = eng.submit(sid, cam, size, size, spp, depth)  # graph capture, layouts
     eng.wait_idle(timeout_ms=0)
+    eng.poll(timeout_ms=0)
     eng.release(warm)
     lat, arrival_of, i = [], {}, 0
     t0 = time.perf_counter()
@@ -189,8 +190,9 @@ def latency_report(updates, precision: int, rate: float = 20.0, seconds: float =
             arrival_of[eng.submit(sid, cam, size, size, spp, depth)] = reqs[i].arrival
             i += 1
         for jid in eng.poll(timeout_ms=1):
-            lat.append((time.perf_counter() - t0 - arrival_of.pop(jid)) * 1e3)
-            eng.release(jid)
+            if jid in arrival_of:  # (the warm-up job is reported here too)
+                lat.append((time.perf_counter() - t0 - arrival_of.pop(jid)) * 1e3)
+                eng.release(jid)
     eng.close()
     tr = pt.PathTracer(updates, (size, size))
     tr.set_kernel(abi.PT_KERNEL_PLAIN)

@@ -47,6 +47,9 @@ typedef struct pt_engine_config {
                                    buffers.  With PT_PRECISION_HALF_ATTRIBUTES a cached scene keeps only
                                    the FP16 attributes and BF16 skybox; with PT_PRECISION_WIDE_BVH an
                                    opaque scene keeps only the 8-wide BVH */
+    uint32_t sort_min_hits;     /* a bounce with at least this many hits sorts them by triangle bucket
+                                   (1024 triangles each, BVH order) before shading; 0 = 65536,
+                                   0xffffffff = never */
 } pt_engine_config;
 
 int pte_create(const pt_engine_config* config, pt_engine** out);
@@ -104,12 +107,12 @@ typedef struct pt_engine_stats {
     uint64_t hbm_used;
     uint64_t hbm_budget;
     double gpu_ms;               /* device time of all finished waves (CUDA events) */
-    uint32_t wave_paths, tile_size, steps_per_refill, use_graphs;
+    uint32_t wave_paths, tile_size, steps_per_refill, use_graphs, precision, sort_min_hits;
 } pt_engine_stats;
 int pte_stats(pt_engine* engine, pt_engine_stats* stats);
 
 /* Autotuner: renders the given jobs once per candidate configuration
- * (wave_paths x tile_size x steps_per_refill) and keeps the one with the
+ * (wave_paths x tile_size x steps_per_refill x sort on/off) and keeps the one with the
  * highest paths per second of device time; writes it to *chosen.  The jobs'
  * results are discarded. */
 int pte_autotune(pt_engine* engine, const pt_job_desc* jobs, uint32_t count, pt_engine_config* chosen);

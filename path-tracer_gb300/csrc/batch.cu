@@ -68,6 +68,7 @@ struct WaveBufs {
 constexpr uint32_t kMaxScenes = 256;
 constexpr uint32_t kMaxSlots = 1u << 16;
 constexpr uint32_t kRounds = PT_MAX_BOUNCES_LIMIT + 1;
+constexpr uint32_t kEngineSortShift = 10;  // sort bucket = triangle index / 1024
 
 // ---------------------------------------------------------------- kernels
 
@@ -132,6 +133,7 @@ __global__ void reset_kernel(uint32_t* cnt, int next) {
     cnt[4] = 0u;
     cnt[5] = 0u;
     cnt[6] = 0u;
+    cnt[7] = 0u;  // set again by the sort when it runs
 }
 
 template <bool kAlpha, bool kWide>
@@ -171,7 +173,7 @@ __global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kern
                                                                                    const JobDev* jobs, WaveBufs b,
                                                                                    int cur, uint32_t bounce) {
     const Stage st = stage_of(b.q, cur);
-    const ShadeRange range(b.q.cnt);
+    const ShadeRange range(b.q);
     const uint32_t count = range.count();
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
@@ -437,6 +439,7 @@ struct pt_engine {
     uint64_t head_seen = 0;
     Buf wave[13];
     Buf d_tag, d_wave_item, d_wave_off;
+    uint32_t* sort_counts = nullptr;  // kSortBuckets counts, then kSortBuckets offsets (inside wave[12])
     ptb::WaveBufs wb{};
     uint32_t max_items = 0;
     bool wave_ready = false;
@@ -469,7 +472,7 @@ struct pt_engine {
 namespace {
 
 uint64_t wave_bytes(uint32_t paths) {
-    return (uint64_t)paths * (11 * 16 + 4 + 8) + 2ull * (paths / 64 + 2) * 4 + 4096;
+    return (uint64_t)paths * (11 * 16 + 4 + 12) + 2ull * (paths / 64 + 2) * 4 + 2 * kSortBuckets * 4 + 4096;
 }
 
 void drop_graphs(pt_engine* e) {
@@ -495,7 +498,8 @@ int setup_wave(pt_engine* e) {
     int rc = PT_OK;
     for (int k = 0; k < 11 && !rc; ++k) rc = e->cuda(e->wave[k].alloc((size_t)W * 16), "wave buffers");
     if (!rc) rc = e->cuda(e->wave[11].alloc(64), "wave counters");
-    if (!rc) rc = e->cuda(e->wave[12].alloc((size_t)W * 8), "wave hit and miss lists");
+    if (!rc) rc = e->cuda(e->wave[12].alloc((size_t)W * 12 + 2 * kSortBuckets * 4), "wave hit lists");
+    if (!rc) rc = e->cuda(cudaMemset(e->wave[12].as<uint32_t>() + 3 * (size_t)W, 0, kSortBuckets * 4), "sort counts");
     if (!rc) rc = e->cuda(e->d_tag.alloc((size_t)W * 4), "wave buffers");
     if (!rc) rc = e->cuda(e->d_wave_item.alloc((size_t)(e->max_items + 1) * 4), "wave buffers");
     if (!rc) rc = e->cuda(e->d_wave_off.alloc((size_t)(e->max_items + 1) * 4), "wave buffers");
@@ -515,6 +519,8 @@ int setup_wave(pt_engine* e) {
     q.cnt = e->wave[11].as<uint32_t>();
     q.hit_list = e->wave[12].as<uint32_t>();
     q.miss_list = q.hit_list + W;
+    q.hit_sorted = q.miss_list + W;
+    e->sort_counts = q.hit_sorted + W;
     q.rec = nullptr;
     q.rec_hits = nullptr;
     e->wb.tag = e->d_tag.as<uint32_t>();
@@ -551,6 +557,15 @@ cudaError_t issue_wave(pt_engine* e) {
     for (uint32_t bounce = 0; bounce < kRounds; ++bounce) {
         reset_kernel<<<1, 1, 0, s>>>(e->wb.q.cnt, cur ^ 1);
         extend_kernel<kAlpha, kWide><<<ext, kExtendThreads, 0, s>>>(scenes, e->wb, cur, e->cfg.steps_per_refill);
+        if (e->cfg.sort_min_hits != 0xffffffffu) {
+            // hits of all jobs by triangle bucket (1024 triangles per bucket)
+            sort_count_kernel<1><<<e->sms * 4, kSortThreads, 0, s>>>(World{}, e->wb.q, e->sort_counts,
+                                                                   e->cfg.sort_min_hits, kEngineSortShift);
+            sort_scan_kernel<0><<<1, 1024, 0, s>>>(e->wb.q, e->sort_counts, e->sort_counts + kSortBuckets,
+                                                   e->cfg.sort_min_hits);
+            sort_scatter_kernel<1><<<e->sms * 4, kSortThreads, 0, s>>>(World{}, e->wb.q, e->sort_counts + kSortBuckets,
+                                                                     e->cfg.sort_min_hits, kEngineSortShift);
+        }
         shade_kernel<kAlpha><<<sha, kShadeThreads, 0, s>>>(scenes, jobs, e->wb, cur, bounce);
         if constexpr (!kAlpha) shadow_kernel<kWide><<<shd, kExtendThreads, 0, s>>>(scenes, e->wb, e->cfg.steps_per_refill);
         cur ^= 1;
@@ -862,6 +877,7 @@ int pte_create(const pt_engine_config* cfg, pt_engine** out) {
     if (e->cfg.wave_paths == 0) e->cfg.wave_paths = 1u << 22;
     if (e->cfg.tile_size == 0) e->cfg.tile_size = 32;
     if (e->cfg.steps_per_refill == 0) e->cfg.steps_per_refill = 32;
+    if (e->cfg.sort_min_hits == 0) e->cfg.sort_min_hits = 65536u;
     e->budget = e->cfg.hbm_budget_bytes ? e->cfg.hbm_budget_bytes : 150ull << 30;
     int rc = PT_OK;
     if (e->cfg.tile_size > 256 || e->cfg.wave_paths < (1u << 12) || e->cfg.wave_paths > (1u << 28))
@@ -1202,6 +1218,8 @@ int pte_stats(pt_engine* e, pt_engine_stats* s) {
     s->wave_paths = e->cfg.wave_paths;
     s->tile_size = e->cfg.tile_size;
     s->steps_per_refill = e->cfg.steps_per_refill;
+    s->precision = e->cfg.precision;
+    s->sort_min_hits = e->cfg.sort_min_hits;
     s->use_graphs = e->cfg.use_graphs;
     return PT_OK;
 }
@@ -1214,11 +1232,13 @@ int pte_autotune(pt_engine* e, const pt_job_desc* jobs, uint32_t count, pt_engin
     const uint32_t waves[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23};
     const uint32_t tiles[] = {16, 32, 64};
     const uint32_t steps[] = {16, 32};
+    const uint32_t sorts[] = {0xffffffffu, 65536u};
     pt_engine_config best = e->cfg;
     double best_rate = -1.0;
     for (uint32_t W : waves)
         for (uint32_t T : tiles)
-            for (uint32_t S : steps) {
+            for (uint32_t S : steps)
+            for (uint32_t H : sorts) {
                 bool fits = true;
                 for (uint32_t k = 0; k < count; ++k) fits &= (uint64_t)T * T * jobs[k].samples <= W;
                 if (!fits) continue;
@@ -1228,6 +1248,7 @@ int pte_autotune(pt_engine* e, const pt_job_desc* jobs, uint32_t count, pt_engin
                 }
                 e->cfg.tile_size = T;
                 e->cfg.steps_per_refill = S;
+                e->cfg.sort_min_hits = H;
                 drop_graphs(e);
                 // one untimed pass to capture graphs, then the timed pass
                 for (int pass = 0; pass < 2; ++pass) {

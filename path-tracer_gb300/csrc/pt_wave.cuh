@@ -30,8 +30,9 @@ struct Queues {
     float4* sc;
     uint32_t* hit_list;   // slots of the current queue whose ray hit a triangle
     uint32_t* miss_list;  // slots whose ray left the scene
+    uint32_t* hit_sorted = nullptr;  // the hit list sorted by key (when cnt[7] != 0)
     uint32_t* cnt;  // [0], [1] ray queue lengths, [2] shadow length, [3] extend fetch, [4] shadow fetch,
-                    // [5] hit list length, [6] miss list length
+                    // [5] hit list length, [6] miss list length, [7] 1 if hit_sorted holds this bounce's hits
     Counters* rec;  // per path (recording variants)
     int32_t* rec_hits;
 };
@@ -578,7 +579,7 @@ struct WideTraverser {
 constexpr int kStepsPerRefill = PT_STEPS_PER_REFILL;
 // steps between refills of the 8-wide traversal (its steps are longer)
 #ifndef PT_WIDE_STEPS_PER_REFILL
-#define PT_WIDE_STEPS_PER_REFILL 16
+#define PT_WIDE_STEPS_PER_REFILL 8
 #endif
 constexpr int kWideStepsPerRefill = PT_WIDE_STEPS_PER_REFILL;
 constexpr unsigned kRefillBelow = PT_REFILL_BELOW;
@@ -655,15 +656,119 @@ struct NoRound {
 // whole warps, then hits.  Entry j of that range maps to a queue slot.
 struct ShadeRange {
     uint32_t n_hit, n_miss, miss_span;
-    PTD ShadeRange(const uint32_t* cnt) : n_hit(cnt[5]), n_miss(cnt[6]), miss_span((cnt[6] + 31u) & ~31u) {}
+    const uint32_t* hits;
+    PTD ShadeRange(const Queues& q)
+        : n_hit(q.cnt[5]), n_miss(q.cnt[6]), miss_span((q.cnt[6] + 31u) & ~31u),
+          hits(q.cnt[7] ? q.hit_sorted : q.hit_list) {}
     PTD uint32_t count() const { return miss_span + n_hit; }
     // queue slot of entry j, or 0xffffffff for the padding after the misses and past the end
     PTD uint32_t slot(const Queues& q, uint32_t j) const {
         if (j < miss_span) return j < n_miss ? q.miss_list[j] : 0xffffffffu;
         const uint32_t k = j - miss_span;
-        return k < n_hit ? q.hit_list[k] : 0xffffffffu;
+        return k < n_hit ? hits[k] : 0xffffffffu;
     }
 };
+
+// ---- hit sorting before shading: a counting sort of the hit list into
+// kSortBuckets keys, so that neighbouring lanes shade hits of the same
+// material (key mode 0: material index) or of nearby triangles (mode 1:
+// triangle index >> shift; triangles are in BVH order, so nearby in space,
+// and mostly of one mesh).  Three passes: block histograms into global
+// counts; one block scans the counts into bucket offsets (and clears the
+// counts for the next bounce); blocks recount their chunk, reserve each
+// key's range with one global atomic and scatter.  Skipped (cnt[7] = 0)
+// below min_hits.
+constexpr uint32_t kSortBuckets = 4096;
+constexpr int kSortThreads = 256, kSortItems = 8;
+
+template <int kMode>
+PTD uint32_t hit_key(const World& w, const Queues& q, uint32_t slot, uint32_t tri_shift) {
+    const uint32_t tri = __float_as_uint(__ldg(&q.hit[slot].y));
+    if constexpr (kMode == 0) return attr_material(w, tri) & (kSortBuckets - 1u);
+    const uint32_t k = tri >> tri_shift;
+    return k < kSortBuckets ? k : kSortBuckets - 1u;
+}
+
+template <int kMode>
+__global__ void __launch_bounds__(kSortThreads) sort_count_kernel(World w, Queues q, uint32_t* counts,
+                                                                   uint32_t min_hits, uint32_t tri_shift) {
+    __shared__ uint32_t hist[kSortBuckets];
+    const uint32_t n = q.cnt[5];
+    if (n < min_hits) return;
+    for (uint32_t i = threadIdx.x; i < kSortBuckets; i += blockDim.x) hist[i] = 0u;
+    __syncthreads();
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        atomicAdd(&hist[hit_key<kMode>(w, q, q.hit_list[j], tri_shift)], 1u);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < kSortBuckets; i += blockDim.x)
+        if (hist[i]) atomicAdd(&counts[i], hist[i]);
+}
+
+// one block of 1024 threads, 4 buckets each
+template <int kUnused>
+__global__ void __launch_bounds__(1024) sort_scan_kernel(Queues q, uint32_t* counts, uint32_t* offsets,
+                                                          uint32_t min_hits) {
+    __shared__ uint32_t part[1024];
+    const uint32_t t = threadIdx.x;
+    if (q.cnt[5] < min_hits) {
+        if (t == 0) q.cnt[7] = 0u;
+        return;
+    }
+    uint32_t c[4], sum = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        c[k] = counts[4 * t + k];
+        counts[4 * t + k] = 0u;
+        sum += c[k];
+    }
+    part[t] = sum;
+    __syncthreads();
+    for (uint32_t off = 1; off < 1024u; off <<= 1) {
+        const uint32_t v = t >= off ? part[t - off] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    uint32_t base = part[t] - sum;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        offsets[4 * t + k] = base;
+        base += c[k];
+    }
+    if (t == 0) q.cnt[7] = 1u;
+}
+
+template <int kMode>
+__global__ void __launch_bounds__(kSortThreads) sort_scatter_kernel(World w, Queues q, uint32_t* offsets,
+                                                                     uint32_t min_hits, uint32_t tri_shift) {
+    __shared__ uint32_t hist[kSortBuckets];
+    const uint32_t n = q.cnt[5];
+    if (n < min_hits) return;
+    const uint32_t chunk = kSortThreads * kSortItems;
+    for (uint32_t c0 = blockIdx.x * chunk; c0 < n; c0 += gridDim.x * chunk) {
+        for (uint32_t i = threadIdx.x; i < kSortBuckets; i += blockDim.x) hist[i] = 0u;
+        __syncthreads();
+        uint32_t keys[kSortItems], slots[kSortItems];
+#pragma unroll
+        for (int k = 0; k < kSortItems; ++k) {
+            const uint32_t j = c0 + (uint32_t)k * kSortThreads + threadIdx.x;
+            keys[k] = 0xffffffffu;
+            if (j < n) {
+                slots[k] = q.hit_list[j];
+                keys[k] = hit_key<kMode>(w, q, slots[k], tri_shift);
+                atomicAdd(&hist[keys[k]], 1u);
+            }
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < kSortBuckets; i += blockDim.x)
+            if (hist[i]) hist[i] = atomicAdd(&offsets[i], hist[i]);  // this block's range of key i
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kSortItems; ++k)
+            if (keys[k] != 0xffffffffu) q.hit_sorted[atomicAdd(&hist[keys[k]], 1u)] = slots[k];
+        __syncthreads();
+    }
+}
 
 // The persistent traversal loop of one warp; every lane holds at most one ray.
 // Each round the warp counts its busy lanes: when fewer than refill_below are

@@ -76,6 +76,7 @@ __global__ void bounce_reset_kernel(uint32_t* cnt, int next) {
     cnt[4] = 0u;
     cnt[5] = 0u;
     cnt[6] = 0u;
+    cnt[7] = 0u;
 }
 
 // Persistent extend kernel: every lane traverses its own ray and takes a new
@@ -122,7 +123,7 @@ template <bool kRec, bool kAlpha>
 __global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kernel(World w, Fast f, Queues q, int cur, uint32_t bounce,
                                                               uint32_t max_bounces) {
     const Stage st = stage_of(q, cur);
-    const ShadeRange range(q.cnt);
+    const ShadeRange range(q);
     const uint32_t count = range.count();
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
@@ -374,12 +375,13 @@ constexpr uint64_t kMaxPaths = 1ull << 25;  // paths in flight per group
 
 struct Wavefront {
     Buf o[2], d[2], T[2], hit, color, so, sd, sc, cnt, rec, rec_hits;
-    Buf lists;  // hit list, miss list (capacity entries each)
+    Buf lists;  // hit list, miss list, sorted hit list (capacity entries each), sort counts and offsets
     Buf pairs, tri4;
     Buf wide, links, attr_h, sky_h;  // precision form copies (links: parent per node, leaf per triangle)
     bool stale = true;
     bool wide_ready = false, attr_h_ready = false, sky_h_ready = false;
     uint64_t wide_count = 0;
+    uint64_t tri_count = 0;    // of the world the layouts were built for
     uint64_t links_nodes = 0;  // node count of the links array (leaf_of follows the parents)
     const void* layout_nodes = nullptr;  // world buffers the layouts were built from
     const void* layout_geo = nullptr;
@@ -428,6 +430,7 @@ cudaError_t build_layouts(Wavefront* wf, const ptd::World& w, uint64_t nodes, ui
     wf->stale = false;
     wf->layout_nodes = w.nodes;
     wf->layout_geo = w.geo;
+    wf->tri_count = tris;
     wf->wide_ready = wf->attr_h_ready = false;
     return cudaSuccess;
 }
@@ -464,7 +467,8 @@ cudaError_t reserve_paths(Wavefront* wf, uint64_t paths, bool record) {
                    &wf->sd, &wf->sc})
         PTW_TRY(x->reserve(b));
     PTW_TRY(wf->cnt.reserve(64));
-    PTW_TRY(wf->lists.reserve(paths * 8));
+    PTW_TRY(wf->lists.reserve(paths * 12 + 2 * ptd::kSortBuckets * 4));
+    PTW_TRY(cudaMemset(static_cast<uint32_t*>(wf->lists.p) + 3 * paths, 0, ptd::kSortBuckets * 4));  // sort counts
     if (record) {
         PTW_TRY(wf->rec.reserve(paths * sizeof(ptd::Counters)));
         PTW_TRY(wf->rec_hits.reserve(paths * PT_RECORD_MAX_BOUNCES * 4));
@@ -480,13 +484,30 @@ int occupancy(K kernel, int threads) {
     return blocks > 0 ? blocks : 1;
 }
 
+// hit sorting of one trace: counts[kSortBuckets] then offsets[kSortBuckets];
+// min_hits == ~0u: no sorting
+struct SortCfg {
+    uint32_t* counts = nullptr;
+    uint32_t min_hits = 0xffffffffu;
+    uint32_t tri_shift = 0;
+};
+
+// hits are sorted before shading when a bounce has at least this many
+// (0xffffffff: never); key 1 = triangle bucket, 0 = material index
+#ifndef PT_SORT_MIN_HITS
+#define PT_SORT_MIN_HITS 65536u
+#endif
+#ifndef PT_SORT_KEY
+#define PT_SORT_KEY 1
+#endif
+
 // one group of paths through raygen, max_bounces + 1 rounds of extend /
-// shade / shadow, and accumulate; kTri36 reads the reference's 36-byte
-// triangles instead of the padded copy
+// (hit sort) / shade / shadow, and accumulate; kTri36 reads the reference's
+// 36-byte triangles instead of the padded copy
 template <bool kRec, bool kAlpha, bool kTri36, bool kWide = false, class TimerF>
 cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const ptd::Queues& q,
                       const ptk::Tile& tile, const ptd::Group& g, ptk::Sinks sinks, cudaStream_t stream,
-                      TimerF&& timer) {
+                      TimerF&& timer, const SortCfg& sort = SortCfg()) {
     using namespace ptd;
     const int ext_blocks = sms * occupancy(extend_kernel<kRec, kAlpha, kTri36, kWide>, kExtendThreads);
     const int sha_blocks = sms * occupancy(shade_kernel<kRec, kAlpha>, kShadeThreads);
@@ -503,6 +524,16 @@ cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const pt
             extend_kernel<kRec, kAlpha, kTri36, kWide><<<ext_blocks, kExtendThreads, 0, stream>>>(w, f, q, cur, bounce);
             return cudaGetLastError();
         }));
+        if (sort.counts && sort.min_hits != 0xffffffffu) {
+            PTW_TRY(timer(PT_KC_SHADE, [&] {
+                sort_count_kernel<PT_SORT_KEY><<<sms * 4, kSortThreads, 0, stream>>>(w, q, sort.counts, sort.min_hits,
+                                                                                    sort.tri_shift);
+                sort_scan_kernel<0><<<1, 1024, 0, stream>>>(q, sort.counts, sort.counts + kSortBuckets, sort.min_hits);
+                sort_scatter_kernel<PT_SORT_KEY><<<sms * 4, kSortThreads, 0, stream>>>(
+                    w, q, sort.counts + kSortBuckets, sort.min_hits, sort.tri_shift);
+                return cudaGetLastError();
+            }));
+        }
         PTW_TRY(timer(PT_KC_SHADE, [&] {
             shade_kernel<kRec, kAlpha><<<sha_blocks, kShadeThreads, 0, stream>>>(w, f, q, cur, bounce, tile.max_bounces);
             return cudaGetLastError();
@@ -565,6 +596,8 @@ cudaError_t trace(Wavefront* wf, const ptd::World& w_in, const ptk::Tile& tile, 
     q.cnt = static_cast<uint32_t*>(wf->cnt.p);
     q.hit_list = static_cast<uint32_t*>(wf->lists.p);
     q.miss_list = q.hit_list + wf->capacity;
+    q.hit_sorted = q.miss_list + wf->capacity;
+    uint32_t* sort_counts = q.hit_sorted + wf->capacity;  // kSortBuckets counts, then kSortBuckets offsets
     q.rec = static_cast<ptd::Counters*>(wf->rec.p);
     q.rec_hits = static_cast<int32_t*>(wf->rec_hits.p);
     ptd::Fast f;
@@ -573,6 +606,10 @@ cudaError_t trace(Wavefront* wf, const ptd::World& w_in, const ptk::Tile& tile, 
     f.wide = static_cast<const float4*>(wf->wide.p);
     f.parent = static_cast<const uint32_t*>(wf->links.p);
     f.leaf_of = f.parent ? f.parent + wf->links_nodes : nullptr;
+    SortCfg sort;
+    sort.counts = sort_counts;
+    sort.min_hits = PT_SORT_MIN_HITS;
+    while (((uint64_t)ptd::kSortBuckets << sort.tri_shift) < wf->tri_count && sort.tri_shift < 31u) sort.tri_shift += 1u;
     for (uint32_t s0 = 0; s0 < samples; s0 += group) {
         ptd::Group g;
         g.vis_w = vis_w;
@@ -587,10 +624,10 @@ cudaError_t trace(Wavefront* wf, const ptd::World& w_in, const ptk::Tile& tile, 
             e = w.any_alpha ? run_group<true, true, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer)
                             : run_group<true, false, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer);
         else if (wide)
-            e = run_group<false, false, false, true>(wf->sms, w, f, q, tile, g, sinks, stream, timer);
+            e = run_group<false, false, false, true>(wf->sms, w, f, q, tile, g, sinks, stream, timer, sort);
         else
-            e = w.any_alpha ? run_group<false, true, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer)
-                            : run_group<false, false, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer);
+            e = w.any_alpha ? run_group<false, true, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer, sort)
+                            : run_group<false, false, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer, sort);
         PTW_TRY(e);
     }
     return cudaSuccess;

@@ -105,6 +105,22 @@ def test_progressive_refinement(scenes):
     eng.close()
 
 
+def test_hit_sorting_keeps_every_job_bit_exact(scenes):
+    """Sorting each bounce's hits before shading only reorders the work: same bits as unsorted."""
+    outs = []
+    for sort in (1, 0xFFFFFFFF):  # sort from one hit on, and never
+        eng = Engine(wave_paths=1 << 15, tile_size=16, sort_min_hits=sort)
+        ids = {name: eng.add_scene(scenes.full[name]) for name in scenes.full}
+        cams = [scenes.camera(n, w, h, yaw) for n, w, h, _, _, yaw in JOBS]
+        jobs = [eng.submit(ids[n], cam, w, h, spp, b) for (n, w, h, spp, b, _), cam in zip(JOBS, cams)]
+        eng.wait_idle(timeout_ms=300000)
+        assert eng.stats()["sort_min_hits"] == sort
+        outs.append([eng.read(j, w, h, abi.PT_TILE_ACCUMULATION) for (_, w, h, _, _, _), j in zip(JOBS, jobs)])
+        eng.close()
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
 def test_graph_replay_matches_plain_launches(scenes):
     outs = []
     for graphs in (True, False):
@@ -162,6 +178,7 @@ def test_autotune_picks_a_candidate(scenes):
     cfg = eng.autotune([abi.JobDesc(sid, cam, 128, 128, 2, 4, 0), abi.JobDesc(sid, cam, 64, 64, 4, 4, 0)])
     assert cfg["wave_paths"] in (1 << 20, 1 << 21, 1 << 22, 1 << 23)
     assert cfg["tile_size"] in (16, 32, 64) and cfg["steps_per_refill"] in (16, 32)
+    assert cfg["sort_min_hits"] in (65536, 0xFFFFFFFF)
     j = eng.submit(sid, cam, 64, 64, 2, 4)
     eng.wait_idle(timeout_ms=300000)
     assert eng.status(j)[0] == abi.PT_JOB_DONE
