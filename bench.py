@@ -38,9 +38,11 @@ KERNEL_NAMES = {"wavefront": 0, "plain": 1}
 # include/pt_precision.h: FP32 (the reference's buffers), 8-wide quantised BVH only, or the full
 # compressed form (wide BVH + FP16 attributes / BF16 skybox + Kahan sums)
 PRECISIONS = {"fp32": 0, "wide": 1, "compressed": 7}
-# DRAM bytes (read + write) per launch of the dominant kernel for this
-# workload, from the ncu capture summarised in profiles/ (None until captured)
-TRAFFIC_PER_LAUNCH: dict = {}
+# DRAM bytes (read + write) per launch of the dominant kernel on this workload
+# (1920x1080, 64 spp, FP32 form), from the single-pass ncu capture of the
+# first 16-spp group's 9 launches summarised in
+# profiles/wavefront_procedural_1920x1080.md
+TRAFFIC_PER_LAUNCH: dict = {("wavefront", "extend", "fp32"): 628.2e6}
 
 
 def parse_args():
@@ -403,7 +405,8 @@ def run_ours(args):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = bytes_per_launch / avg_launch_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": TRAFFIC_PER_LAUNCH.get((args.kernel, cls)), "kernel": cls,
+                "traffic": TRAFFIC_PER_LAUNCH.get((args.kernel, cls, args.precision)) if WIDTH * HEIGHT * spp ==
+                1920 * 1080 * 64 else None, "kernel": cls,
                 "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs), of measured" if peaks else "fallback 6.8 TB/s"}
 

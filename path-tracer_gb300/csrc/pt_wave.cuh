@@ -678,7 +678,12 @@ struct ShadeRange {
 // counts for the next bounce); blocks recount their chunk, reserve each
 // key's range with one global atomic and scatter.  Skipped (cnt[7] = 0)
 // below min_hits.
-constexpr uint32_t kSortBuckets = 4096;
+#ifndef PT_SORT_BUCKETS
+#define PT_SORT_BUCKETS 4096
+#endif
+constexpr uint32_t kSortBuckets = PT_SORT_BUCKETS;  // a multiple of 1024, at most 8192 (shared memory)
+static_assert(kSortBuckets % 1024 == 0 && kSortBuckets <= 8192, "sort buckets: 1024 .. 8192 in steps of 1024");
+constexpr uint32_t kSortPerThread = kSortBuckets / 1024;
 constexpr int kSortThreads = 256, kSortItems = 8;
 
 template <int kMode>
@@ -704,7 +709,7 @@ __global__ void __launch_bounds__(kSortThreads) sort_count_kernel(World w, Queue
         if (hist[i]) atomicAdd(&counts[i], hist[i]);
 }
 
-// one block of 1024 threads, 4 buckets each
+// one block of 1024 threads, kSortPerThread buckets each
 template <int kUnused>
 __global__ void __launch_bounds__(1024) sort_scan_kernel(Queues q, uint32_t* counts, uint32_t* offsets,
                                                           uint32_t min_hits) {
@@ -714,11 +719,11 @@ __global__ void __launch_bounds__(1024) sort_scan_kernel(Queues q, uint32_t* cou
         if (t == 0) q.cnt[7] = 0u;
         return;
     }
-    uint32_t c[4], sum = 0;
+    uint32_t c[kSortPerThread], sum = 0;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        c[k] = counts[4 * t + k];
-        counts[4 * t + k] = 0u;
+    for (uint32_t k = 0; k < kSortPerThread; ++k) {
+        c[k] = counts[kSortPerThread * t + k];
+        counts[kSortPerThread * t + k] = 0u;
         sum += c[k];
     }
     part[t] = sum;
@@ -731,8 +736,8 @@ __global__ void __launch_bounds__(1024) sort_scan_kernel(Queues q, uint32_t* cou
     }
     uint32_t base = part[t] - sum;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        offsets[4 * t + k] = base;
+    for (uint32_t k = 0; k < kSortPerThread; ++k) {
+        offsets[kSortPerThread * t + k] = base;
         base += c[k];
     }
     if (t == 0) q.cnt[7] = 1u;
