@@ -61,6 +61,7 @@ struct pt_ctx {
 
     // world (bind group 1)
     DevBuf geo, attr, mat, nodes, srgb, linear, sky, sky_alias, scene_alias, srgb_lut;
+    DevBuf stage_geo, stage_attr, stage_mat, stage_nodes, stage_srgb, stage_linear;  // next scene upload
     uint64_t tri_count = 0, mat_count = 0, node_count = 0, sky_alias_count = 0, scene_alias_live = 0;
     uint32_t srgb_count = 0, linear_count = 0;
     pt_camera camera{};
@@ -170,6 +171,32 @@ int copy_to(pt_ctx* c, DevBuf& buf, const void* src, size_t bytes, const char* w
 // more than 64 deferred entries (trace.slang:632,786)
 int validate_bvh(pt_ctx* c, const pt_bvh_node* nodes, uint64_t count, uint64_t tris) {
     if (count == 0) return c->fail(PT_ERR_INVALID_ARG, "BVH has no nodes");
+    // one forward pass when every child follows its parent (the reference
+    // builder allocates children after their parent, world.rs:1578-1583): then
+    // the graph is acyclic, and at most one parent per node makes it a tree
+    {
+        std::vector<uint8_t> depth(count, 0), parents(count, 0);
+        bool ordered = true;
+        for (uint64_t i = 0; i < count && ordered; ++i) {
+            const pt_bvh_node& n = nodes[i];
+            if (i > 0 && parents[i] == 0) continue;  // unreachable from the root: ignored, as by the traversal
+            if (n.tri_count > 0) {
+                if ((uint64_t)n.left_first + n.tri_count > tris)
+                    return c->fail(PT_ERR_INVALID_ARG, "BVH leaf triangle range outside the triangle buffer");
+                continue;
+            }
+            const uint64_t l = n.left_first;
+            if (l <= i || l + 1 >= count) {
+                ordered = false;  // out of order or out of range: the general walk below decides
+                break;
+            }
+            if (depth[i] >= 64) return c->fail(PT_ERR_OUT_OF_LIMITS, "BVH deeper than the 64-entry traversal stack");
+            if (parents[l] || parents[l + 1]) return c->fail(PT_ERR_INVALID_ARG, "BVH node reached twice (not a tree)");
+            parents[l] = parents[l + 1] = 1;
+            depth[l] = depth[l + 1] = (uint8_t)(depth[i] + 1);
+        }
+        if (ordered) return PT_OK;
+    }
     std::vector<uint8_t> seen(count, 0);
     std::vector<std::pair<uint64_t, uint32_t>> st{{0, 0}};
     while (!st.empty()) {
@@ -190,6 +217,27 @@ int validate_bvh(pt_ctx* c, const pt_bvh_node* nodes, uint64_t count, uint64_t t
         }
     }
     return PT_OK;
+}
+
+// every triangle's material index below material_count; large scenes are
+// scanned by several host threads
+bool materials_in_range(const pt_triangle_attribute* attrs, uint64_t n, uint64_t materials) {
+    const auto scan = [&](uint64_t lo, uint64_t hi) {
+        for (uint64_t i = lo; i < hi; ++i)
+            if (attrs[i].material_index >= materials) return false;
+        return true;
+    };
+    const unsigned hw = std::thread::hardware_concurrency();
+    const unsigned threads = n < (1u << 18) || hw < 2 ? 1u : (hw < 16 ? hw : 16u);
+    if (threads == 1) return scan(0, n);
+    std::vector<std::thread> pool;
+    std::vector<char> ok(threads, 1);
+    for (unsigned t = 0; t < threads; ++t)
+        pool.emplace_back([&, t] { ok[t] = scan(n * t / threads, n * (t + 1) / threads); });
+    for (auto& th : pool) th.join();
+    for (char v : ok)
+        if (!v) return false;
+    return true;
 }
 
 int validate_lights(pt_ctx* c, const pt_scene_uniforms& s, uint64_t scene_alias_live, uint64_t sky_alias_count,
@@ -223,67 +271,94 @@ int apply(pt_ctx* c, const pt_world_updates* u, bool initial) {
         if (!u->scene_uniforms) return c->fail(PT_ERR_INVALID_ARG, "initial scene uniforms missing");
         if (!u->skybox_uniforms) return c->fail(PT_ERR_INVALID_ARG, "initial skybox uniforms missing");
     }
-    // ---- validate everything before touching device state
-    uint64_t tri = c->tri_count, mats = c->mat_count;
+    // ---- the scene's buffers start copying into staging buffers while the
+    // host validates the update; they replace the live buffers only if every
+    // check passes, so a rejected update leaves the device state untouched
+    bool staged = false;
     if (const pt_scene_upload* s = u->scene) {
-        if (!s->geometries || !s->attributes || !s->materials || !s->bvh_nodes)
-            return c->fail(PT_ERR_INVALID_ARG, "scene upload has a NULL buffer");
-        if (s->triangle_count == 0) return c->fail(PT_ERR_INVALID_ARG, "scene has no triangles");
-        if (s->triangle_count > 0x7fffffffull) return c->fail(PT_ERR_OUT_OF_LIMITS, "too many triangles");
-        if (s->material_count == 0) return c->fail(PT_ERR_INVALID_ARG, "scene has no materials");
-        if ((s->srgb_atlas_count && !s->srgb_texture_atlases) || (s->linear_atlas_count && !s->linear_texture_atlases))
-            return c->fail(PT_ERR_INVALID_ARG, "atlas count without atlas data");
-        for (uint64_t i = 0; i < s->triangle_count; ++i)
-            if (s->attributes[i].material_index >= s->material_count)
-                return c->fail(PT_ERR_INVALID_ARG, "triangle material index outside the material buffer");
-        int rc = validate_bvh(c, s->bvh_nodes, s->node_count, s->triangle_count);
-        if (rc) return rc;
-        tri = s->triangle_count;
-        mats = s->material_count;
+        if (s->geometries && s->attributes && s->materials && s->bvh_nodes && s->triangle_count &&
+            !((s->srgb_atlas_count && !s->srgb_texture_atlases) || (s->linear_atlas_count && !s->linear_texture_atlases))) {
+            const size_t layer = (size_t)PT_ATLAS_SIZE * PT_ATLAS_SIZE * 4;
+            int rc = copy_to(c, c->stage_geo, s->geometries, s->triangle_count * sizeof(pt_triangle_geometry), "geometries");
+            if (!rc) rc = copy_to(c, c->stage_attr, s->attributes, s->triangle_count * sizeof(pt_triangle_attribute), "attributes");
+            if (!rc) rc = copy_to(c, c->stage_mat, s->materials, s->material_count * sizeof(pt_material), "materials");
+            if (!rc) rc = copy_to(c, c->stage_nodes, s->bvh_nodes, s->node_count * sizeof(pt_bvh_node), "BVH");
+            if (!rc) rc = copy_to(c, c->stage_srgb, s->srgb_texture_atlases, s->srgb_atlas_count * layer, "sRGB atlases");
+            if (!rc) rc = copy_to(c, c->stage_linear, s->linear_texture_atlases, s->linear_atlas_count * layer, "linear atlases");
+            if (rc) {
+                cudaStreamSynchronize(c->stream);  // copies already issued still read the caller's memory
+                return rc;
+            }
+            staged = true;
+        }
     }
-    for (uint64_t i = 0; i < u->material_update_count; ++i)
-        if (!u->materials || u->materials[i].index >= mats)
-            return c->fail(PT_ERR_INVALID_ARG, "material update index outside the material buffer");
+    // ---- validate everything before touching the live device state
+    uint64_t tri = c->tri_count, mats = c->mat_count;
     pt_skybox_uniforms sky = u->skybox_uniforms ? *u->skybox_uniforms : c->sky_u;
     uint64_t sky_alias_count = c->sky_alias_count;
-    if (const pt_skybox_upload* k = u->skybox) {
-        if (!k->rgba) return c->fail(PT_ERR_INVALID_ARG, "skybox upload has no pixels");
-        if (k->uniforms.width == 0 || k->uniforms.height == 0 || (uint64_t)k->uniforms.width * k->uniforms.height > 0xffffffffull)
-            return c->fail(PT_ERR_OUT_OF_LIMITS, "skybox dimensions out of range");
-        if (k->alias_count && k->alias_count != (uint64_t)k->uniforms.width * k->uniforms.height)
-            return c->fail(PT_ERR_INVALID_ARG, "skybox alias table size does not match the skybox");
-        if (!u->skybox_uniforms) sky = k->uniforms;
-        sky_alias_count = k->alias_count;
-        for (uint64_t i = 0; i < k->alias_count; ++i)
-            if (k->alias_table[i].alias_index >= k->alias_count)
-                return c->fail(PT_ERR_INVALID_ARG, "skybox alias index out of range");
-    }
-    if (u->skybox_uniforms && !u->skybox && (u->skybox_uniforms->width != c->sky_u.width || u->skybox_uniforms->height != c->sky_u.height))
-        return c->fail(PT_ERR_INVALID_ARG, "skybox uniforms change the size of the uploaded skybox");
     uint64_t live = u->scene ? 0 : c->scene_alias_live;
-    if (u->scene_alias_table) {
-        if (u->scene_alias_count > tri)
-            return c->fail(PT_ERR_OUT_OF_LIMITS, "scene alias table larger than the triangle count");
-        for (uint64_t i = 0; i < u->scene_alias_count; ++i) {
-            const pt_scene_alias_entry& e = u->scene_alias_table[i];
-            if (e.triangle_index >= tri || e.alias_index >= u->scene_alias_count)
-                return c->fail(PT_ERR_INVALID_ARG, "scene alias entry out of range");
+    const auto validate = [&]() -> int {
+        if (const pt_scene_upload* s = u->scene) {
+            if (!s->geometries || !s->attributes || !s->materials || !s->bvh_nodes)
+                return c->fail(PT_ERR_INVALID_ARG, "scene upload has a NULL buffer");
+            if (s->triangle_count == 0) return c->fail(PT_ERR_INVALID_ARG, "scene has no triangles");
+            if (s->triangle_count > 0x7fffffffull) return c->fail(PT_ERR_OUT_OF_LIMITS, "too many triangles");
+            if (s->material_count == 0) return c->fail(PT_ERR_INVALID_ARG, "scene has no materials");
+            if ((s->srgb_atlas_count && !s->srgb_texture_atlases) || (s->linear_atlas_count && !s->linear_texture_atlases))
+                return c->fail(PT_ERR_INVALID_ARG, "atlas count without atlas data");
+            if (!materials_in_range(s->attributes, s->triangle_count, s->material_count))
+                return c->fail(PT_ERR_INVALID_ARG, "triangle material index outside the material buffer");
+            int rc = validate_bvh(c, s->bvh_nodes, s->node_count, s->triangle_count);
+            if (rc) return rc;
+            tri = s->triangle_count;
+            mats = s->material_count;
         }
-        live = u->scene_alias_count;
+        for (uint64_t i = 0; i < u->material_update_count; ++i)
+            if (!u->materials || u->materials[i].index >= mats)
+                return c->fail(PT_ERR_INVALID_ARG, "material update index outside the material buffer");
+        if (const pt_skybox_upload* k = u->skybox) {
+            if (!k->rgba) return c->fail(PT_ERR_INVALID_ARG, "skybox upload has no pixels");
+            if (k->uniforms.width == 0 || k->uniforms.height == 0 || (uint64_t)k->uniforms.width * k->uniforms.height > 0xffffffffull)
+                return c->fail(PT_ERR_OUT_OF_LIMITS, "skybox dimensions out of range");
+            if (k->alias_count && k->alias_count != (uint64_t)k->uniforms.width * k->uniforms.height)
+                return c->fail(PT_ERR_INVALID_ARG, "skybox alias table size does not match the skybox");
+            if (!u->skybox_uniforms) sky = k->uniforms;
+            sky_alias_count = k->alias_count;
+            for (uint64_t i = 0; i < k->alias_count; ++i)
+                if (k->alias_table[i].alias_index >= k->alias_count)
+                    return c->fail(PT_ERR_INVALID_ARG, "skybox alias index out of range");
+        }
+        if (u->skybox_uniforms && !u->skybox && (u->skybox_uniforms->width != c->sky_u.width || u->skybox_uniforms->height != c->sky_u.height))
+            return c->fail(PT_ERR_INVALID_ARG, "skybox uniforms change the size of the uploaded skybox");
+        if (u->scene_alias_table) {
+            if (u->scene_alias_count > tri)
+                return c->fail(PT_ERR_OUT_OF_LIMITS, "scene alias table larger than the triangle count");
+            for (uint64_t i = 0; i < u->scene_alias_count; ++i) {
+                const pt_scene_alias_entry& e = u->scene_alias_table[i];
+                if (e.triangle_index >= tri || e.alias_index >= u->scene_alias_count)
+                    return c->fail(PT_ERR_INVALID_ARG, "scene alias entry out of range");
+            }
+            live = u->scene_alias_count;
+        }
+        const pt_scene_uniforms scene = u->scene_uniforms ? *u->scene_uniforms : c->scene;
+        return validate_lights(c, scene, live, sky_alias_count, sky);
+    };
+    int rc = validate();
+    if (rc) {
+        if (staged) cudaStreamSynchronize(c->stream);
+        return rc;
     }
-    const pt_scene_uniforms scene = u->scene_uniforms ? *u->scene_uniforms : c->scene;
-    int rc = validate_lights(c, scene, live, sky_alias_count, sky);
-    if (rc) return rc;
 
     // ---- upload
     if (const pt_scene_upload* s = u->scene) {
-        const size_t layer = (size_t)PT_ATLAS_SIZE * PT_ATLAS_SIZE * 4;
-        if ((rc = copy_to(c, c->geo, s->geometries, s->triangle_count * sizeof(pt_triangle_geometry), "geometries"))) return rc;
-        if ((rc = copy_to(c, c->attr, s->attributes, s->triangle_count * sizeof(pt_triangle_attribute), "attributes"))) return rc;
-        if ((rc = copy_to(c, c->mat, s->materials, s->material_count * sizeof(pt_material), "materials"))) return rc;
-        if ((rc = copy_to(c, c->nodes, s->bvh_nodes, s->node_count * sizeof(pt_bvh_node), "BVH"))) return rc;
-        if ((rc = copy_to(c, c->srgb, s->srgb_texture_atlases, s->srgb_atlas_count * layer, "sRGB atlases"))) return rc;
-        if ((rc = copy_to(c, c->linear, s->linear_texture_atlases, s->linear_atlas_count * layer, "linear atlases"))) return rc;
+        // the validated staging buffers become the live ones (stream order keeps
+        // earlier traces on the previous buffers)
+        std::swap(c->geo, c->stage_geo);
+        std::swap(c->attr, c->stage_attr);
+        std::swap(c->mat, c->stage_mat);
+        std::swap(c->nodes, c->stage_nodes);
+        std::swap(c->srgb, c->stage_srgb);
+        std::swap(c->linear, c->stage_linear);
         // the alias buffer holds every triangle (world_resources.rs:158-165)
         if ((rc = c->cuda(c->scene_alias.reserve(s->triangle_count * sizeof(pt_scene_alias_entry)), "scene aliases"))) return rc;
         c->tri_count = s->triangle_count;
@@ -469,7 +544,8 @@ void pt_destroy(pt_ctx* c) {
     for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
     if (c->wavefront) ptw::destroy(c->wavefront);
     for (DevBuf* b : {&c->geo, &c->attr, &c->mat, &c->nodes, &c->srgb, &c->linear, &c->sky, &c->sky_alias,
-                      &c->scene_alias, &c->srgb_lut, &c->accum, &c->image, &c->comp, &c->display, &c->records, &c->totals})
+                      &c->scene_alias, &c->srgb_lut, &c->accum, &c->image, &c->comp, &c->display, &c->records, &c->totals,
+                      &c->stage_geo, &c->stage_attr, &c->stage_mat, &c->stage_nodes, &c->stage_srgb, &c->stage_linear})
         b->release();
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;

@@ -221,6 +221,9 @@ def main(argv=None) -> None:
     p.add_argument("--precision", choices=["fp32", "wide", "compressed"], default="fp32",
                    help="engine form: the reference's FP32 buffers, the 8-wide BVH, or the compressed form "
                         "(8-wide BVH + FP16 attributes / BF16 skybox + Kahan sums)")
+    p.add_argument("--autotune", action="store_true",
+                   help="with --compare: let the engine's autotuner pick wave size, tile size, refill steps and the "
+                        "hit-sort threshold on 16 of the requests first")
     p.add_argument("--compare", type=int, default=0,
                    help="instead of serving: render this many requests of the mix back to back with the plain "
                         "kernel, the wavefront kernel (one job per call) and the batched engine")
@@ -238,6 +241,12 @@ def main(argv=None) -> None:
         reqs = request_stream(1000.0, args.compare / 1000.0 * 2.0 + 1.0, names, args.seed, 0.0, fixed)[:args.compare]
         out = {"requests": len(reqs), "engine_precision": args.precision,
                "triangles": {n: worlds[n].triangle_count() for n in names}}
+        if args.autotune:
+            sample = [abi.JobDesc(server.scene_ids[r.scene], server.camera(r.scene, r), r.width, r.height, r.samples,
+                                  r.max_bounces, 0) for r in reqs[:16]]
+            t = time.perf_counter()
+            out["autotuned"] = eng.autotune(sample)
+            out["autotune_s"] = time.perf_counter() - t
         for mode in ("engine", "wavefront", "plain"):
             out[mode] = closed_loop(server, reqs, mode)
         out["engine_over_plain"] = out["engine"]["samples_per_s"] / out["plain"]["samples_per_s"]

@@ -95,9 +95,19 @@ def test_malformed_bvh_rejected_on_host(cornell, field, value):
     with pytest.raises(pt.PathTracerError):
         pt.PathTracer(bad, (8, 8))
     tr = pt.PathTracer(updates, (8, 8))
+    tr.set_tile((256, 256), (120, 120), (8, 8))
+    tr.trace(2)
+    want = tr.read_tile(abi.PT_TILE_ACCUMULATION)
     with pytest.raises(pt.PathTracerError):
         tr.apply_updates(bad)
-    tr.trace(1)  # the context still works after the rejection
+    # the rejected upload was staged, never made live: the same world renders the same bits
+    tr.set_tile((256, 256), (120, 120), (8, 8))
+    tr.trace(2)
+    np.testing.assert_array_equal(tr.read_tile(abi.PT_TILE_ACCUMULATION).view(np.uint32), want.view(np.uint32))
+    tr.apply_updates(updates)  # a valid full upload after a rejected one
+    tr.set_tile((256, 256), (120, 120), (8, 8))
+    tr.trace(2)
+    np.testing.assert_array_equal(tr.read_tile(abi.PT_TILE_ACCUMULATION).view(np.uint32), want.view(np.uint32))
     tr.close()
 
 

@@ -202,3 +202,25 @@ def test_textured_cornell_tile_bit_exact(kernel):
     _, ref = oracle.trace_paths(ow, (256, 256), 8, px, 1, 4, records=True)
     assert_records_equal(gpu, ref)
     tr.close()
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_large_scene_fp64_rmse(large_world, kernel):
+    """Config 2: relative RMSE of a 48x48 crop at 64 spp against the FP64 oracle render (same RNG streams)."""
+    w, u, ow = large_world
+    origin, size, spp = (900, 500), (48, 48), 64
+    tr = pt.PathTracer(u, size)
+    tr.set_kernel(kernel)
+    tr.set_max_bounces(8)
+    tr.set_tile((1920, 1080), origin, size)
+    done = 0
+    while done < spp:
+        done += tr.trace(spp - done)
+    acc = tr.read_tile(abi.PT_TILE_ACCUMULATION)[..., :3].astype(np.float64) / spp
+    px = pixels_of(origin, size, (1920, 1080))
+    rad64, _ = oracle.trace_paths(ow, (1920, 1080), 8, px, 1, spp, precision=64)
+    ref = rad64.mean(axis=0).reshape(size[1], size[0], 3)
+    rel_rmse = np.sqrt(np.mean((acc - ref) ** 2)) / np.sqrt(np.mean(ref ** 2))
+    print(f"config 2 relative RMSE vs FP64 oracle ({spp} spp, 48x48 crop, kernel {kernel}): {rel_rmse:.3e}")
+    assert rel_rmse < 1e-2
+    tr.close()
