@@ -75,6 +75,20 @@ int ptw_build(ptw_world* world);
  * 1x1 skybox.  Without a call the skybox is black. */
 int ptw_set_skybox_rgba(ptw_world* world, const float* rgba, uint32_t width, uint32_t height);
 
+/* Skybox::new on an image file (the reference decodes its skybox asset with
+ * an image library, world.rs:1872-1880): Radiance RGBE (.hdr, "-Y H +X W")
+ * or single-part scanline OpenEXR (HALF/FLOAT/UINT channels R, G, B [, A] or
+ * Y; compression NONE, RLE, ZIPS, ZIP or PIZ), chosen by the file's magic
+ * bytes.  On failure `error` (if given) receives the reason and the skybox is
+ * unchanged. */
+int ptw_set_skybox_file(ptw_world* world, const char* path, char* error, size_t error_size);
+
+/* Decodes the same image files to linear RGBA32F, row 0 at the top.  With
+ * rgba == NULL only *width and *height are set; otherwise rgba must hold
+ * capacity >= width * height * 4 floats (PT_ERR_OUT_OF_LIMITS if not). */
+int ptw_read_image_rgba(const char* path, float* rgba, uint64_t capacity, uint32_t* width, uint32_t* height,
+                        char* error, size_t error_size);
+
 /* the procedural sky of the large scene (vertical gradient plus a Gaussian
  * sun lobe), width x height, passed through ptw_set_skybox_rgba */
 int ptw_set_procedural_skybox(ptw_world* world, uint32_t width, uint32_t height);

@@ -124,114 +124,6 @@ Options parse(int argc, char** argv) {
     return o;
 }
 
-// Radiance RGBE (.hdr) reader: "#?RADIANCE"/"#?RGBE" header, FORMAT=32-bit_rle_rgbe,
-// "-Y H +X W" resolution, new-style run-length scanlines or flat pixels.
-bool read_hdr(const std::string& path, std::vector<float>& rgba, uint32_t& w, uint32_t& h, std::string& err) {
-    FILE* f = fopen(path.c_str(), "rb");
-    if (!f) {
-        err = "cannot read skybox " + path + ": " + strerror(errno);
-        return false;
-    }
-    std::vector<uint8_t> data;
-    uint8_t buf[1 << 16];
-    size_t n;
-    while ((n = fread(buf, 1, sizeof buf, f)) > 0) data.insert(data.end(), buf, buf + n);
-    fclose(f);
-    size_t pos = 0;
-    auto line = [&]() {
-        std::string s;
-        while (pos < data.size() && data[pos] != '\n') s.push_back((char)data[pos++]);
-        if (pos < data.size()) pos++;
-        return s;
-    };
-    const std::string magic = line();
-    if (magic.rfind("#?", 0) != 0) {
-        err = "not a Radiance HDR file";
-        return false;
-    }
-    for (;;) {
-        if (pos >= data.size()) {
-            err = "truncated HDR header";
-            return false;
-        }
-        const std::string s = line();
-        if (s.empty()) break;
-        if (s.rfind("FORMAT=", 0) == 0 && s != "FORMAT=32-bit_rle_rgbe") {
-            err = "unsupported HDR format " + s;
-            return false;
-        }
-    }
-    const std::string res = line();
-    int hh = 0, ww = 0;
-    if (sscanf(res.c_str(), "-Y %d +X %d", &hh, &ww) != 2 || hh <= 0 || ww <= 0) {
-        err = "unsupported HDR orientation: " + res;
-        return false;
-    }
-    w = (uint32_t)ww;
-    h = (uint32_t)hh;
-    rgba.assign((size_t)w * h * 4, 0.0f);
-    std::vector<uint8_t> scan((size_t)w * 4);
-    for (uint32_t y = 0; y < h; ++y) {
-        if (pos + 4 > data.size()) {
-            err = "truncated HDR data";
-            return false;
-        }
-        if (w >= 8 && w < 32768 && data[pos] == 2 && data[pos + 1] == 2 && !(data[pos + 2] & 0x80)) {
-            if ((uint32_t)((data[pos + 2] << 8) | data[pos + 3]) != w) {
-                err = "bad HDR scanline";
-                return false;
-            }
-            pos += 4;
-            for (int c = 0; c < 4; ++c) {
-                uint32_t x = 0;
-                while (x < w) {
-                    if (pos >= data.size()) {
-                        err = "truncated HDR data";
-                        return false;
-                    }
-                    uint32_t count = data[pos++];
-                    if (count > 128) {
-                        count -= 128;
-                        if (pos >= data.size() || x + count > w) {
-                            err = "bad HDR run";
-                            return false;
-                        }
-                        const uint8_t v = data[pos++];
-                        for (uint32_t k = 0; k < count; ++k) scan[(x++) * 4 + c] = v;
-                    } else {
-                        if (count == 0 || pos + count > data.size() || x + count > w) {
-                            err = "bad HDR run";
-                            return false;
-                        }
-                        for (uint32_t k = 0; k < count; ++k) scan[(x++) * 4 + c] = data[pos++];
-                    }
-                }
-            }
-        } else {
-            if (pos + (size_t)w * 4 > data.size()) {
-                err = "truncated HDR data";
-                return false;
-            }
-            memcpy(scan.data(), &data[pos], (size_t)w * 4);
-            pos += (size_t)w * 4;
-        }
-        for (uint32_t x = 0; x < w; ++x) {
-            const uint8_t* p = &scan[x * 4];
-            float* o = &rgba[((size_t)y * w + x) * 4];
-            if (p[3] == 0) {
-                o[0] = o[1] = o[2] = 0.0f;
-            } else {
-                const float scale = std::ldexp(1.0f, (int)p[3] - 136);
-                o[0] = (float)p[0] * scale;
-                o[1] = (float)p[1] * scale;
-                o[2] = (float)p[2] * scale;
-            }
-            o[3] = 1.0f;
-        }
-    }
-    return true;
-}
-
 uint32_t crc32(const uint8_t* d, size_t n, uint32_t c = 0xffffffffu) {
     static uint32_t table[256];
     static bool init = false;
@@ -352,10 +244,14 @@ int main(int argc, char** argv) {
     if (opt.skybox == "procedural") {
         rc = ptw_set_procedural_skybox(world, 1024, 512);
     } else if (opt.skybox != "black") {
-        std::vector<float> px;
+        // .hdr or .exr, decoded by the library
         uint32_t w = 0, h = 0;
-        std::string err;
-        if (!read_hdr(opt.skybox, px, w, h, err)) return fail("skybox", err);
+        char err[512] = {0};
+        if (ptw_read_image_rgba(opt.skybox.c_str(), nullptr, 0, &w, &h, err, sizeof err))
+            return fail("skybox", "cannot read skybox " + opt.skybox + ": " + err);
+        std::vector<float> px((size_t)w * h * 4);
+        if (ptw_read_image_rgba(opt.skybox.c_str(), px.data(), px.size(), &w, &h, err, sizeof err))
+            return fail("skybox", "cannot read skybox " + opt.skybox + ": " + err);
         if (w / 2 != h) fprintf(stderr, "Skybox image should usually have 2:1 aspect ratio, but is %ux%u\n", w, h);
         rc = ptw_set_skybox_rgba(world, px.data(), w, h);
     }

@@ -150,6 +150,13 @@ class World:
         h, w = a.shape[0], a.shape[1]
         self._check(self._lib.ptw_set_skybox_rgba(self._h, a.ctypes.data, w, h))
 
+    def set_skybox_file(self, path) -> None:
+        """Skybox from a Radiance .hdr or OpenEXR .exr file (the reference's skybox assets)."""
+        err = C.create_string_buffer(512)
+        rc = self._lib.ptw_set_skybox_file(self._h, str(path).encode(), err, len(err))
+        if rc != abi.PT_OK:
+            raise PathTracerError(rc, f"skybox {path}: {err.value.decode()}")
+
     def edit_skybox_average_luminance(self, luminance: float) -> None:
         self._check(self._lib.ptw_edit_skybox_average_luminance(self._h, luminance))
 
@@ -253,6 +260,21 @@ def half_attributes(attributes: np.ndarray) -> np.ndarray:
     out = np.zeros(n * 64, dtype=np.uint8)
     load().pt_half_attributes(a.ctypes.data_as(C.POINTER(abi.TriangleAttribute)), n, out.ctypes.data)
     return out.reshape(n, 64)
+
+
+def read_image(path) -> np.ndarray:
+    """A Radiance .hdr or OpenEXR .exr file as (height, width, 4) float32 linear RGBA."""
+    lib = load()
+    err = C.create_string_buffer(512)
+    w, h = C.c_uint32(), C.c_uint32()
+    rc = lib.ptw_read_image_rgba(str(path).encode(), None, 0, C.byref(w), C.byref(h), err, len(err))
+    if rc != abi.PT_OK:
+        raise PathTracerError(rc, f"{path}: {err.value.decode()}")
+    out = np.empty((h.value, w.value, 4), np.float32)
+    rc = lib.ptw_read_image_rgba(str(path).encode(), out.ctypes.data, out.size, C.byref(w), C.byref(h), err, len(err))
+    if rc != abi.PT_OK:
+        raise PathTracerError(rc, f"{path}: {err.value.decode()}")
+    return out
 
 
 def build_bvh(triangles: np.ndarray):
