@@ -33,6 +33,20 @@ sys.path[:0] = [str(ROOT), str(ROOT / "path-tracer_gb300")]
 import numpy as np  # noqa: E402
 
 WIDTH, HEIGHT, SPP, MAX_BOUNCES = 1920, 1080, 64, 8
+# the large procedural scene is the bench line; the 36-triangle Cornell room
+# (256x256, 16 spp) is the small plain-method case, measured with --workload cornell
+WORKLOADS = {
+    "procedural": {"image": (1920, 1080), "spp": 64,
+                   "text": "procedural scene (1024x512-quad heightfield + 2000 boxes + 200 icospheres s4 + 64 "
+                           "emissive triangles, 1024x512 sky)",
+                   "l2": "inputs larger than L2 (scene buffers ~440 MB vs 129 MB L2), no flush"},
+    "cornell": {"image": (256, 256), "spp": 16,
+                "text": "Cornell room (36 triangles: 5 wall quads, two rotated boxes, 0.25x0.25 emissive ceiling quad; "
+                        "black sky)",
+                "l2": "scene (~4 KB) resident in L1/L2 by nature; no flush (the case is bound by arithmetic, "
+                      "not memory)"},
+}
+WORKLOAD = "procedural"
 METRIC = "Mrays/s"
 KERNEL_NAMES = {"wavefront": 0, "plain": 1}
 # include/pt_precision.h: FP32 (the reference's buffers), 8-wide quantised BVH only, or the full
@@ -56,7 +70,9 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--spp", type=int, default=SPP, help="samples per pixel of one step")
+    p.add_argument("--workload", choices=list(WORKLOADS), default="procedural",
+                   help="procedural: the large scene of the bench line; cornell: the 36-triangle room")
+    p.add_argument("--spp", type=int, default=None, help="samples per pixel of one step (default: the workload's)")
     p.add_argument("--profile-run", action="store_true",
                    help="only the timed steps (no counting pass, e2e or CPU baseline): for ncu captures")
     p.add_argument("--no-latency", action="store_true",
@@ -64,9 +80,10 @@ def parse_args():
     p.add_argument("--image", type=int, nargs=2, metavar=("W", "H"), default=None,
                    help="image size (default 1920 1080); smaller sizes are for ncu captures, not bench lines")
     args = p.parse_args()
-    if args.image:
-        global WIDTH, HEIGHT
-        WIDTH, HEIGHT = args.image
+    global WIDTH, HEIGHT, SPP, WORKLOAD
+    WORKLOAD = args.workload
+    WIDTH, HEIGHT = args.image or WORKLOADS[WORKLOAD]["image"]
+    SPP = args.spp = args.spp or WORKLOADS[WORKLOAD]["spp"]
     return args
 
 
@@ -76,22 +93,21 @@ def dist_env():
 
 def workload_config(world, kernel: str) -> dict:
     return {
-        "workload": "procedural scene (1024x512-quad heightfield + 2000 boxes + 200 icospheres s4 + 64 emissive "
-                    f"triangles, 1024x512 sky), {WIDTH}x{HEIGHT}, {SPP} spp, max_bounces 8, one image per step",
+        "workload": f"{WORKLOADS[WORKLOAD]['text']}, {WIDTH}x{HEIGHT}, {SPP} spp, max_bounces 8, one image per step",
         "triangles": int(world.triangle_count()),
         "bvh_nodes": int(world.node_count()),
         "image": [WIDTH, HEIGHT],
         "spp": SPP,
         "max_bounces": MAX_BOUNCES,
         "kernel": kernel,
-        "l2": "inputs larger than L2 (scene buffers ~440 MB vs 129 MB L2), no flush",
-        "seed": 1,
+        "l2": WORKLOADS[WORKLOAD]["l2"],
+        "seed": 1 if WORKLOAD == "procedural" else 0,
     }
 
 
 def build_world():
     import pathtracer as pt
-    world = pt.World.procedural()
+    world = pt.World.procedural() if WORKLOAD == "procedural" else pt.World.cornell_box()
     world.set_aspect_ratio(WIDTH / HEIGHT)
     return world, world.take_updates()
 
@@ -279,10 +295,10 @@ def oracle_sample(updates, seconds: float, threads: int = 0):
         rays = int(rec["extend_rays"].sum() + rec["shadow_rays"].sum())
         return rays, dt, px.shape[0]
 
-    rays, dt, _ = run(64, 4)  # calibration
+    rays, dt, n_cal = run(max(1, int(math.sqrt(WIDTH * HEIGHT / 4096))), 4)  # calibration on ~4096 pixels
     rate = rays / max(dt, 1e-6)
     want_rays = rate * seconds
-    rays_per_px = rays / max(1, (HEIGHT // 64 + 1) * (WIDTH // 64 + 1) * 4) * SPP
+    rays_per_px = rays / max(1, n_cal * 4) * SPP
     n_px = max(64, int(want_rays / max(rays_per_px, 1.0)))
     stride = max(1, int(math.sqrt(WIDTH * HEIGHT / n_px)))
     rays, dt, npx = run(stride, SPP)
@@ -447,6 +463,9 @@ def run_ours(args):
             "config": dict(workload_config(world, args.kernel), precision=args.precision,
                            parallelism=f"replicas x{world_size}"),
             "rays_per_step": rays_per_step, "samples_per_s": paths_per_step * args.steps * world_size / (elapsed_ms / 1e3),
+            # whole-pass algorithmic bytes per ray and the Mrays/s they would allow at the HBM peak
+            "bytes_per_ray": bytes_per_step["total"] / rays_per_step,
+            "hbm_roofline_mrays": peak * 1e9 / (bytes_per_step["total"] / rays_per_step) / 1e6,
             "roofline": roofline, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": WIDTH * HEIGHT * 4},

@@ -8,8 +8,10 @@
  * (world.rs:1691-1735), skybox normalisation, alias table and flux
  * (world.rs:1872-1987), light category probabilities (world.rs:484-498), the
  * auto camera and GpuCamera (world.rs:2159-2193), and World::take_updates
- * (world.rs:790-884).  glTF import is replaced by meshes handed over in memory
- * (ptw_add_mesh) and by the procedural scene generators below.
+ * (world.rs:790-884).  Scenes come from a glTF file (ptw_load_gltf, with its
+ * texture images packed into atlas layers), from meshes handed over in memory
+ * (ptw_add_mesh) or from the procedural scene generators below; skyboxes from
+ * .hdr / .exr files or pixels.
  *
  * All functions return PT_OK or an error code from pt.h; ptw_last_error
  * gives the message.
@@ -60,9 +62,13 @@ int ptw_add_atlas_layer(ptw_world* world, int srgb, const uint8_t* rgba8, int32_
 /* glTF 2.0 import (.glb, or .gltf with external or base64 buffers): adds the
  * default scene's triangle primitives and their materials, walking the node
  * tree as the reference's Scene::new does (world.rs:1078-1337; materials
- * world.rs:1992-2155).  Call before ptw_build.  Textured materials are
- * refused (the import decodes no images).  On failure `error` (if given)
- * receives the reason. */
+ * world.rs:1992-2155).  Every image of the file (PNG or JPEG; buffer view,
+ * data URI or file) is decoded as ptw_decode_texture_rgba8 does and packed
+ * into new 8192^2 atlas layers, sRGB for images that a material uses as base
+ * colour, emission or specular colour, linear otherwise (world.rs:893-1076);
+ * material texture slots get the layer and the UV offset/scale of their
+ * image.  Call before ptw_build.  On failure `error` (if given) receives the
+ * reason. */
 int ptw_load_gltf(ptw_world* world, const char* path, char* error, size_t error_size);
 
 /* Builds the BVH over all added meshes, reorders triangles to BVH order and
@@ -88,6 +94,15 @@ int ptw_set_skybox_file(ptw_world* world, const char* path, char* error, size_t 
  * capacity >= width * height * 4 floats (PT_ERR_OUT_OF_LIMITS if not). */
 int ptw_read_image_rgba(const char* path, float* rgba, uint64_t capacity, uint32_t* width, uint32_t* height,
                         char* error, size_t error_size);
+
+/* Decodes a glTF texture image (PNG, or baseline / extended / progressive
+ * Huffman JPEG) held in memory to RGBA8 with the importer's format rules
+ * (world.rs:949-1011): grey -> (l, l, l, 255), grey + alpha -> (l, a, 0, 255),
+ * RGB -> (r, g, b, 255), 16-bit samples -> their high byte.  Images larger
+ * than PT_ATLAS_SIZE on a side are refused.  With rgba == NULL only *width
+ * and *height are set; otherwise rgba must hold width * height * 4 bytes. */
+int ptw_decode_texture_rgba8(const void* bytes, size_t size, uint8_t* rgba, uint64_t capacity, uint32_t* width,
+                             uint32_t* height, char* error, size_t error_size);
 
 /* the procedural sky of the large scene (vertical gradient plus a Gaussian
  * sun lobe), width x height, passed through ptw_set_skybox_rgba */

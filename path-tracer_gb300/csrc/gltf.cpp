@@ -10,19 +10,31 @@
 // KHR_materials_specular, alpha mode and cutoff, OpenPBR_* extras).  Per
 // primitive the positions are transformed by the node matrix, normals by its
 // inverse transpose and tangents by the matrix; ptw_add_mesh then applies
-// the reference's normalisation and tangent rules.  Textured materials are
-// refused: the reference decodes PNG/JPEG images into its atlases, which
-// this import does not do.
+// the reference's normalisation and tangent rules.  Texture images (PNG or
+// JPEG, from data URIs, files or buffer views) are decoded, converted to RGBA8
+// by the reference's format rules and packed into 8192^2 sRGB or linear atlas
+// layers (world.rs:890-1076); each material slot gets its layer and UV
+// offset/scale in the atlas.
+#include <algorithm>
+#include <atomic>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
 #include <map>
 #include <memory>
+#include <set>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/pt_world.h"
+
+namespace ptimg {
+bool decode_texture_rgba8(const uint8_t* bytes, size_t size, std::vector<uint8_t>& rgba, uint32_t& width,
+                          uint32_t& height, std::string& error, uint32_t max_side);
+}
 
 namespace {
 
@@ -281,12 +293,58 @@ void normal_matrix(const M4& a, double n[9]) {
 }
 
 // ------------------------------------------------------------------ glTF
+// Guillotine packer for one atlas layer: a list of free rectangles; an image
+// takes the free rectangle it fits with the shortest leftover side (ties: the
+// shorter longer side), and the remainder is cut along its shorter leftover
+// side into two free rectangles.
+struct AtlasPacker {
+    struct Rect {
+        int x, y, w, h;
+    };
+    std::vector<Rect> free{{0, 0, (int)PT_ATLAS_SIZE, (int)PT_ATLAS_SIZE}};
+    bool place(int w, int h, int& x, int& y) {
+        long best = -1, best_short = LONG_MAX, best_long = LONG_MAX;
+        for (size_t i = 0; i < free.size(); ++i) {
+            const Rect& f = free[i];
+            if (w > f.w || h > f.h) continue;
+            const long a = f.w - w, b = f.h - h, sh = std::min(a, b), lo = std::max(a, b);
+            if (sh < best_short || (sh == best_short && lo < best_long)) {
+                best = (long)i;
+                best_short = sh;
+                best_long = lo;
+            }
+        }
+        if (best < 0) return false;
+        const Rect f = free[(size_t)best];
+        free.erase(free.begin() + best);
+        x = f.x;
+        y = f.y;
+        Rect right, below;
+        if (f.w - w < f.h - h) {
+            right = {f.x + w, f.y, f.w - w, h};
+            below = {f.x, f.y + h, f.w, f.h - h};
+        } else {
+            right = {f.x + w, f.y, f.w - w, f.h};
+            below = {f.x, f.y + h, w, f.h - h};
+        }
+        if (right.w > 0 && right.h > 0) free.push_back(right);
+        if (below.w > 0 && below.h > 0) free.push_back(below);
+        return true;
+    }
+};
+
+struct AtlasSlot {
+    int32_t layer = -1;
+    float uv[4] = {0, 0, 0, 0};  // offset x, y, scale x, y
+};
+
 struct Loader {
     ptw_world* world;
     std::string dir;
     Json doc;
     std::vector<std::vector<uint8_t>> buffers;
     std::map<long, uint32_t> material_cache;  // glTF material index -> world material
+    std::map<long, AtlasSlot> srgb_slots, linear_slots;  // image index -> atlas placement
     std::string error;
 
     bool fail(const std::string& msg) {
@@ -500,6 +558,128 @@ struct Loader {
 
     bool has_texture(const Json* t) const { return t && t->kind == Json::Object; }
 
+    // textureInfo -> textures[index].source (the image index), -1 without one
+    long texture_image(const Json* info) const {
+        if (!has_texture(info)) return -1;
+        const Json* textures = doc.get("textures");
+        const long ti = info->integer("index", -1);
+        if (!textures || ti < 0 || (size_t)ti >= textures->arr.size()) return -1;
+        return textures->arr[(size_t)ti].integer("source", -1);
+    }
+
+    // the encoded bytes of image i: a data URI, a file beside the glTF, or a buffer view
+    bool image_bytes(size_t i, std::vector<uint8_t>& out) {
+        const Json& im = doc.get("images")->arr[i];
+        if (const Json* uri = im.get("uri")) {
+            if (uri->str.rfind("data:", 0) == 0) {
+                const size_t comma = uri->str.find(',');
+                if (comma == std::string::npos || uri->str.find(";base64") == std::string::npos ||
+                    !base64(uri->str.substr(comma + 1), out))
+                    return fail("unsupported data URI in image " + std::to_string(i));
+                return true;
+            }
+            if (!read_file(dir + uri->str, out)) return fail("cannot read image " + uri->str);
+            return true;
+        }
+        const Json* views = doc.get("bufferViews");
+        const long vi = im.integer("bufferView", -1);
+        if (!views || vi < 0 || (size_t)vi >= views->arr.size()) return fail("image without uri or buffer view");
+        const Json& v = views->arr[(size_t)vi];
+        const long b = v.integer("buffer", -1), off = v.integer("byteOffset", 0), len = v.integer("byteLength", 0);
+        if (b < 0 || (size_t)b >= buffers.size() || off < 0 || len < 0 || (size_t)(off + len) > buffers[(size_t)b].size())
+            return fail("image buffer view out of range");
+        out.assign(buffers[(size_t)b].begin() + off, buffers[(size_t)b].begin() + off + len);
+        return true;
+    }
+
+    // world.rs:893-1076: every image of the file decoded to RGBA8 and packed,
+    // in image order, into sRGB atlas layers if any material uses it as a base
+    // colour, emission or specular colour texture, else into linear layers;
+    // a new layer is opened when an image fits in none of the open ones
+    bool images() {
+        const Json* imgs = doc.get("images");
+        if (!imgs || imgs->arr.empty()) return true;
+        std::set<long> srgb;
+        if (const Json* mats = doc.get("materials"))
+            for (const Json& m : mats->arr) {
+                if (const Json* pbr = m.get("pbrMetallicRoughness")) srgb.insert(texture_image(pbr->get("baseColorTexture")));
+                srgb.insert(texture_image(m.get("emissiveTexture")));
+                if (const Json* ext = m.get("extensions"))
+                    if (const Json* sp = ext->get("KHR_materials_specular"))
+                        srgb.insert(texture_image(sp->get("specularColorTexture")));
+            }
+        const size_t n = imgs->arr.size();
+        std::vector<std::vector<uint8_t>> encoded(n), rgba(n);
+        std::vector<uint32_t> w(n), h(n);
+        for (size_t i = 0; i < n; ++i)
+            if (!image_bytes(i, encoded[i])) return false;
+        // decode in parallel; each image is independent
+        std::vector<std::string> errs(n);
+        std::atomic<size_t> next{0};
+        const auto worker = [&]() {
+            for (size_t i; (i = next.fetch_add(1)) < n;) {
+                if (!ptimg::decode_texture_rgba8(encoded[i].data(), encoded[i].size(), rgba[i], w[i], h[i], errs[i],
+                                                 PT_ATLAS_SIZE) && errs[i].empty())
+                    errs[i] = "decode failed";
+                std::vector<uint8_t>().swap(encoded[i]);
+            }
+        };
+        const size_t nt = std::min<size_t>(n, std::max(1u, std::min(std::thread::hardware_concurrency(), 16u)));
+        std::vector<std::thread> pool;
+        for (size_t t = 1; t < nt; ++t) pool.emplace_back(worker);
+        worker();
+        for (auto& t : pool) t.join();
+        for (size_t i = 0; i < n; ++i)
+            if (!errs[i].empty()) return fail("image " + std::to_string(i) + ": " + errs[i]);
+        struct Layer {
+            AtlasPacker packer;
+            std::vector<uint8_t> pixels;
+        };
+        std::vector<Layer> layers[2];  // [0] linear, [1] sRGB
+        std::vector<std::pair<int, AtlasSlot>> placed(n);
+        const size_t layer_bytes = (size_t)PT_ATLAS_SIZE * PT_ATLAS_SIZE * 4;
+        for (size_t i = 0; i < n; ++i) {
+            const int kind = srgb.count((long)i) ? 1 : 0;
+            auto& ls = layers[kind];
+            int x = 0, y = 0;
+            size_t li = 0;
+            while (li < ls.size() && !ls[li].packer.place((int)w[i], (int)h[i], x, y)) ++li;
+            if (li == ls.size()) {
+                ls.emplace_back();
+                ls.back().pixels.assign(layer_bytes, 0);
+                if (!ls.back().packer.place((int)w[i], (int)h[i], x, y))
+                    return fail("image " + std::to_string(i) + " is larger than the atlas");
+            }
+            uint8_t* dst = ls[li].pixels.data();
+            for (uint32_t r = 0; r < h[i]; ++r)
+                memcpy(dst + (((size_t)(y + r) * PT_ATLAS_SIZE) + (size_t)x) * 4, rgba[i].data() + (size_t)r * w[i] * 4,
+                       (size_t)w[i] * 4);
+            std::vector<uint8_t>().swap(rgba[i]);
+            AtlasSlot a;
+            a.layer = (int32_t)li;
+            a.uv[0] = (float)x / (float)PT_ATLAS_SIZE;
+            a.uv[1] = (float)y / (float)PT_ATLAS_SIZE;
+            a.uv[2] = (float)w[i] / (float)PT_ATLAS_SIZE;
+            a.uv[3] = (float)h[i] / (float)PT_ATLAS_SIZE;
+            placed[i] = {kind, a};
+        }
+        // hand the layers to the world; its layer indices may start after layers added earlier
+        std::vector<int32_t> index[2];
+        for (int kind = 0; kind < 2; ++kind)
+            for (Layer& l : layers[kind]) {
+                int32_t li = -1;
+                if (ptw_add_atlas_layer(world, kind, l.pixels.data(), &li) != PT_OK) return fail(ptw_last_error(world));
+                index[kind].push_back(li);
+                std::vector<uint8_t>().swap(l.pixels);
+            }
+        for (size_t i = 0; i < n; ++i) {
+            AtlasSlot a = placed[i].second;
+            a.layer = index[placed[i].first][(size_t)a.layer];
+            (placed[i].first ? srgb_slots : linear_slots)[(long)i] = a;
+        }
+        return true;
+    }
+
     // GpuMaterial::new, world.rs:1992-2155
     bool material(const Json* m, uint32_t* out) {
         pt_material g;
@@ -508,9 +688,25 @@ struct Loader {
         const Json& mat = m ? *m : empty;
         const Json* pbr = mat.get("pbrMetallicRoughness");
         const Json& p = pbr ? *pbr : empty;
-        if (has_texture(p.get("baseColorTexture")) || has_texture(p.get("metallicRoughnessTexture")) ||
-            has_texture(mat.get("normalTexture")) || has_texture(mat.get("emissiveTexture")))
-            return fail("textured glTF materials are not supported (no image decoding)");
+        // atlas layer and UV offset/scale of each texture slot; -1 and zeros without one
+        const auto slot = [&](const Json* t, bool srgb, int32_t* layer, float* uv) {
+            const long img = texture_image(t);
+            const auto& slots = srgb ? srgb_slots : linear_slots;
+            const auto it = img >= 0 ? slots.find(img) : slots.end();
+            const AtlasSlot none;
+            const AtlasSlot& a = it == slots.end() ? none : it->second;
+            *layer = a.layer;
+            for (int i = 0; i < 4; ++i) uv[i] = a.uv[i];
+        };
+        slot(p.get("baseColorTexture"), true, &g.base_color_tex_layer, g.base_color_uv);
+        slot(p.get("metallicRoughnessTexture"), false, &g.metallic_roughness_tex_layer, g.metallic_roughness_uv);
+        slot(mat.get("normalTexture"), false, &g.normal_tex_layer, g.normal_uv);
+        slot(mat.get("emissiveTexture"), true, &g.emission_tex_layer, g.emission_uv);
+        const Json* spec_ext = mat.get("extensions") ? mat.get("extensions")->get("KHR_materials_specular") : nullptr;
+        slot(spec_ext ? spec_ext->get("specularTexture") : nullptr, false, &g.specular_weight_tex_layer,
+             g.specular_weight_uv);
+        slot(spec_ext ? spec_ext->get("specularColorTexture") : nullptr, true, &g.specular_color_tex_layer,
+             g.specular_color_uv);
         const Json* bcf = p.get("baseColorFactor");
         for (int i = 0; i < 4; ++i)
             g.base_color[i] = bcf && bcf->arr.size() == 4 ? (float)bcf->arr[i].num : 1.0f;
@@ -531,13 +727,13 @@ struct Loader {
         g.specular_ior = 1.5f;
         g.specular_retroreflectivity = 0.0f;
         g.normal_scale = 1.0f;
+        if (const Json* nt = mat.get("normalTexture"))
+            if (has_texture(nt)) g.normal_scale = (float)nt->number("scale", 1.0);
         if (const Json* ext = mat.get("extensions")) {
             if (const Json* es = ext->get("KHR_materials_emissive_strength"))
                 g.emission_color_and_luminance[3] = (float)es->number("emissiveStrength", 1.0);
             if (const Json* ior = ext->get("KHR_materials_ior")) g.specular_ior = (float)ior->number("ior", 1.5);
             if (const Json* sp = ext->get("KHR_materials_specular")) {
-                if (has_texture(sp->get("specularTexture")) || has_texture(sp->get("specularColorTexture")))
-                    return fail("textured glTF materials are not supported (no image decoding)");
                 g.specular_color_and_weight[3] = (float)sp->number("specularFactor", 1.0);
                 if (const Json* sc = sp->get("specularColorFactor"))
                     for (int i = 0; i < 3 && i < (int)sc->arr.size(); ++i)
@@ -564,10 +760,6 @@ struct Loader {
             apply("OpenPBR_specular_haze_spread", &g.specular_haze_spread);
             apply("OpenPBR_specular_retroreflectivity", &g.specular_retroreflectivity);
         }
-        // no texture: layer -1 and a zero UV transform
-        for (float* uv : {g.base_color_uv, g.normal_uv, g.metallic_roughness_uv, g.emission_uv, g.specular_weight_uv,
-                          g.specular_color_uv})
-            uv[0] = uv[1] = uv[2] = uv[3] = 0.0f;
         return ptw_add_material(world, &g, out) == PT_OK || fail(ptw_last_error(world));
     }
 
@@ -641,6 +833,7 @@ struct Loader {
     }
 
     bool load() {
+        if (!images()) return false;
         const Json* nodes = doc.get("nodes");
         const Json* meshes = doc.get("meshes");
         std::vector<long> roots;
@@ -699,7 +892,13 @@ extern "C" int ptw_load_gltf(ptw_world* world, const char* path, char* error, si
     if (!world || !path) return PT_ERR_INVALID_ARG;
     Loader l;
     l.world = world;
-    const bool ok = l.open(path) && l.load();
+    bool ok;
+    try {
+        ok = l.open(path) && l.load();
+    } catch (const std::bad_alloc&) {
+        if (error && error_size) snprintf(error, error_size, "out of host memory");
+        return PT_ERR_OOM;
+    }
     if (!ok && error && error_size) snprintf(error, error_size, "%s", l.error.c_str());
     return ok ? PT_OK : PT_ERR_INVALID_ARG;
 }

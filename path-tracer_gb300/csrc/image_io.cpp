@@ -12,11 +12,13 @@
 // run-length symbol, and a two-dimensional Haar-style wavelet per channel
 // plane, as the OpenEXR format specifies them.
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <new>
 #include <string>
 #include <thread>
 #include <vector>
@@ -24,6 +26,9 @@
 #include "../../include/pt_world.h"
 
 namespace {
+
+// skybox images up to 2^28 pixels (4 GiB as RGBA32F); the reference's are 2K and 4K equirects
+constexpr int64_t kMaxSkyPixels = (int64_t)1 << 28;
 
 bool read_file(const char* path, std::vector<uint8_t>& data, std::string& err) {
     FILE* f = fopen(path, "rb");
@@ -71,6 +76,10 @@ bool read_hdr(const std::vector<uint8_t>& data, std::vector<float>& rgba, uint32
     int hh = 0, ww = 0;
     if (sscanf(res.c_str(), "-Y %d +X %d", &hh, &ww) != 2 || hh <= 0 || ww <= 0) {
         err = "unsupported HDR orientation: " + res;
+        return false;
+    }
+    if ((uint64_t)ww * (uint64_t)hh > (uint64_t)kMaxSkyPixels) {
+        err = "HDR image too large";
         return false;
     }
     w = (uint32_t)ww;
@@ -660,7 +669,7 @@ bool read_exr(const std::vector<uint8_t>& d, std::vector<float>& rgba, uint32_t&
     if (ch.empty()) return fail("no channels");
     if (win[2] < win[0] || win[3] < win[1]) return fail("empty data window");
     const int64_t W = (int64_t)win[2] - win[0] + 1, H = (int64_t)win[3] - win[1] + 1;
-    if (W > 65536 || H > 65536) return fail("image too large");
+    if (W > 65536 || H > 65536 || W * H > kMaxSkyPixels) return fail("image too large");
     int lines;
     switch (compression) {
         case 0: case 1: case 2: lines = 1; break;
@@ -760,6 +769,733 @@ bool read_exr(const std::vector<uint8_t>& d, std::vector<float>& rgba, uint32_t&
     return true;
 }
 
+// ------------------------------------------------------------- PNG
+// Decoded samples as the image library hands them to the glTF importer:
+// palette and low-bit-depth grey expanded to 8 bits, a tRNS chunk expanded
+// to an alpha channel, 16-bit samples kept.
+struct Raster {
+    uint32_t w = 0, h = 0;
+    int channels = 0;  // 1 grey, 2 grey + alpha, 3 RGB, 4 RGBA
+    int depth = 8;     // 8 or 16
+    std::vector<uint16_t> v;
+};
+
+uint32_t be32(const uint8_t* p) { return ((uint32_t)p[0] << 24) | ((uint32_t)p[1] << 16) | ((uint32_t)p[2] << 8) | p[3]; }
+
+uint32_t crc32_png(const uint8_t* d, size_t n) {
+    static const std::array<uint32_t, 256> table = [] {
+        std::array<uint32_t, 256> t{};
+        for (uint32_t i = 0; i < 256; ++i) {
+            uint32_t c = i;
+            for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xedb88320u ^ (c >> 1) : c >> 1;
+            t[i] = c;
+        }
+        return t;
+    }();
+    uint32_t c = 0xffffffffu;
+    for (size_t i = 0; i < n; ++i) c = table[(c ^ d[i]) & 0xff] ^ (c >> 8);
+    return c ^ 0xffffffffu;
+}
+
+bool decode_png(const uint8_t* d, size_t n, Raster& out, std::string& err, uint32_t max_side) {
+    static const uint8_t kSig[8] = {0x89, 'P', 'N', 'G', 0x0d, 0x0a, 0x1a, 0x0a};
+    if (n < 8 || memcmp(d, kSig, 8) != 0) {
+        err = "not a PNG file";
+        return false;
+    }
+    uint32_t w = 0, h = 0;
+    int depth = 0, ctype = -1, interlace = 0;
+    std::vector<uint8_t> idat, palette, trns;
+    bool seen_ihdr = false, seen_iend = false;
+    for (size_t pos = 8; pos + 12 <= n && !seen_iend;) {
+        const uint32_t len = be32(d + pos);
+        if (len > n - pos - 12) {
+            err = "PNG chunk runs past the end of the file";
+            return false;
+        }
+        const uint8_t* type = d + pos + 4;
+        const uint8_t* body = d + pos + 8;
+        if (crc32_png(type, (size_t)len + 4) != be32(body + len)) {
+            err = "PNG chunk CRC mismatch";
+            return false;
+        }
+        if (!memcmp(type, "IHDR", 4)) {
+            if (len != 13) {
+                err = "bad PNG header";
+                return false;
+            }
+            w = be32(body);
+            h = be32(body + 4);
+            depth = body[8];
+            ctype = body[9];
+            interlace = body[12];
+            seen_ihdr = true;
+            if (body[10] != 0 || body[11] != 0 || interlace > 1) {
+                err = "unsupported PNG compression, filter or interlace method";
+                return false;
+            }
+        } else if (!memcmp(type, "PLTE", 4)) {
+            palette.assign(body, body + len);
+        } else if (!memcmp(type, "tRNS", 4)) {
+            trns.assign(body, body + len);
+        } else if (!memcmp(type, "IDAT", 4)) {
+            idat.insert(idat.end(), body, body + len);
+        } else if (!memcmp(type, "IEND", 4)) {
+            seen_iend = true;
+        } else if (!(type[0] & 0x20)) {
+            err = "unknown critical PNG chunk";
+            return false;
+        }
+        pos += (size_t)len + 12;
+    }
+    if (!seen_ihdr || w == 0 || h == 0 || w > 65536 || h > 65536) {
+        err = "bad PNG header";
+        return false;
+    }
+    if (w > max_side || h > max_side) {
+        err = "image larger than the atlas";
+        return false;
+    }
+    int samples;  // per pixel in the file
+    switch (ctype) {
+        case 0: samples = 1; break;
+        case 2: samples = 3; break;
+        case 3: samples = 1; break;
+        case 4: samples = 2; break;
+        case 6: samples = 4; break;
+        default: err = "bad PNG colour type"; return false;
+    }
+    const bool depth_ok = ctype == 0   ? (depth == 1 || depth == 2 || depth == 4 || depth == 8 || depth == 16)
+                          : ctype == 3 ? (depth == 1 || depth == 2 || depth == 4 || depth == 8)
+                                       : (depth == 8 || depth == 16);
+    if (!depth_ok) {
+        err = "bad PNG bit depth";
+        return false;
+    }
+    if (ctype == 3 && (palette.empty() || palette.size() % 3)) {
+        err = "PNG palette missing";
+        return false;
+    }
+    const int bpp_bits = samples * depth;
+    const size_t fb = (size_t)std::max(1, bpp_bits / 8);  // filter byte distance
+    // Adam7 passes (x0, y0, dx, dy), or one pass
+    static const int kAdam7[7][4] = {{0, 0, 8, 8}, {4, 0, 8, 8}, {0, 4, 4, 8}, {2, 0, 4, 4},
+                                     {0, 2, 2, 4}, {1, 0, 2, 2}, {0, 1, 1, 2}};
+    const int npass = interlace ? 7 : 1;
+    size_t raw_size = 0;
+    for (int ps = 0; ps < npass; ++ps) {
+        const int* a = interlace ? kAdam7[ps] : nullptr;
+        const uint64_t pw = a ? (w > (uint32_t)a[0] ? (w - a[0] + a[2] - 1) / a[2] : 0) : w;
+        const uint64_t ph = a ? (h > (uint32_t)a[1] ? (h - a[1] + a[3] - 1) / a[3] : 0) : h;
+        if (pw && ph) raw_size += (size_t)ph * (1 + (size_t)((pw * bpp_bits + 7) / 8));
+    }
+    std::vector<uint8_t> raw;
+    if (!zlib_inflate(idat.data(), idat.size(), raw, raw_size) || raw.size() != raw_size) {
+        err = "bad PNG image data";
+        return false;
+    }
+    const bool has_trns = !trns.empty() && ctype != 4 && ctype != 6;
+    out.w = w;
+    out.h = h;
+    out.depth = (ctype == 3 || depth < 8) ? 8 : depth;
+    out.channels = ctype == 3 ? (has_trns ? 4 : 3) : samples + (has_trns ? 1 : 0);
+    out.v.assign((size_t)w * h * out.channels, 0);
+    const uint16_t maxv = out.depth == 16 ? 65535 : 255;
+    size_t at = 0;
+    std::vector<uint8_t> prev, cur;
+    for (int ps = 0; ps < npass; ++ps) {
+        const int* a = interlace ? kAdam7[ps] : nullptr;
+        const uint32_t x0 = a ? a[0] : 0, y0 = a ? a[1] : 0, dx = a ? a[2] : 1, dy = a ? a[3] : 1;
+        const uint32_t pw = w > x0 ? (w - x0 + dx - 1) / dx : 0, ph = h > y0 ? (h - y0 + dy - 1) / dy : 0;
+        if (!pw || !ph) continue;
+        const size_t rb = (size_t)(((uint64_t)pw * bpp_bits + 7) / 8);
+        prev.assign(rb, 0);
+        cur.assign(rb, 0);
+        for (uint32_t r = 0; r < ph; ++r) {
+            const uint8_t f = raw[at++];
+            const uint8_t* src = &raw[at];
+            at += rb;
+            for (size_t i = 0; i < rb; ++i) {
+                const int left = i >= fb ? cur[i - fb] : 0, up = prev[i], ul = i >= fb ? prev[i - fb] : 0;
+                int v = src[i];
+                switch (f) {
+                    case 0: break;
+                    case 1: v += left; break;
+                    case 2: v += up; break;
+                    case 3: v += (left + up) >> 1; break;
+                    case 4: {
+                        const int pp = left + up - ul, pa = std::abs(pp - left), pb = std::abs(pp - up),
+                                  pc = std::abs(pp - ul);
+                        v += (pa <= pb && pa <= pc) ? left : (pb <= pc ? up : ul);
+                        break;
+                    }
+                    default: err = "bad PNG filter type"; return false;
+                }
+                cur[i] = (uint8_t)v;
+            }
+            // unpack the row's samples into the output
+            const uint32_t y = y0 + r * dy;
+            for (uint32_t c = 0; c < pw; ++c) {
+                const uint32_t x = x0 + c * dx;
+                uint16_t* o = &out.v[((size_t)y * w + x) * out.channels];
+                uint32_t s[4] = {0, 0, 0, 0};
+                for (int k = 0; k < samples; ++k) {
+                    const uint64_t bit = ((uint64_t)c * samples + k) * depth;
+                    if (depth == 16)
+                        s[k] = ((uint32_t)cur[bit / 8] << 8) | cur[bit / 8 + 1];
+                    else if (depth == 8)
+                        s[k] = cur[bit / 8];
+                    else
+                        s[k] = (cur[bit / 8] >> (8 - depth - (bit % 8))) & ((1u << depth) - 1u);
+                }
+                if (ctype == 3) {
+                    const uint32_t i = s[0];
+                    if ((size_t)i * 3 + 2 >= palette.size()) {
+                        err = "PNG palette index out of range";
+                        return false;
+                    }
+                    o[0] = palette[i * 3];
+                    o[1] = palette[i * 3 + 1];
+                    o[2] = palette[i * 3 + 2];
+                    if (has_trns) o[3] = i < trns.size() ? trns[i] : 255;
+                    continue;
+                }
+                const uint32_t scale = depth < 8 ? 255u / ((1u << depth) - 1u) : 1u;
+                for (int k = 0; k < samples; ++k) o[k] = (uint16_t)(s[k] * scale);
+                if (has_trns) {
+                    bool key;
+                    if (ctype == 0)
+                        key = trns.size() >= 2 && s[0] == (((uint32_t)trns[0] << 8 | trns[1]) & (depth == 16 ? 0xffffu : (1u << depth) - 1u));
+                    else
+                        key = trns.size() >= 6 && s[0] == (((uint32_t)trns[0] << 8) | trns[1]) &&
+                              s[1] == (((uint32_t)trns[2] << 8) | trns[3]) && s[2] == (((uint32_t)trns[4] << 8) | trns[5]);
+                    o[samples] = key ? 0 : maxv;
+                }
+            }
+            std::swap(prev, cur);
+        }
+    }
+    return true;
+}
+
+// ------------------------------------------------------------- JPEG
+// Huffman-coded JPEG (ITU-T T.81): baseline, extended sequential and
+// progressive, 8-bit samples, 1, 3 or 4 components with sampling factors
+// 1..4, restart intervals.  Floating-point separable inverse DCT, chroma
+// upsampled with the triangle filter for 2:1 horizontal and 2:1 horizontal +
+// vertical subsampling (replication otherwise), JFIF YCbCr -> RGB.
+const uint8_t kNatural[64 + 16] = {
+    0,  1,  8,  16, 9,  2,  3,  10, 17, 24, 32, 25, 18, 11, 4,  5,  12, 19, 26, 33, 40, 48,
+    41, 34, 27, 20, 13, 6,  7,  14, 21, 28, 35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23,
+    30, 37, 44, 51, 58, 59, 52, 45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63,
+    // a malformed run past coefficient 63 lands on 63
+    63, 63, 63, 63, 63, 63, 63, 63, 63, 63, 63, 63, 63, 63, 63, 63};
+
+struct JHuff {
+    bool present = false;
+    uint8_t sym[256] = {0};
+    int32_t maxcode[18];
+    int32_t valoff[18];
+    uint16_t fast[1 << 9];  // 9-bit lookahead: length << 8 | symbol, 0 for longer codes
+    bool build(const uint8_t counts[16], const uint8_t* syms, int n) {
+        memcpy(sym, syms, (size_t)n);
+        int32_t code = 0, k = 0;
+        for (int l = 1; l <= 16; ++l) {
+            valoff[l] = k - code;
+            code += counts[l - 1];
+            k += counts[l - 1];
+            if (code > (1 << l)) return false;  // over-subscribed
+            maxcode[l] = counts[l - 1] ? code - 1 : -1;
+            code <<= 1;
+        }
+        maxcode[17] = 0x7fffffff;
+        memset(fast, 0, sizeof fast);
+        code = 0;
+        k = 0;
+        for (int l = 1; l <= 9; ++l, code <<= 1)
+            for (int i = 0; i < counts[l - 1]; ++i, ++code, ++k)
+                for (int e = code << (9 - l); e < ((code + 1) << (9 - l)); ++e) fast[e] = (uint16_t)(l << 8 | sym[k]);
+        present = true;
+        return true;
+    }
+};
+
+struct JBits {
+    const uint8_t* d;
+    size_t n, pos;
+    uint64_t acc = 0;
+    int cnt = 0;
+    bool marker = false;  // stopped at a marker: zeros are fed from here on
+    void fill() {
+        while (cnt <= 56) {
+            uint32_t b = 0;
+            if (!marker && pos < n) {
+                b = d[pos];
+                if (b == 0xff) {
+                    if (pos + 1 < n && d[pos + 1] == 0x00) {
+                        pos += 2;
+                    } else {
+                        marker = true;
+                        b = 0;
+                    }
+                } else {
+                    ++pos;
+                }
+            }
+            acc |= (uint64_t)b << (56 - cnt);
+            cnt += 8;
+        }
+    }
+    uint32_t peek(int k) {
+        if (cnt < k) fill();
+        return (uint32_t)(acc >> (64 - k));
+    }
+    void skip(int k) {
+        acc <<= k;
+        cnt -= k;
+    }
+    uint32_t get(int k) {
+        if (k == 0) return 0;
+        const uint32_t v = peek(k);
+        skip(k);
+        return v;
+    }
+    int decode(const JHuff& h) {
+        const uint32_t e = h.fast[peek(9)];
+        if (e) {
+            skip((int)(e >> 8));
+            return (int)(e & 0xff);
+        }
+        const uint32_t look = peek(16);
+        for (int l = 10; l <= 16; ++l) {
+            const int32_t code = (int32_t)(look >> (16 - l));
+            if (code <= h.maxcode[l]) {
+                skip(l);
+                const int32_t i = h.valoff[l] + code;
+                return i >= 0 && i < 256 ? h.sym[i] : -1;
+            }
+        }
+        return -1;
+    }
+    static int extend(uint32_t v, int t) { return t && v < (1u << (t - 1)) ? (int)v - (1 << t) + 1 : (int)v; }
+};
+
+struct JComp {
+    int id = 0, h = 1, v = 1, tq = 0;
+    int dc = 0, ac = 0;
+    int bw = 0, bh = 0;  // blocks of the MCU-aligned grid
+    int pred = 0;
+    bool latched = false;
+    uint16_t q[64] = {0};
+    std::vector<int16_t> coef;
+};
+
+bool decode_jpeg(const uint8_t* d, size_t n, Raster& out, std::string& err, uint32_t max_side) {
+    auto fail = [&](const char* m) {
+        err = std::string("JPEG: ") + m;
+        return false;
+    };
+    if (n < 4 || d[0] != 0xff || d[1] != 0xd8) return fail("not a JPEG file");
+    uint16_t qt[4][64] = {{0}};
+    bool qt_present[4] = {false, false, false, false};
+    JHuff hdc[4], hac[4];
+    std::vector<JComp> comps;
+    int W = 0, H = 0, hmax = 1, vmax = 1, mcux = 0, mcuy = 0;
+    bool progressive = false, frame = false;
+    int adobe = -1;  // APP14 colour transform, -1 when absent
+    uint32_t restart = 0;
+    size_t pos = 2;
+    for (;;) {
+        while (pos < n && d[pos] != 0xff) ++pos;  // tolerate junk between segments
+        while (pos < n && d[pos] == 0xff) ++pos;
+        if (pos >= n) return fail("no end-of-image marker");
+        const uint8_t m = d[pos++];
+        if (m == 0xd9) break;
+        if (m == 0xd8 || (m >= 0xd0 && m <= 0xd7) || m == 0x01) continue;
+        if (pos + 2 > n) return fail("truncated segment");
+        const size_t len = ((size_t)d[pos] << 8) | d[pos + 1];
+        if (len < 2 || pos + len > n) return fail("truncated segment");
+        const uint8_t* s = d + pos + 2;
+        const size_t sl = len - 2;
+        pos += len;
+        if (m == 0xdb) {  // DQT
+            for (size_t i = 0; i < sl;) {
+                const int pq = s[i] >> 4, tq = s[i] & 15;
+                if (tq > 3 || pq > 1 || i + 1 + 64 * (size_t)(pq + 1) > sl) return fail("bad quantisation table");
+                for (int k = 0; k < 64; ++k)
+                    qt[tq][kNatural[k]] = pq ? (uint16_t)(s[i + 1 + 2 * k] << 8 | s[i + 2 + 2 * k]) : s[i + 1 + k];
+                qt_present[tq] = true;
+                i += 1 + 64 * (size_t)(pq + 1);
+            }
+        } else if (m == 0xc4) {  // DHT
+            for (size_t i = 0; i < sl;) {
+                if (i + 17 > sl) return fail("bad Huffman table");
+                const int tc = s[i] >> 4, th = s[i] & 15;
+                int total = 0;
+                for (int k = 0; k < 16; ++k) total += s[i + 1 + k];
+                if (tc > 1 || th > 3 || total > 256 || i + 17 + (size_t)total > sl) return fail("bad Huffman table");
+                if (!(tc ? hac[th] : hdc[th]).build(s + i + 1, s + i + 17, total)) return fail("bad Huffman table");
+                i += 17 + (size_t)total;
+            }
+        } else if (m == 0xdd) {  // DRI
+            if (sl < 2) return fail("bad restart interval");
+            restart = ((uint32_t)s[0] << 8) | s[1];
+        } else if (m == 0xee) {  // APP14
+            if (sl >= 12 && !memcmp(s, "Adobe", 5)) adobe = s[11];
+        } else if (m == 0xc0 || m == 0xc1 || m == 0xc2) {
+            if (frame) return fail("more than one frame");
+            frame = true;
+            progressive = m == 0xc2;
+            if (sl < 6 || s[0] != 8) return fail("only 8-bit samples are supported");
+            H = s[1] << 8 | s[2];
+            W = s[3] << 8 | s[4];
+            const int nc = s[5];
+            if (W == 0 || H == 0) return fail("zero image size (DNL is not supported)");
+            if ((uint32_t)W > max_side || (uint32_t)H > max_side) return fail("image larger than the atlas");
+            if ((nc != 1 && nc != 3 && nc != 4) || sl < 6 + 3 * (size_t)nc) return fail("unsupported component count");
+            for (int c = 0; c < nc; ++c) {
+                JComp jc;
+                jc.id = s[6 + 3 * c];
+                jc.h = s[7 + 3 * c] >> 4;
+                jc.v = s[7 + 3 * c] & 15;
+                jc.tq = s[8 + 3 * c];
+                if (jc.h < 1 || jc.h > 4 || jc.v < 1 || jc.v > 4 || jc.tq > 3) return fail("bad component");
+                hmax = std::max(hmax, jc.h);
+                vmax = std::max(vmax, jc.v);
+                comps.push_back(jc);
+            }
+            mcux = (W + 8 * hmax - 1) / (8 * hmax);
+            mcuy = (H + 8 * vmax - 1) / (8 * vmax);
+            for (JComp& c : comps) {
+                c.bw = mcux * c.h;
+                c.bh = mcuy * c.v;
+                c.coef.assign((size_t)c.bw * c.bh * 64, 0);
+            }
+        } else if ((m >= 0xc3 && m <= 0xcf) && m != 0xc4 && m != 0xc8 && m != 0xcc) {
+            return fail("unsupported coding (lossless, hierarchical or arithmetic)");
+        } else if (m == 0xda) {  // SOS
+            if (!frame || sl < 1) return fail("scan before frame");
+            const int ns = s[0];
+            if (ns < 1 || ns > 4 || sl < 4 + 2 * (size_t)ns) return fail("bad scan header");
+            JComp* sc[4];
+            for (int i = 0; i < ns; ++i) {
+                sc[i] = nullptr;
+                for (JComp& c : comps)
+                    if (c.id == s[1 + 2 * i]) sc[i] = &c;
+                if (!sc[i]) return fail("scan names an unknown component");
+                sc[i]->dc = s[2 + 2 * i] >> 4;
+                sc[i]->ac = s[2 + 2 * i] & 15;
+                if (sc[i]->dc > 3 || sc[i]->ac > 3) return fail("bad table selector");
+                if (!sc[i]->latched) {
+                    if (!qt_present[sc[i]->tq]) return fail("missing quantisation table");
+                    memcpy(sc[i]->q, qt[sc[i]->tq], sizeof sc[i]->q);
+                    sc[i]->latched = true;
+                }
+            }
+            const int ss = s[1 + 2 * ns], se = s[2 + 2 * ns], ah = s[3 + 2 * ns] >> 4, al = s[3 + 2 * ns] & 15;
+            if (progressive) {
+                if (ss > se || se > 63 || (ss == 0 && se != 0) || (ss > 0 && ns != 1) || al > 13)
+                    return fail("bad progressive scan");
+            } else if (ss != 0 || se != 63 || ah || al) {
+                return fail("bad sequential scan");
+            }
+            const bool dc_scan = ss == 0;
+            for (int i = 0; i < ns; ++i) {
+                if (((!progressive || (dc_scan && ah == 0)) && !hdc[sc[i]->dc].present) ||
+                    ((!progressive || !dc_scan) && !hac[sc[i]->ac].present))
+                    return fail("missing Huffman table");
+                sc[i]->pred = 0;
+            }
+            JBits bits{d, n, pos};
+            int eobrun = 0;
+            bool bad = false;
+            // one block of component c at coefficient offset `blk`
+            auto block = [&](JComp& c, int16_t* coef) {
+                if (!progressive) {
+                    const int t = bits.decode(hdc[c.dc]);
+                    if (t < 0 || t > 11) return bad = true, void();
+                    c.pred += JBits::extend(bits.get(t), t);
+                    coef[0] = (int16_t)c.pred;
+                    for (int k = 1; k < 64;) {
+                        const int rs = bits.decode(hac[c.ac]);
+                        if (rs < 0) return bad = true, void();
+                        const int r = rs >> 4, sz = rs & 15;
+                        if (!sz) {
+                            if (r != 15) break;
+                            k += 16;
+                            continue;
+                        }
+                        k += r;
+                        coef[kNatural[k]] = (int16_t)JBits::extend(bits.get(sz), sz);
+                        ++k;
+                    }
+                } else if (dc_scan) {
+                    if (ah == 0) {
+                        const int t = bits.decode(hdc[c.dc]);
+                        if (t < 0 || t > 11) return bad = true, void();
+                        c.pred += JBits::extend(bits.get(t), t);
+                        coef[0] = (int16_t)(c.pred * (1 << al));
+                    } else if (bits.get(1)) {
+                        coef[0] = (int16_t)(coef[0] | (1 << al));
+                    }
+                } else if (ah == 0) {
+                    if (eobrun > 0) {
+                        --eobrun;
+                        return;
+                    }
+                    for (int k = ss; k <= se;) {
+                        const int rs = bits.decode(hac[c.ac]);
+                        if (rs < 0) return bad = true, void();
+                        const int r = rs >> 4, sz = rs & 15;
+                        if (!sz) {
+                            if (r < 15) {
+                                eobrun = (1 << r) - 1;
+                                if (r) eobrun += (int)bits.get(r);
+                                break;
+                            }
+                            k += 16;
+                            continue;
+                        }
+                        k += r;
+                        coef[kNatural[k]] = (int16_t)(JBits::extend(bits.get(sz), sz) * (1 << al));
+                        ++k;
+                    }
+                } else {
+                    // successive-approximation refinement of AC coefficients
+                    const int p1 = 1 << al, m1 = -p1;
+                    int k = ss;
+                    const auto refine = [&](int16_t& cf) {
+                        if (bits.get(1) && (cf & p1) == 0) cf = (int16_t)(cf + (cf >= 0 ? p1 : m1));
+                    };
+                    if (eobrun == 0) {
+                        for (; k <= se; ++k) {
+                            const int rs = bits.decode(hac[c.ac]);
+                            if (rs < 0) return bad = true, void();
+                            int r = rs >> 4, val = 0;
+                            if (rs & 15) {
+                                val = bits.get(1) ? p1 : m1;
+                            } else if (r != 15) {
+                                eobrun = 1 << r;
+                                if (r) eobrun += (int)bits.get(r);
+                                break;
+                            }
+                            while (k <= se) {
+                                int16_t& cf = coef[kNatural[k]];
+                                if (cf != 0) {
+                                    refine(cf);
+                                } else if (--r < 0) {
+                                    break;
+                                }
+                                ++k;
+                            }
+                            if (val && k <= se) coef[kNatural[k]] = (int16_t)val;
+                        }
+                    }
+                    if (eobrun > 0) {
+                        for (; k <= se; ++k)
+                            if (coef[kNatural[k]] != 0) refine(coef[kNatural[k]]);
+                        --eobrun;
+                    }
+                }
+            };
+            auto restart_marker = [&]() {
+                bits.acc = 0;
+                bits.cnt = 0;
+                bits.marker = false;
+                size_t p = bits.pos;
+                while (p + 1 < n && !(d[p] == 0xff && d[p + 1] != 0x00 && d[p + 1] != 0xff)) ++p;
+                if (p + 1 < n && d[p + 1] >= 0xd0 && d[p + 1] <= 0xd7) p += 2;
+                bits.pos = p;
+                for (int i = 0; i < ns; ++i) sc[i]->pred = 0;
+                eobrun = 0;
+            };
+            uint32_t mcu = 0;
+            if (ns == 1) {
+                JComp& c = *sc[0];
+                const int cw = ((W * c.h + hmax - 1) / hmax + 7) / 8, ch = ((H * c.v + vmax - 1) / vmax + 7) / 8;
+                for (int by = 0; by < ch && !bad; ++by)
+                    for (int bx = 0; bx < cw && !bad; ++bx, ++mcu) {
+                        if (restart && mcu && mcu % restart == 0) restart_marker();
+                        block(c, &c.coef[((size_t)by * c.bw + bx) * 64]);
+                    }
+            } else {
+                for (int my = 0; my < mcuy && !bad; ++my)
+                    for (int mx = 0; mx < mcux && !bad; ++mx, ++mcu) {
+                        if (restart && mcu && mcu % restart == 0) restart_marker();
+                        for (int i = 0; i < ns; ++i) {
+                            JComp& c = *sc[i];
+                            for (int v = 0; v < c.v; ++v)
+                                for (int h = 0; h < c.h; ++h)
+                                    block(c, &c.coef[((size_t)(my * c.v + v) * c.bw + (mx * c.h + h)) * 64]);
+                        }
+                    }
+            }
+            if (bad) return fail("corrupt entropy-coded data");
+            // continue after the scan's data: the next marker that is not a restart marker
+            size_t p = bits.pos;
+            while (p + 1 < n && !(d[p] == 0xff && d[p + 1] != 0x00 && d[p + 1] != 0xff &&
+                                  !(d[p + 1] >= 0xd0 && d[p + 1] <= 0xd7)))
+                ++p;
+            pos = p;
+        } else if (m == 0xdc) {
+            return fail("DNL marker is not supported");
+        }
+        // APPn, COM and other segments are skipped
+    }
+    if (!frame) return fail("no frame");
+    // dequantise and inverse-transform every block into component planes
+    static const std::array<float, 64> kCos = [] {
+        std::array<float, 64> t{};
+        for (int x = 0; x < 8; ++x)
+            for (int u = 0; u < 8; ++u)
+                t[x * 8 + u] = (float)((u == 0 ? std::sqrt(0.5) : 1.0) * std::cos((2 * x + 1) * u * 3.14159265358979323846 / 16.0) / 2.0);
+        return t;
+    }();
+    std::vector<std::vector<uint8_t>> plane(comps.size());
+    for (size_t ci = 0; ci < comps.size(); ++ci) {
+        JComp& c = comps[ci];
+        const size_t stride = (size_t)c.bw * 8;
+        plane[ci].assign(stride * c.bh * 8, 0);
+        for (int by = 0; by < c.bh; ++by)
+            for (int bx = 0; bx < c.bw; ++bx) {
+                const int16_t* cf = &c.coef[((size_t)by * c.bw + bx) * 64];
+                float f[64], t[64];
+                for (int i = 0; i < 64; ++i) f[i] = (float)cf[i] * (float)c.q[i];
+                for (int v = 0; v < 8; ++v)  // rows: horizontal frequencies -> x
+                    for (int x = 0; x < 8; ++x) {
+                        float a = 0.0f;
+                        for (int u = 0; u < 8; ++u) a += kCos[x * 8 + u] * f[v * 8 + u];
+                        t[v * 8 + x] = a;
+                    }
+                for (int y = 0; y < 8; ++y)
+                    for (int x = 0; x < 8; ++x) {
+                        float a = 0.0f;
+                        for (int v = 0; v < 8; ++v) a += kCos[y * 8 + v] * t[v * 8 + x];
+                        const float px = std::floor(a + 128.0f + 0.5f);
+                        plane[ci][((size_t)by * 8 + y) * stride + (size_t)bx * 8 + x] =
+                            (uint8_t)(px < 0.0f ? 0.0f : px > 255.0f ? 255.0f : px);
+                    }
+            }
+        std::vector<int16_t>().swap(c.coef);
+    }
+    // upsample every component to the image size
+    std::vector<std::vector<uint8_t>> full(comps.size());
+    for (size_t ci = 0; ci < comps.size(); ++ci) {
+        const JComp& c = comps[ci];
+        const size_t stride = (size_t)c.bw * 8;
+        const int cw = (W * c.h + hmax - 1) / hmax, ch = (H * c.v + vmax - 1) / vmax;
+        const std::vector<uint8_t>& in = plane[ci];
+        std::vector<uint8_t>& o = full[ci];
+        o.assign((size_t)W * H, 0);
+        const bool h2 = hmax == 2 * c.h, v1 = vmax == c.v, v2 = vmax == 2 * c.v;
+        if (c.h == hmax && c.v == vmax) {
+            for (int y = 0; y < H; ++y) memcpy(&o[(size_t)y * W], &in[(size_t)y * stride], (size_t)W);
+        } else if (h2 && (v1 || v2) && cw >= 2) {
+            std::vector<int> row(2 * (size_t)cw);
+            for (int y = 0; y < H; ++y) {
+                if (v1) {
+                    const uint8_t* r = &in[(size_t)y * stride];
+                    row[0] = r[0];
+                    row[1] = (r[0] * 3 + r[1] + 2) >> 2;
+                    for (int x = 1; x < cw - 1; ++x) {
+                        row[2 * x] = (r[x] * 3 + r[x - 1] + 1) >> 2;
+                        row[2 * x + 1] = (r[x] * 3 + r[x + 1] + 2) >> 2;
+                    }
+                    row[2 * cw - 2] = (r[cw - 1] * 3 + r[cw - 2] + 1) >> 2;
+                    row[2 * cw - 1] = r[cw - 1];
+                } else {
+                    // the nearer input row counts three times, the other once
+                    const int yc = y / 2, yo = (y & 1) ? std::min(yc + 1, ch - 1) : std::max(yc - 1, 0);
+                    const uint8_t* r0 = &in[(size_t)yc * stride];
+                    const uint8_t* r1 = &in[(size_t)yo * stride];
+                    int last = 0, cur = r0[0] * 3 + r1[0], next = r0[1] * 3 + r1[1];
+                    row[0] = (cur * 4 + 8) >> 4;
+                    row[1] = (cur * 3 + next + 7) >> 4;
+                    last = cur;
+                    cur = next;
+                    for (int x = 1; x < cw - 1; ++x) {
+                        next = r0[x + 1] * 3 + r1[x + 1];
+                        row[2 * x] = (cur * 3 + last + 8) >> 4;
+                        row[2 * x + 1] = (cur * 3 + next + 7) >> 4;
+                        last = cur;
+                        cur = next;
+                    }
+                    row[2 * cw - 2] = (cur * 3 + last + 8) >> 4;
+                    row[2 * cw - 1] = (cur * 4 + 7) >> 4;
+                }
+                for (int x = 0; x < W; ++x) o[(size_t)y * W + x] = (uint8_t)row[(size_t)x];
+            }
+        } else {
+            for (int y = 0; y < H; ++y)
+                for (int x = 0; x < W; ++x)
+                    o[(size_t)y * W + x] = in[(size_t)(y * c.v / vmax) * stride + (size_t)(x * c.h / hmax)];
+        }
+    }
+    out.w = (uint32_t)W;
+    out.h = (uint32_t)H;
+    out.depth = 8;
+    out.channels = comps.size() == 1 ? 1 : 3;
+    out.v.assign((size_t)W * H * out.channels, 0);
+    const bool rgb_ids = comps.size() == 3 && comps[0].id == 'R' && comps[1].id == 'G' && comps[2].id == 'B';
+    const bool ycc = comps.size() == 3 ? (adobe >= 0 ? adobe != 0 : !rgb_ids) : adobe == 2;
+    const auto clamp8 = [](float v) { return (uint16_t)(v < 0.0f ? 0.0f : v > 255.0f ? 255.0f : std::floor(v + 0.5f)); };
+    for (size_t i = 0; i < (size_t)W * H; ++i) {
+        if (comps.size() == 1) {
+            out.v[i] = full[0][i];
+            continue;
+        }
+        uint16_t r = full[0][i], g = full[1][i], b = full[2][i];
+        if (ycc) {
+            const float y = full[0][i], cb = (float)full[1][i] - 128.0f, cr = (float)full[2][i] - 128.0f;
+            r = clamp8(y + 1.402f * cr);
+            g = clamp8(y - 0.344136f * cb - 0.714136f * cr);
+            b = clamp8(y + 1.772f * cb);
+        }
+        if (comps.size() == 4) {  // Adobe CMYK is stored inverted: ink-free = 255
+            const uint32_t k = full[3][i];
+            r = (uint16_t)((r * k + 127) / 255);
+            g = (uint16_t)((g * k + 127) / 255);
+            b = (uint16_t)((b * k + 127) / 255);
+        }
+        out.v[i * 3] = r;
+        out.v[i * 3 + 1] = g;
+        out.v[i * 3 + 2] = b;
+    }
+    return true;
+}
+
+// glTF texture image (PNG or JPEG) -> RGBA8 by the importer's conversion of
+// the decoded format (world.rs:949-1011): grey -> (l, l, l, 255); grey +
+// alpha (two channels) -> (l, a, 0, 255); RGB -> (r, g, b, 255); 16-bit
+// samples keep their high byte.
+bool decode_texture(const uint8_t* d, size_t n, std::vector<uint8_t>& rgba, uint32_t& w, uint32_t& h, std::string& err,
+                    uint32_t max_side) {
+    Raster r;
+    if (n >= 8 && d[0] == 0x89 && d[1] == 'P') {
+        if (!decode_png(d, n, r, err, max_side)) return false;
+    } else if (n >= 2 && d[0] == 0xff && d[1] == 0xd8) {
+        if (!decode_jpeg(d, n, r, err, max_side)) return false;
+    } else {
+        err = "unsupported image encoding (PNG and JPEG are read)";
+        return false;
+    }
+    w = r.w;
+    h = r.h;
+    rgba.assign((size_t)w * h * 4, 0);
+    const int shift = r.depth == 16 ? 8 : 0;
+    for (size_t i = 0; i < (size_t)w * h; ++i) {
+        const uint16_t* s = &r.v[i * r.channels];
+        uint8_t* o = &rgba[i * 4];
+        switch (r.channels) {
+            case 1: o[0] = o[1] = o[2] = (uint8_t)(s[0] >> shift); o[3] = 255; break;
+            case 2: o[0] = (uint8_t)(s[0] >> shift); o[1] = (uint8_t)(s[1] >> shift); o[2] = 0; o[3] = 255; break;
+            case 3: for (int k = 0; k < 3; ++k) o[k] = (uint8_t)(s[k] >> shift); o[3] = 255; break;
+            default: for (int k = 0; k < 4; ++k) o[k] = (uint8_t)(s[k] >> shift); break;
+        }
+    }
+    return true;
+}
+
 bool read_image(const char* path, std::vector<float>& rgba, uint32_t& w, uint32_t& h, std::string& err,
                 bool size_only = false) {
     std::vector<uint8_t> data;
@@ -775,8 +1511,15 @@ void put_error(char* error, size_t size, const std::string& msg) {
 
 }  // namespace
 
+namespace ptimg {
+bool decode_texture_rgba8(const uint8_t* bytes, size_t size, std::vector<uint8_t>& rgba, uint32_t& width,
+                          uint32_t& height, std::string& error, uint32_t max_side) {
+    return decode_texture(bytes, size, rgba, width, height, error, max_side);
+}
+}  // namespace ptimg
+
 extern "C" int ptw_read_image_rgba(const char* path, float* rgba, uint64_t capacity, uint32_t* width, uint32_t* height,
-                                   char* error, size_t error_size) {
+                                   char* error, size_t error_size) try {
     if (!path || !width || !height) return PT_ERR_INVALID_ARG;
     std::vector<float> px;
     uint32_t w = 0, h = 0;
@@ -794,9 +1537,12 @@ extern "C" int ptw_read_image_rgba(const char* path, float* rgba, uint64_t capac
     }
     memcpy(rgba, px.data(), px.size() * sizeof(float));
     return PT_OK;
+} catch (const std::bad_alloc&) {
+    put_error(error, error_size, "out of host memory");
+    return PT_ERR_OOM;
 }
 
-extern "C" int ptw_set_skybox_file(ptw_world* world, const char* path, char* error, size_t error_size) {
+extern "C" int ptw_set_skybox_file(ptw_world* world, const char* path, char* error, size_t error_size) try {
     if (!world || !path) return PT_ERR_INVALID_ARG;
     std::vector<float> px;
     uint32_t w = 0, h = 0;
@@ -808,4 +1554,31 @@ extern "C" int ptw_set_skybox_file(ptw_world* world, const char* path, char* err
     const int rc = ptw_set_skybox_rgba(world, px.data(), w, h);
     if (rc) put_error(error, error_size, ptw_last_error(world));
     return rc;
+} catch (const std::bad_alloc&) {
+    put_error(error, error_size, "out of host memory");
+    return PT_ERR_OOM;
+}
+
+extern "C" int ptw_decode_texture_rgba8(const void* bytes, size_t size, uint8_t* rgba, uint64_t capacity,
+                                        uint32_t* width, uint32_t* height, char* error, size_t error_size) try {
+    if (!bytes || !width || !height) return PT_ERR_INVALID_ARG;
+    std::vector<uint8_t> px;
+    uint32_t w = 0, h = 0;
+    std::string err;
+    if (!decode_texture((const uint8_t*)bytes, size, px, w, h, err, PT_ATLAS_SIZE)) {
+        put_error(error, error_size, err);
+        return PT_ERR_INVALID_ARG;
+    }
+    *width = w;
+    *height = h;
+    if (!rgba) return PT_OK;
+    if (capacity < px.size()) {
+        put_error(error, error_size, "output buffer too small");
+        return PT_ERR_OUT_OF_LIMITS;
+    }
+    memcpy(rgba, px.data(), px.size());
+    return PT_OK;
+} catch (const std::bad_alloc&) {
+    put_error(error, error_size, "out of host memory");
+    return PT_ERR_OOM;
 }

@@ -277,6 +277,22 @@ def read_image(path) -> np.ndarray:
     return out
 
 
+def decode_texture(data: bytes) -> np.ndarray:
+    """A PNG or JPEG image in memory as (height, width, 4) uint8 RGBA, converted as the glTF importer does."""
+    lib = load()
+    err = C.create_string_buffer(512)
+    w, h = C.c_uint32(), C.c_uint32()
+    buf = C.create_string_buffer(bytes(data), len(data))
+    rc = lib.ptw_decode_texture_rgba8(buf, len(data), None, 0, C.byref(w), C.byref(h), err, len(err))
+    if rc != abi.PT_OK:
+        raise PathTracerError(rc, err.value.decode())
+    out = np.empty((h.value, w.value, 4), np.uint8)
+    rc = lib.ptw_decode_texture_rgba8(buf, len(data), out.ctypes.data, out.size, C.byref(w), C.byref(h), err, len(err))
+    if rc != abi.PT_OK:
+        raise PathTracerError(rc, err.value.decode())
+    return out
+
+
 def build_bvh(triangles: np.ndarray):
     """Binned SAH BVH of world.rs:1430-1591 over (n, 9) float32 triangles -> (nodes (m, 8) uint32, order)."""
     t = np.ascontiguousarray(triangles, dtype=np.float32).reshape(-1, 9)

@@ -1,6 +1,7 @@
 """glTF 2.0 import (ptw_load_gltf): node transforms, the reference's LIFO node
 order, attribute defaults, material conversion (world.rs:1992-2155) and the
-refusals, on small files written here (.gltf with a base64 buffer and .glb)."""
+refusals, texture images packed into atlas layers, on small files written
+here (.gltf with a base64 buffer and .glb)."""
 import base64
 import json
 import struct
@@ -20,8 +21,9 @@ def quad(z=0.0):
     return pos, nor, uv, idx
 
 
-def write_gltf(tmp_path, nodes, scene_nodes, materials, binary=False, extra_prims=None):
-    """One mesh (the quad, indexed uint16, with normals and uvs) plus optional extra primitives."""
+def write_gltf(tmp_path, nodes, scene_nodes, materials, binary=False, extra_prims=None, images=None, textures=None):
+    """One mesh (the quad, indexed uint16, with normals and uvs) plus optional extra primitives.
+    images: list of (encoded bytes, how) with how "view" (a buffer view), "data" (a data URI) or "file"."""
     pos, nor, uv, idx = quad()
     blobs = [pos.tobytes(), nor.tobytes(), uv.tobytes(), idx.tobytes() + b"\0\0"]
     views, accessors, off = [], [], 0
@@ -30,12 +32,29 @@ def write_gltf(tmp_path, nodes, scene_nodes, materials, binary=False, extra_prim
         views.append({"buffer": 0, "byteOffset": off, "byteLength": len(b)})
         accessors.append({"bufferView": len(views) - 1, "componentType": ctype, "count": count, "type": typ})
         off += len(b)
+    image_docs = []
+    for k, (enc, how) in enumerate(images or []):
+        mime = "image/png" if enc[:4] == b"\x89PNG" else "image/jpeg"
+        if how == "view":
+            enc = enc + b"\0" * (-len(enc) % 4)
+            blobs.append(enc)
+            views.append({"buffer": 0, "byteOffset": off, "byteLength": len(enc)})
+            off += len(enc)
+            image_docs.append({"bufferView": len(views) - 1, "mimeType": mime})
+        elif how == "data":
+            image_docs.append({"uri": f"data:{mime};base64," + base64.b64encode(enc).decode()})
+        else:
+            (tmp_path / f"image{k}.bin").write_bytes(enc)
+            image_docs.append({"uri": f"image{k}.bin"})
     prims = [{"attributes": {"POSITION": 0, "NORMAL": 1, "TEXCOORD_0": 2}, "indices": 3, "material": 0}]
     prims += extra_prims or []
     data = b"".join(blobs)
     doc = {"asset": {"version": "2.0"}, "scene": 0, "scenes": [{"nodes": scene_nodes}], "nodes": nodes,
            "meshes": [{"primitives": prims}], "materials": materials, "accessors": accessors,
            "bufferViews": views, "buffers": [{"byteLength": len(data)}]}
+    if images:
+        doc["images"] = image_docs
+        doc["textures"] = textures if textures is not None else [{"source": i} for i in range(len(images))]
     if binary:
         js = json.dumps(doc).encode()
         js += b" " * (-len(js) % 4)
@@ -112,8 +131,8 @@ def test_defaults_without_normals_uvs_or_material(tmp_path):
 
 def test_refusals(tmp_path):
     textured = dict(MATERIAL, pbrMetallicRoughness={"baseColorTexture": {"index": 0}})
-    path = write_gltf(tmp_path, [{"mesh": 0}], [0], [textured])
-    with pytest.raises(pt.PathTracerError, match="textured"):
+    path = write_gltf(tmp_path, [{"mesh": 0}], [0], [textured], images=[(b"GIF89a....", "view")])
+    with pytest.raises(pt.PathTracerError, match="unsupported image encoding"):
         pt.World.from_gltf(path)
     (tmp_path / "bad.glb").write_bytes(b"glTF\x01\x00\x00\x00\x0c\x00\x00\x00")
     with pytest.raises(pt.PathTracerError, match="2.0"):
@@ -123,3 +142,87 @@ def test_refusals(tmp_path):
         pt.World.from_gltf(tmp_path / "broken.gltf")
     with pytest.raises(pt.PathTracerError, match="cannot read"):
         pt.World.from_gltf(tmp_path / "missing.glb")
+
+
+def _atlases(updates, srgb):
+    sc = updates.scene.contents
+    ptr, count = (sc.srgb_texture_atlases, sc.srgb_atlas_count) if srgb else (sc.linear_texture_atlases,
+                                                                              sc.linear_atlas_count)
+    n = abi.PT_ATLAS_SIZE
+    return np.ctypeslib.as_array(ptr, (count * n * n * 4,)).reshape(count, n, n, 4) if count else None
+
+
+@pytest.mark.parametrize("binary", [False, True])
+def test_textures_into_atlases(tmp_path, binary):
+    from test_texture_io import QUANT, _test_image, encode_jpeg, write_png
+    rng = np.random.default_rng(8)
+    img0 = write_png(rng.integers(0, 256, size=(30, 40, 3)), 2, 8)                  # base colour (sRGB)
+    img1 = write_png(rng.integers(0, 65536, size=(16, 16, 4)), 6, 16)               # metallic-roughness (linear)
+    img2, _ = encode_jpeg(_test_image(20, 24, 1)[..., 0], [(1, 1)], QUANT, grey=True)  # normal (linear)
+    img3 = write_png(rng.integers(0, 256, size=(8, 12, 2)), 4, 8)                   # emission and specular factor
+    img4 = write_png(rng.integers(0, 256, size=(5, 7, 1)), 0, 8)                    # used by no material
+    mat = {"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}, "metallicRoughnessTexture": {"index": 1}},
+           "normalTexture": {"index": 2, "scale": 0.5}, "emissiveTexture": {"index": 3},
+           "extensions": {"KHR_materials_specular": {"specularTexture": {"index": 3}}}}
+    hows = ["view", "data", "file", "view", "data"] if binary else ["data", "file", "data", "file", "data"]
+    images = list(zip([img0, img1, img2, img3, img4], hows))
+    path = write_gltf(tmp_path, [{"mesh": 0}], [0], [mat], binary, images=images)
+    w = pt.World.from_gltf(path)
+    m = w.materials()[0]
+    u = w.take_updates()
+    assert u.scene.contents.srgb_atlas_count == 1 and u.scene.contents.linear_atlas_count == 1
+    srgb, linear = _atlases(u, True), _atlases(u, False)
+    n = abi.PT_ATLAS_SIZE
+    rects = {True: [], False: []}
+
+    def check(layer, uv, enc, is_srgb):
+        want = pt.decode_texture(enc)
+        h, wd = want.shape[:2]
+        assert layer == 0
+        x, y = int(round(uv[0] * n)), int(round(uv[1] * n))
+        assert list(uv) == [np.float32(x) / n, np.float32(y) / n, np.float32(wd) / n, np.float32(h) / n]
+        atlas = srgb if is_srgb else linear
+        np.testing.assert_array_equal(atlas[0, y:y + h, x:x + wd], want)
+        rects[is_srgb].append((x, y, wd, h))
+
+    check(m.base_color_tex_layer, m.base_color_uv, img0, True)
+    check(m.metallic_roughness_tex_layer, m.metallic_roughness_uv, img1, False)
+    check(m.normal_tex_layer, m.normal_uv, img2, False)
+    check(m.emission_tex_layer, m.emission_uv, img3, True)
+    # an image in the sRGB set is not in the linear atlases: the specular-factor slot has none
+    assert m.specular_weight_tex_layer == -1 and list(m.specular_weight_uv) == [0, 0, 0, 0]
+    assert m.specular_color_tex_layer == -1
+    assert m.normal_scale == 0.5
+    # the unused image went to the linear layer too, and no two placements overlap
+    for r in rects.values():
+        for i in range(len(r)):
+            for j in range(i + 1, len(r)):
+                a, b = r[i], r[j]
+                assert a[0] + a[2] <= b[0] or b[0] + b[2] <= a[0] or a[1] + a[3] <= b[1] or b[1] + b[3] <= a[1]
+    # 16-bit RGBA keeps the high bytes; grey-alpha becomes (l, a, 0, 255)
+    d3 = pt.decode_texture(img3)
+    assert (d3[..., 2] == 0).all() and (d3[..., 3] == 255).all()
+    w.close()
+
+
+def test_atlas_packing_opens_layers(tmp_path):
+    # three 5000x5000 images cannot share an 8192^2 layer: one layer each; an image above 8192 is refused
+    big = write_png_solid(5000, 5000)
+    images = [(big, "data")] * 3
+    mat = {"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}}}
+    path = write_gltf(tmp_path, [{"mesh": 0}], [0], [mat], images=images)
+    w = pt.World.from_gltf(path)
+    u = w.take_updates()
+    assert u.scene.contents.srgb_atlas_count == 1 and u.scene.contents.linear_atlas_count == 2
+    w.close()
+    path = write_gltf(tmp_path, [{"mesh": 0}], [0], [mat], images=[(write_png_solid(8193, 2), "data")])
+    with pytest.raises(pt.PathTracerError, match="larger"):
+        pt.World.from_gltf(path)
+
+
+def write_png_solid(w, h):
+    import zlib
+    from test_texture_io import _chunk
+    raw = (b"\0" + b"\x10\x20\x30" * w) * h
+    return (b"\x89PNG\r\n\x1a\n" + _chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0))
+            + _chunk(b"IDAT", zlib.compress(raw, 1)) + _chunk(b"IEND", b""))

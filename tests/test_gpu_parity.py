@@ -205,6 +205,43 @@ def test_textured_cornell_tile_bit_exact(kernel):
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
+def test_gltf_textured_bit_exact(tmp_path, kernel):
+    """A glTF scene whose material has PNG base-colour and metallic-roughness textures and a JPEG normal
+    map, packed into the atlases by the import, under a sky: identical paths in kernels and oracle."""
+    from test_gltf import write_gltf
+    from test_texture_io import QUANT, _test_image, encode_jpeg, write_png
+    rng = np.random.default_rng(4)
+    base = write_png(rng.integers(0, 256, size=(64, 64, 3)), 2, 8)
+    mr = write_png(rng.integers(0, 65536, size=(16, 16, 4)), 6, 16)
+    normal, _ = encode_jpeg(_test_image(32, 32, 2), [(1, 1), (1, 1), (1, 1)], QUANT)
+    mat = {"pbrMetallicRoughness": {"baseColorTexture": {"index": 0}, "metallicRoughnessTexture": {"index": 1},
+                                    "metallicFactor": 0.5},
+           "normalTexture": {"index": 2, "scale": 0.8}}
+    s2 = np.sqrt(0.5)
+    nodes = [{"mesh": 0}, {"mesh": 0, "rotation": [s2, 0, 0, s2]}, {"mesh": 0, "rotation": [0, -s2, 0, s2]}]
+    path = write_gltf(tmp_path, nodes, [0, 1, 2], [mat], True, images=[(base, "view"), (mr, "view"), (normal, "view")])
+    w = pt.World.from_gltf(path)
+    w.set_aspect_ratio(1.0)
+    y, x = np.mgrid[0:32, 0:64]
+    sky = np.stack([0.5 + 0.5 * np.sin(x / 10.0), 0.6 + 0.3 * np.cos(y / 6.0), np.full((32, 64), 0.9),
+                    np.ones((32, 64))], axis=-1).astype(np.float32)
+    w.set_skybox_rgba(sky)
+    u = w.take_updates()
+    assert u.scene.contents.srgb_atlas_count == 1 and u.scene.contents.linear_atlas_count == 1
+    ow = oracle.world_from_updates(u)
+    tr = pt.PathTracer(u, (64, 64))
+    tr.set_kernel(kernel)
+    tr.set_max_bounces(4)
+    tr.set_tile((128, 128), (32, 32), (64, 64))
+    gpu = tr.trace_recorded(2)
+    _, ref = oracle.trace_paths(ow, (128, 128), 4, pixels_of((32, 32), (64, 64), (128, 128)), 1, 2, records=True)
+    assert_records_equal(gpu, ref)
+    assert (gpu["hits"] > 0).mean() > 0.5  # the camera sees the textured quads
+    tr.close()
+    w.close()
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
 def test_large_scene_fp64_rmse(large_world, kernel):
     """Config 2: relative RMSE of a 48x48 crop at 64 spp against the FP64 oracle render (same RNG streams)."""
     w, u, ow = large_world
