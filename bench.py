@@ -300,7 +300,7 @@ def oracle_sample(updates, seconds: float, threads: int = 0):
     want_rays = rate * seconds
     rays_per_px = rays / max(1, n_cal * 4) * SPP
     n_px = max(64, int(want_rays / max(rays_per_px, 1.0)))
-    stride = max(1, int(math.sqrt(WIDTH * HEIGHT / n_px)))
+    stride = max(1, math.ceil(math.sqrt(WIDTH * HEIGHT / n_px)))  # never above the time budget
     rays, dt, npx = run(stride, SPP)
     desc = f"every {stride}th pixel in x and y ({npx} pixels) x {SPP} spp of the {WIDTH}x{HEIGHT} image, {threads} threads"
     return rays / dt / 1e6, threads, desc, dt
