@@ -33,8 +33,10 @@ typedef struct ptw_world ptw_world;
 /* A triangle mesh already in world space.  Optional arrays may be NULL:
  * normals -> flat normals per triangle (world.rs:1221-1235); uvs -> the
  * repeating (0,0),(1,0),(0,1) pattern (world.rs:1107-1111, 1170-1175);
- * tangents -> a per-triangle tangent from the UV gradient, handedness -1
- * (the reference runs MikkTSpace here, world.rs:1238-1260). */
+ * tangents -> MikkTSpace frames per corner with the handedness negated, as
+ * the reference computes them (world.rs:1238-1260); so are given tangents
+ * that hold the (1, 0, 0, 1) placeholder or mix handedness within a
+ * triangle (world.rs:1188-1217). */
 typedef struct ptw_mesh {
     const float* positions;  /* vertex_count * 3 */
     const float* normals;    /* vertex_count * 3 or NULL */

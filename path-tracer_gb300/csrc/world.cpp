@@ -15,6 +15,7 @@
 
 #include "../../include/pt_world.h"
 #include "pt_fmath.h"
+#include "pt_mikktspace.h"
 
 namespace {
 
@@ -615,6 +616,23 @@ int ptw_add_mesh(ptw_world* w, const ptw_mesh* mesh) {
     auto UV = [&](uint32_t i, int c) {
         return mesh->uvs ? mesh->uvs[2 * i + c] : dummy_uv[i % 3][c];
     };
+    // MikkTSpace frames per corner where the mesh has no usable tangents (world.rs:1238-1260)
+    std::vector<float> mikk;
+    if (computed_tangents) {
+        const size_t tris = idx.size() / 3;
+        std::vector<float> cp(tris * 9), cn(tris * 9), cu(tris * 6);
+        for (size_t c = 0; c < idx.size(); ++c) {
+            const uint32_t v = idx[c];
+            for (int k = 0; k < 3; ++k) cp[3 * c + k] = mesh->positions[3 * v + k];
+            cn[3 * c] = normals[v].x;
+            cn[3 * c + 1] = normals[v].y;
+            cn[3 * c + 2] = normals[v].z;
+            cu[2 * c] = UV(v, 0);
+            cu[2 * c + 1] = UV(v, 1);
+        }
+        mikk.resize(tris * 12);
+        ptw::mikktspace_tangents(tris, cp.data(), cn.data(), cu.data(), mikk.data());
+    }
     for (size_t t = 0; t + 2 < idx.size(); t += 3) {
         const uint32_t i0 = idx[t], i1 = idx[t + 1], i2 = idx[t + 2];
         const Vec3 a = P(i0), b = P(i1), c = P(i2);
@@ -646,27 +664,13 @@ int ptw_add_mesh(ptw_world* w, const ptw_mesh* mesh) {
                 ts[k][3] = src[3];
             }
         } else {
-            // per-triangle tangent from the UV gradient (stand-in for MikkTSpace)
-            const Vec3 e1 = b - a, e2 = c - a;
-            const float du1 = uvs[1][0] - uvs[0][0], dv1 = uvs[1][1] - uvs[0][1];
-            const float du2 = uvs[2][0] - uvs[0][0], dv2 = uvs[2][1] - uvs[0][1];
-            const float det = du1 * dv2 - du2 * dv1;
-            Vec3 tan = v3(1, 0, 0);
-            float sign = 1.0f;
-            if (det != 0.0f && std::isfinite(det)) {
-                const float r = 1.0f / det;
-                Vec3 tt = (e1 * dv2 - e2 * dv1) * r;
-                Vec3 bb = (e2 * du1 - e1 * du2) * r;
-                if (dot(tt, tt) > 0.0f) {
-                    tan = normalize(tt);
-                    sign = dot(cross(tri_normal(a, b, c), tan), bb) < 0.0f ? -1.0f : 1.0f;
-                }
-            }
+            // the handedness is negated after MikkTSpace, world.rs:1252-1259
             for (int k = 0; k < 3; ++k) {
-                ts[k][0] = tan.x;
-                ts[k][1] = tan.y;
-                ts[k][2] = tan.z;
-                ts[k][3] = -sign;  // handedness negated as in world.rs:1257-1259
+                const float* m = &mikk[4 * (t + (size_t)k)];
+                ts[k][0] = m[0];
+                ts[k][1] = m[1];
+                ts[k][2] = m[2];
+                ts[k][3] = -m[3];
             }
         }
         w->in_geos.push_back(g);
