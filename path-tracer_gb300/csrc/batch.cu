@@ -137,13 +137,15 @@ __global__ void reset_kernel(uint32_t* cnt, int next) {
 }
 
 template <bool kAlpha, bool kWide>
-__global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : 1) extend_kernel(const SceneDev* scenes, WaveBufs b, int cur,
+__global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : PT_EXTEND_MIN_BLOCKS) extend_kernel(const SceneDev* scenes, WaveBufs b, int cur,
                                                                 uint32_t steps_per_refill) {
     static_assert(!(kAlpha && kWide), "the wide form runs opaque scenes only");
     const Stage st = stage_of(b.q, cur);
     const uint32_t count = *st.count;
     typename std::conditional<kWide, WideTraverser<false>, Traverser<false, kAlpha, false>>::type tr;
-    uint2 stack[64];
+    __shared__ uint2 stack_top[kSmemStack > 0u ? kSmemStack * kExtendThreads : 1u];
+    LaneStack<kExtendThreads> stack;
+    stack.col = stack_top + threadIdx.x;
     uint32_t istack[1];
     const SceneDev* sc = scenes;
     uint32_t slot = 0;
@@ -229,11 +231,13 @@ __global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kern
 }
 
 template <bool kWide>
-__global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : 1) shadow_kernel(const SceneDev* scenes, WaveBufs b,
+__global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : PT_EXTEND_MIN_BLOCKS) shadow_kernel(const SceneDev* scenes, WaveBufs b,
                                                                 uint32_t steps_per_refill) {
     const uint32_t count = b.q.cnt[2];
     typename std::conditional<kWide, WideTraverser<true>, Traverser<false, false, true>>::type tr;
-    uint2 stack[64];
+    __shared__ uint2 stack_top[kSmemStack > 0u ? kSmemStack * kExtendThreads : 1u];
+    LaneStack<kExtendThreads> stack;
+    stack.col = stack_top + threadIdx.x;
     uint32_t istack[1];
     const SceneDev* sc = scenes;
     uint32_t path = 0;

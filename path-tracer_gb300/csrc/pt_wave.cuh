@@ -66,8 +66,9 @@ PTD Stage stage_of(const Queues& q, int cur) {
 #ifndef PT_EXTEND_THREADS
 #define PT_EXTEND_THREADS 128
 #endif
+// 9 resident blocks of the traversal kernels per SM: at most 56 registers, no spills
 #ifndef PT_EXTEND_MIN_BLOCKS
-#define PT_EXTEND_MIN_BLOCKS 1
+#define PT_EXTEND_MIN_BLOCKS 9
 #endif
 #ifndef PT_SHADE_THREADS
 #define PT_SHADE_THREADS 128
@@ -101,6 +102,37 @@ constexpr uint32_t kWideLeafMerge = PT_WIDE_LEAF_MERGE;
 #endif
 constexpr int kExtendThreads = PT_EXTEND_THREADS;
 constexpr int kShadeThreads = PT_SHADE_THREADS;
+// entries at the top of each traversal lane's stack kept in shared memory
+#ifndef PT_SMEM_STACK
+#define PT_SMEM_STACK 8
+#endif
+constexpr uint32_t kSmemStack = PT_SMEM_STACK;
+
+// The deferred stack of one traversal lane: 64 entries in the lane's local
+// memory, of which the first kSmemStack live in the block's shared memory
+// instead (one column per thread, so a warp touches consecutive words).
+template <uint32_t kThreads>
+struct LaneStack {
+    uint2* col;  // &shared[threadIdx.x]; entry i at col[i * kThreads]
+    uint2 deep[64];
+    PTD void put(uint32_t i, uint2 e) {
+        if (kSmemStack > 0u && i < kSmemStack)
+            col[i * kThreads] = e;
+        else
+            deep[i & 63u] = e;
+    }
+    PTD uint2 get(uint32_t i) const {
+        if (kSmemStack > 0u && i < kSmemStack) return col[i * kThreads];
+        return deep[i & 63u];
+    }
+};
+
+// the whole stack in local memory
+struct LocalStack {
+    uint2 deep[64];
+    PTD void put(uint32_t i, uint2 e) { deep[i & 63u] = e; }
+    PTD uint2 get(uint32_t i) const { return deep[i & 63u]; }
+};
 
 PTD Tri load_tri4(const Fast& f, uint32_t tri) {
     const float4* p = f.tri4 + 3 * (size_t)tri;
@@ -162,10 +194,11 @@ struct Traverser {
         }
     }
 
-    PTD bool pop(uint2* stack, uint32_t* istack) {
+    template <class S>
+    PTD bool pop(S& stack, uint32_t* istack) {
         if (sp == 0u) return true;
         sp -= 1u;
-        const uint2 e = stack[sp & 63u];
+        const uint2 e = stack.get(sp);
         lf = e.x;
         tc = e.y;
         if constexpr (kRec) idx = istack[sp & 63u];
@@ -205,7 +238,8 @@ struct Traverser {
     // has finished (for kShadow, hit == 1 marks an occluder).  Testing a
     // leaf's triangles one per step keeps the two divergent paths of a warp
     // (box pair vs triangle) about equally long.
-    PTD bool step(const World& w, const Fast& f, uint2* stack, uint32_t* istack) {
+    template <class S>
+    PTD bool step(const World& w, const Fast& f, S& stack, uint32_t* istack) {
         if (tri_left == 0u) {
             rec.visit(idx);
             if (tc == 0u) {
@@ -219,7 +253,7 @@ struct Traverser {
                     const bool go_left = hl && (!hr || dl < dr);
                     if (hl && hr) {
                         const float4 f0 = go_left ? r0 : l0, f1 = go_left ? r1 : l1;
-                        stack[sp & 63u] = make_uint2(__float_as_uint(f0.w), __float_as_uint(f1.w));
+                        stack.put(sp, make_uint2(__float_as_uint(f0.w), __float_as_uint(f1.w)));
                         if constexpr (kRec) istack[sp & 63u] = go_left ? lf + 1u : lf;
                         sp += 1u;
                     }
@@ -246,7 +280,8 @@ struct Traverser {
 #else
     // one node visit; true when the traversal has finished (for kShadow,
     // hit == 1 marks an occluder)
-    PTD bool step(const World& w, const Fast& f, uint2* stack, uint32_t* istack) {
+    template <class S>
+    PTD bool step(const World& w, const Fast& f, S& stack, uint32_t* istack) {
         rec.visit(idx);
         if (tc > 0u) {
             rec.leaf();
@@ -289,7 +324,7 @@ struct Traverser {
                 const bool go_left = hl && (!hr || dl < dr);
                 if (hl && hr) {
                     const float4 f0 = go_left ? r0 : l0, f1 = go_left ? r1 : l1;
-                    stack[sp & 63u] = make_uint2(__float_as_uint(f0.w), __float_as_uint(f1.w));
+                    stack.put(sp, make_uint2(__float_as_uint(f0.w), __float_as_uint(f1.w)));
                     if constexpr (kRec) istack[sp & 63u] = go_left ? lf + 1u : lf;
                     sp += 1u;
                 }
@@ -531,13 +566,14 @@ struct WideTraverser {
     }
 
     // one node visit or one triangle test; true when the traversal has finished
-    PTD bool step(const World& w, const Fast& f, uint2* stack, uint32_t*) {
+    template <class S>
+    PTD bool step(const World& w, const Fast& f, S& stack, uint32_t*) {
         if (tri_left == 0u) {
             uint32_t cnt = list >> 24;
             if (cnt == 0u) {
                 if (sp == 0u) return true;
                 sp -= 1u;
-                const uint2 e = stack[sp & 63u];
+                const uint2 e = stack.get(sp);
                 node = e.x;
                 list = e.y;
                 cnt = list >> 24;
@@ -549,7 +585,7 @@ struct WideTraverser {
             const uint32_t tc = __ldg(reinterpret_cast<const unsigned short*>(p + 6) + k);
             if (tc == 0u) {
                 if (cnt > 1u) {
-                    stack[sp & 63u] = make_uint2(node, list);
+                    stack.put(sp, make_uint2(node, list));
                     sp += 1u;
                 }
                 node = child;

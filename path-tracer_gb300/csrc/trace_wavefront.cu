@@ -90,7 +90,9 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
     const Stage st = stage_of(q, cur);
     const uint32_t count = *st.count;
     typename std::conditional<kWide, WideTraverser<false, kTri36>, Traverser<kRec, kAlpha, false, kTri36>>::type tr;
-    uint2 stack[64];
+    __shared__ uint2 stack_top[kSmemStack > 0u ? kSmemStack * kExtendThreads : 1u];
+    LaneStack<kExtendThreads> stack;
+    stack.col = stack_top + threadIdx.x;
     uint32_t istack[kRec ? 64 : 1];
     uint32_t slot = 0, path = 0;
     __shared__ FilerSlots<kExtendThreads> filer_slots;
@@ -187,7 +189,9 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
     static_assert(!(kWide && kRec), "the wide form keeps no records");
     const uint32_t count = q.cnt[2];
     typename std::conditional<kWide, WideTraverser<true, kTri36>, Traverser<kRec, false, true, kTri36>>::type tr;
-    uint2 stack[64];
+    __shared__ uint2 stack_top[kSmemStack > 0u ? kSmemStack * kExtendThreads : 1u];
+    LaneStack<kExtendThreads> stack;
+    stack.col = stack_top + threadIdx.x;
     uint32_t istack[kRec ? 64 : 1];
     uint32_t path = 0;
     float4 contribution = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -329,7 +333,7 @@ __global__ void debug_intersect_wide_kernel(World w, Fast f, uint64_t n, const f
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     WideTraverser<false> tr;
-    uint2 stack[64];
+    LocalStack stack;
     tr.init(f, mk(origins[3 * i], origins[3 * i + 1], origins[3 * i + 2]),
             mk(directions[3 * i], directions[3 * i + 1], directions[3 * i + 2]), t_max ? t_max[i] : kFltMax, -1);
     while (!tr.step(w, f, stack, nullptr)) {
