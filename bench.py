@@ -91,6 +91,22 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
 
+def max_over_ranks(x: float, pg, device: str) -> float:
+    """The largest value of `x` over the replicas (a job's time is its slowest replica's);
+    `pg` is torch.distributed when more than one replica runs, else None."""
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_step: float, steps: int, world_size: int, seconds: float) -> float:
+    """Whole-job throughput: every replica processes `units_per_step` per step (weak scaling)."""
+    return units_per_step * steps * world_size / seconds
+
+
 def workload_config(world, kernel: str) -> dict:
     return {
         "workload": f"{WORKLOADS[WORKLOAD]['text']}, {WIDTH}x{HEIGHT}, {SPP} spp, max_bounces 8, one image per step",
@@ -404,12 +420,10 @@ def run_ours(args):
     launches = tracer.launch_count() - launches0
     times = tracer.kernel_times()
     tracer.set_profiling(False)
+    elapsed_ms = max_over_ranks(elapsed_ms, pg, "cuda")
     if pg:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
         pg.barrier()
-    value = rays_per_step * args.steps * world_size / (elapsed_ms / 1e3) / 1e6
+    value = job_rate(rays_per_step, args.steps, world_size, elapsed_ms / 1e3) / 1e6
 
     # dominant kernel and its roofline
     cls = max(times.milliseconds, key=lambda k: times.milliseconds[k])
@@ -433,18 +447,16 @@ def run_ours(args):
     step()
     tracer.display_tile()
     torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
     t0 = time.perf_counter()
     e2e_steps = max(1, args.e2e_steps)
     for _ in range(e2e_steps):
         tracer.apply_updates(pinned)
         step()
         tracer.display_tile()
-    e2e_s = time.perf_counter() - t0
-    e2e_value = rays_per_step * e2e_steps / e2e_s / 1e6
-    if pg:
-        t = torch.tensor([e2e_s], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_value = rays_per_step * e2e_steps * world_size / float(t.item()) / 1e6
+    e2e_s = max_over_ranks(time.perf_counter() - t0, pg, "cuda")
+    e2e_value = job_rate(rays_per_step, e2e_steps, world_size, e2e_s) / 1e6
 
     latency = None
     if rank == 0 and world_size == 1 and not args.no_latency:
@@ -462,7 +474,8 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
             "config": dict(workload_config(world, args.kernel), precision=args.precision,
                            parallelism=f"replicas x{world_size}"),
-            "rays_per_step": rays_per_step, "samples_per_s": paths_per_step * args.steps * world_size / (elapsed_ms / 1e3),
+            "rays_per_step": rays_per_step, "samples_per_s": job_rate(paths_per_step, args.steps, world_size,
+                                                                     elapsed_ms / 1e3),
             # whole-pass algorithmic bytes per ray and the Mrays/s they would allow at the HBM peak
             "bytes_per_ray": bytes_per_step["total"] / rays_per_step,
             "hbm_roofline_mrays": peak * 1e9 / (bytes_per_step["total"] / rays_per_step) / 1e6,
