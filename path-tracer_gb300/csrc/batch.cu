@@ -143,8 +143,9 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
     const Stage st = stage_of(b.q, cur);
     const uint32_t count = *st.count;
     typename std::conditional<kWide, WideTraverser<false>, Traverser<false, kAlpha, false>>::type tr;
-    __shared__ uint2 stack_top[kSmemStack > 0u ? kSmemStack * kExtendThreads : 1u];
-    LaneStack<kExtendThreads> stack;
+    constexpr uint32_t kShared = kWide ? kWideSmemStack : kSmemStack;
+    __shared__ uint2 stack_top[kShared > 0u ? kShared * kExtendThreads : 1u];
+    LaneStack<kExtendThreads, kShared> stack;
     stack.col = stack_top + threadIdx.x;
     uint32_t istack[1];
     const SceneDev* sc = scenes;
@@ -235,8 +236,9 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
                                                                 uint32_t steps_per_refill) {
     const uint32_t count = b.q.cnt[2];
     typename std::conditional<kWide, WideTraverser<true>, Traverser<false, false, true>>::type tr;
-    __shared__ uint2 stack_top[kSmemStack > 0u ? kSmemStack * kExtendThreads : 1u];
-    LaneStack<kExtendThreads> stack;
+    constexpr uint32_t kShared = kWide ? kWideSmemStack : kSmemStack;
+    __shared__ uint2 stack_top[kShared > 0u ? kShared * kExtendThreads : 1u];
+    LaneStack<kExtendThreads, kShared> stack;
     stack.col = stack_top + threadIdx.x;
     uint32_t istack[1];
     const SceneDev* sc = scenes;

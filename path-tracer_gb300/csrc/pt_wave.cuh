@@ -107,22 +107,27 @@ constexpr int kShadeThreads = PT_SHADE_THREADS;
 #define PT_SMEM_STACK 8
 #endif
 constexpr uint32_t kSmemStack = PT_SMEM_STACK;
+// the same for the 8-wide traversal kernels
+#ifndef PT_WIDE_SMEM_STACK
+#define PT_WIDE_SMEM_STACK 8
+#endif
+constexpr uint32_t kWideSmemStack = PT_WIDE_SMEM_STACK;
 
 // The deferred stack of one traversal lane: 64 entries in the lane's local
-// memory, of which the first kSmemStack live in the block's shared memory
+// memory, of which the first kShared live in the block's shared memory
 // instead (one column per thread, so a warp touches consecutive words).
-template <uint32_t kThreads>
+template <uint32_t kThreads, uint32_t kShared>
 struct LaneStack {
     uint2* col;  // &shared[threadIdx.x]; entry i at col[i * kThreads]
     uint2 deep[64];
     PTD void put(uint32_t i, uint2 e) {
-        if (kSmemStack > 0u && i < kSmemStack)
+        if (kShared > 0u && i < kShared)
             col[i * kThreads] = e;
         else
             deep[i & 63u] = e;
     }
     PTD uint2 get(uint32_t i) const {
-        if (kSmemStack > 0u && i < kSmemStack) return col[i * kThreads];
+        if (kShared > 0u && i < kShared) return col[i * kThreads];
         return deep[i & 63u];
     }
 };

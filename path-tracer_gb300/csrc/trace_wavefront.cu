@@ -90,8 +90,9 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
     const Stage st = stage_of(q, cur);
     const uint32_t count = *st.count;
     typename std::conditional<kWide, WideTraverser<false, kTri36>, Traverser<kRec, kAlpha, false, kTri36>>::type tr;
-    __shared__ uint2 stack_top[kSmemStack > 0u ? kSmemStack * kExtendThreads : 1u];
-    LaneStack<kExtendThreads> stack;
+    constexpr uint32_t kShared = kWide ? kWideSmemStack : kSmemStack;
+    __shared__ uint2 stack_top[kShared > 0u ? kShared * kExtendThreads : 1u];
+    LaneStack<kExtendThreads, kShared> stack;
     stack.col = stack_top + threadIdx.x;
     uint32_t istack[kRec ? 64 : 1];
     uint32_t slot = 0, path = 0;
@@ -189,8 +190,9 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
     static_assert(!(kWide && kRec), "the wide form keeps no records");
     const uint32_t count = q.cnt[2];
     typename std::conditional<kWide, WideTraverser<true, kTri36>, Traverser<kRec, false, true, kTri36>>::type tr;
-    __shared__ uint2 stack_top[kSmemStack > 0u ? kSmemStack * kExtendThreads : 1u];
-    LaneStack<kExtendThreads> stack;
+    constexpr uint32_t kShared = kWide ? kWideSmemStack : kSmemStack;
+    __shared__ uint2 stack_top[kShared > 0u ? kShared * kExtendThreads : 1u];
+    LaneStack<kExtendThreads, kShared> stack;
     stack.col = stack_top + threadIdx.x;
     uint32_t istack[kRec ? 64 : 1];
     uint32_t path = 0;
