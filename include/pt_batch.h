@@ -17,13 +17,18 @@
  *     ring; every wave a planner kernel packs queued items into a fixed path
  *     budget and the wavefront kernels trace them together, whatever job they
  *     belong to; work submitted while a wave runs joins the next wave;
- *   - each wave is replayed from a captured CUDA graph.
+ *   - each wave is replayed from a captured CUDA graph;
+ *   - a background thread of the engine harvests finished waves and queues
+ *     the next ones every 100 us, so the GPU stays fed while the caller's
+ *     thread is busy between calls (at most two waves in flight).
  * Every path computes exactly what pt_trace computes for the same pixel and
  * sample, and each pixel accumulates its samples in order, so a job's result
  * is bit-identical whether it runs alone or mixed with others.
  *
  * All functions return PT_OK or an error code from pt.h; pte_last_error gives
- * the message.  An engine is not thread-safe.
+ * the message.  Calls on one engine may come from several threads; they are
+ * serialised with the background thread by a lock.  An error of the
+ * background thread is returned by every later call.
  */
 #ifndef PT_BATCH_H
 #define PT_BATCH_H

@@ -7,6 +7,7 @@
 // is one captured CUDA graph.  Host side: the scene cache (content hash, HBM
 // budget, LRU eviction), jobs and their resident accumulation buffers, the
 // ring producer, wave launching and completion polling, and the autotuner.
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -14,6 +15,7 @@
 #include <deque>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -350,6 +352,32 @@ struct Buf {
     }
 };
 
+// A device buffer allocated and freed in stream order from the engine's
+// memory pool: neither call synchronises the device, so per-job buffers come
+// and go while waves run (cudaFree would wait for the whole GPU).
+struct StreamBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaStream_t stream = nullptr;
+    cudaError_t alloc(size_t n, cudaMemPool_t pool, cudaStream_t s) {
+        release();
+        stream = s;
+        cudaError_t e = cudaMallocFromPoolAsync(&p, n ? n : 16, pool, s);
+        if (e == cudaSuccess) bytes = n ? n : 16;
+        return e;
+    }
+    void release() {
+        if (p) cudaFreeAsync(p, stream);
+        p = nullptr;
+        bytes = 0;
+    }
+    ~StreamBuf() { release(); }
+    template <class T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
 struct Scene {
     uint64_t id = 0;
     uint32_t slot = 0;
@@ -370,7 +398,7 @@ struct Accumulation {
     bool busy = false;
     uint64_t bytes = 0;
     int job_refs = 0;
-    Buf accum, image, comp;
+    StreamBuf accum, image, comp;
     std::deque<uint64_t> waiting;  // jobs queued behind the running pass
 };
 
@@ -422,6 +450,7 @@ struct pt_engine {
     pt_engine_config cfg{};
     std::string error;
     cudaStream_t stream = nullptr;
+    cudaMemPool_t pool = nullptr;  // per-job buffers, kept cached (release threshold: never)
     int sms = 0;
     uint64_t budget = 0, used = 0;
     // scenes
@@ -453,6 +482,12 @@ struct pt_engine {
     std::deque<Flight> flights;
     std::vector<cudaEvent_t> event_pool;
     pt_engine_stats stats{};
+    // a background thread keeps waves queued on the stream (harvest + pump)
+    // whatever the caller's thread is doing; every entry point takes `mu`
+    mutable std::recursive_mutex mu;
+    std::thread pumper;
+    std::atomic<bool> stop{false};
+    int sticky = PT_OK;  // first error of the background thread, returned by later calls
 
     int fail(int code, const std::string& m) {
         error = m;
@@ -872,6 +907,24 @@ bool evict_one(pt_engine* e) {
 
 }  // namespace
 
+// The background pump: every 100 us, finished waves are harvested and new
+// ones queued, so the stream never runs dry while the caller is busy between
+// calls (two waves in flight at most).
+static void pump_loop(pt_engine* e) {
+    cudaSetDevice(e->cfg.device);
+    while (!e->stop.load(std::memory_order_relaxed)) {
+        {
+            std::lock_guard<std::recursive_mutex> g(e->mu);
+            if (e->sticky == PT_OK) {
+                int rc = harvest(e, false);
+                if (!rc) rc = pump(e);
+                if (rc) e->sticky = rc;
+            }
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(100));
+    }
+}
+
 extern "C" {
 
 int pte_create(const pt_engine_config* cfg, pt_engine** out) {
@@ -893,6 +946,15 @@ int pte_create(const pt_engine_config* cfg, pt_engine** out) {
     if (!rc) rc = e->cuda(cudaSetDevice(e->cfg.device), "cudaSetDevice");
     if (!rc) rc = e->cuda(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "stream");
     if (!rc) rc = e->cuda(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, e->cfg.device), "SM count");
+    if (!rc) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = e->cfg.device;
+        rc = e->cuda(cudaMemPoolCreate(&e->pool, &props), "memory pool");
+        uint64_t keep = ~0ull;
+        if (!rc) rc = e->cuda(cudaMemPoolSetAttribute(e->pool, cudaMemPoolAttrReleaseThreshold, &keep), "memory pool");
+    }
     if (!rc) rc = e->cuda(e->d_scenes.alloc(kMaxScenes * sizeof(SceneDev)), "scene table");
     if (!rc) rc = e->cuda(e->d_jobs.alloc((size_t)kMaxSlots * sizeof(JobDev)), "job table");
     if (!rc) rc = e->cuda(e->d_done.alloc((size_t)kMaxSlots * 4), "job counters");
@@ -916,12 +978,15 @@ int pte_create(const pt_engine_config* cfg, pt_engine** out) {
         pte_destroy(e);
         return rc;
     }
+    e->pumper = std::thread(pump_loop, e);
     *out = e;
     return PT_OK;
 }
 
 void pte_destroy(pt_engine* e) {
     if (!e) return;
+    e->stop.store(true);
+    if (e->pumper.joinable()) e->pumper.join();
     cudaSetDevice(e->cfg.device);
     if (e->stream) cudaStreamSynchronize(e->stream);
     drop_graphs(e);
@@ -933,16 +998,24 @@ void pte_destroy(pt_engine* e) {
     e->jobs.clear();
     for (auto& s : e->slots) s.reset();
     e->scenes.clear();
+    if (e->stream) cudaStreamSynchronize(e->stream);  // the stream-ordered frees above
+    if (e->pool) cudaMemPoolDestroy(e->pool);
     if (e->h_done) cudaFreeHost(e->h_done);
     if (e->h_ctrl) cudaFreeHost(e->h_ctrl);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
 }
 
-const char* pte_last_error(const pt_engine* e) { return e ? e->error.c_str() : "null engine"; }
+const char* pte_last_error(const pt_engine* e) {
+    if (!e) return "null engine";
+    std::lock_guard<std::recursive_mutex> lock(e->mu);
+    return e->error.c_str();
+}
 
 int pte_scene_add(pt_engine* e, const pt_world_updates* u, uint64_t* scene_id) {
     if (!e || !u || !scene_id) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lock(e->mu);
+    if (e->sticky) return e->sticky;
     if (!u->scene || !u->skybox || !u->scene_uniforms || !u->skybox_uniforms || !u->scene_alias_table)
         return e->fail(PT_ERR_INVALID_ARG, "a scene needs a full upload (scene, skybox, uniforms, alias table)");
     cudaSetDevice(e->cfg.device);
@@ -1062,6 +1135,8 @@ int pte_scene_add(pt_engine* e, const pt_world_updates* u, uint64_t* scene_id) {
 
 int pte_scene_release(pt_engine* e, uint64_t scene_id) {
     if (!e) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lock(e->mu);
+    if (e->sticky) return e->sticky;
     auto it = e->scenes.find(scene_id);
     if (it == e->scenes.end()) return e->fail(PT_ERR_INVALID_ARG, "unknown scene");
     it->second->caller_refs -= 1;
@@ -1070,6 +1145,8 @@ int pte_scene_release(pt_engine* e, uint64_t scene_id) {
 
 int pte_submit(pt_engine* e, const pt_job_desc* d, uint64_t* job_id) {
     if (!e || !d || !job_id) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lock(e->mu);
+    if (e->sticky) return e->sticky;
     cudaSetDevice(e->cfg.device);
     if (d->samples == 0 || d->max_bounces > PT_MAX_BOUNCES_LIMIT)
         return e->fail(PT_ERR_INVALID_ARG, "samples must be positive and max_bounces at most 16");
@@ -1108,9 +1185,9 @@ int pte_submit(pt_engine* e, const pt_job_desc* d, uint64_t* job_id) {
         a->max_bounces = d->max_bounces;
         a->bytes = bytes;
         const size_t plane = (size_t)d->width * d->height * 16;
-        int rc = e->cuda(a->accum.alloc(plane), "accumulation buffer");
-        if (!rc) rc = e->cuda(a->image.alloc(plane), "image buffer");
-        if (!rc && kahan) rc = e->cuda(a->comp.alloc(plane), "Kahan compensation");
+        int rc = e->cuda(a->accum.alloc(plane, e->pool, e->stream), "accumulation buffer");
+        if (!rc) rc = e->cuda(a->image.alloc(plane, e->pool, e->stream), "image buffer");
+        if (!rc && kahan) rc = e->cuda(a->comp.alloc(plane, e->pool, e->stream), "Kahan compensation");
         if (rc) return rc;
         e->used += bytes;
         e->slots[slot] = a;
@@ -1142,14 +1219,18 @@ int pte_poll(pt_engine* e, uint32_t timeout_ms, uint64_t* done, uint32_t capacit
     *count = 0;
     const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
     for (;;) {
-        int rc = harvest(e, false);
-        if (!rc) rc = pump(e);
-        if (rc) return rc;
-        while (*count < capacity && !e->done_unreported.empty()) {
-            done[(*count)++] = e->done_unreported.front();
-            e->done_unreported.pop_front();
+        {
+            std::lock_guard<std::recursive_mutex> lock(e->mu);
+            if (e->sticky) return e->sticky;
+            int rc = harvest(e, false);
+            if (!rc) rc = pump(e);
+            if (rc) return rc;
+            while (*count < capacity && !e->done_unreported.empty()) {
+                done[(*count)++] = e->done_unreported.front();
+                e->done_unreported.pop_front();
+            }
+            if (*count > 0 || e->flights.empty() || std::chrono::steady_clock::now() >= deadline) return PT_OK;
         }
-        if (*count > 0 || e->flights.empty() || std::chrono::steady_clock::now() >= deadline) return PT_OK;
         std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
 }
@@ -1159,19 +1240,26 @@ int pte_wait_idle(pt_engine* e, uint32_t timeout_ms) {
     cudaSetDevice(e->cfg.device);
     const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
     for (;;) {
-        int rc = harvest(e, false);
-        if (!rc) rc = pump(e);
-        if (rc) return rc;
-        bool busy = !e->flights.empty();
-        for (auto& [id, j] : e->jobs) busy |= j.status != PT_JOB_DONE;
-        if (!busy) return PT_OK;
-        if (timeout_ms && std::chrono::steady_clock::now() >= deadline) return e->fail(PT_ERR_TIMEOUT, "engine still busy");
+        {
+            std::lock_guard<std::recursive_mutex> lock(e->mu);
+            if (e->sticky) return e->sticky;
+            int rc = harvest(e, false);
+            if (!rc) rc = pump(e);
+            if (rc) return rc;
+            bool busy = !e->flights.empty();
+            for (auto& [id, j] : e->jobs) busy |= j.status != PT_JOB_DONE;
+            if (!busy) return PT_OK;
+            if (timeout_ms && std::chrono::steady_clock::now() >= deadline)
+                return e->fail(PT_ERR_TIMEOUT, "engine still busy");
+        }
         std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
 }
 
 int pte_job_status(pt_engine* e, uint64_t id, int* status, uint32_t* samples_done) {
     if (!e) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lock(e->mu);
+    if (e->sticky) return e->sticky;
     auto it = e->jobs.find(id);
     if (it == e->jobs.end()) return e->fail(PT_ERR_INVALID_ARG, "unknown job");
     if (status) *status = it->second.status;
@@ -1182,6 +1270,8 @@ int pte_job_status(pt_engine* e, uint64_t id, int* status, uint32_t* samples_don
 int pte_job_read(pt_engine* e, uint64_t id, int which, float* host) {
     if (!e || !host || (which != PT_TILE_IMAGE && which != PT_TILE_ACCUMULATION && which != PT_TILE_COMPENSATION))
         return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lock(e->mu);
+    if (e->sticky) return e->sticky;
     cudaSetDevice(e->cfg.device);
     auto it = e->jobs.find(id);
     if (it == e->jobs.end() || !it->second.acc) return e->fail(PT_ERR_INVALID_ARG, "unknown job");
@@ -1191,7 +1281,7 @@ int pte_job_read(pt_engine* e, uint64_t id, int which, float* host) {
         memset(host, 0, (size_t)a.width * a.height * 16);
         return PT_OK;
     }
-    const Buf& b = which == PT_TILE_IMAGE ? a.image : (which == PT_TILE_ACCUMULATION ? a.accum : a.comp);
+    const StreamBuf& b = which == PT_TILE_IMAGE ? a.image : (which == PT_TILE_ACCUMULATION ? a.accum : a.comp);
     int rc = e->cuda(cudaMemcpyAsync(host, b.p, (size_t)a.width * a.height * 16, cudaMemcpyDeviceToHost, e->stream), "job readback");
     if (!rc) rc = e->cuda(cudaStreamSynchronize(e->stream), "job readback");
     return rc;
@@ -1199,6 +1289,8 @@ int pte_job_read(pt_engine* e, uint64_t id, int which, float* host) {
 
 int pte_job_release(pt_engine* e, uint64_t id) {
     if (!e) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lock(e->mu);
+    if (e->sticky) return e->sticky;
     cudaSetDevice(e->cfg.device);
     auto it = e->jobs.find(id);
     if (it == e->jobs.end()) return e->fail(PT_ERR_INVALID_ARG, "unknown job");
@@ -1217,6 +1309,7 @@ int pte_job_release(pt_engine* e, uint64_t id) {
 
 int pte_stats(pt_engine* e, pt_engine_stats* s) {
     if (!e || !s) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lock(e->mu);
     *s = e->stats;
     s->scenes_cached = e->scenes.size();
     s->hbm_used = e->used;
@@ -1232,6 +1325,8 @@ int pte_stats(pt_engine* e, pt_engine_stats* s) {
 
 int pte_autotune(pt_engine* e, const pt_job_desc* jobs, uint32_t count, pt_engine_config* chosen) {
     if (!e || !jobs || count == 0) return PT_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lock(e->mu);
+    if (e->sticky) return e->sticky;
     cudaSetDevice(e->cfg.device);
     int rc = pte_wait_idle(e, 0);
     if (rc) return rc;

@@ -20,6 +20,7 @@ import ctypes as C
 import json
 import math
 import time
+from collections import OrderedDict
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -104,10 +105,14 @@ class Server:
             self._last[name] = abi.Camera.from_buffer_copy(u.camera.contents)
         return abi.Camera.from_buffer_copy(self._last[name])
 
-    def run(self, requests: list[Request], max_outstanding_paths: int = 2_000_000_000) -> ServeResult:
+    def run(self, requests: list[Request], max_outstanding_paths: int = 2_000_000_000,
+            keep_finished: int = 256) -> ServeResult:
+        """Serve the stream.  The `keep_finished` most recently finished jobs stay resident (their
+        accumulations can be refined by later progressive requests); older ones are released."""
         eng, res = self.engine, ServeResult()
         arrival_of, is_512_16, paths_of = {}, {}, {}
         finished: dict[tuple, list[int]] = {}  # (scene, w, h, depth) -> finished job ids to refine
+        kept: OrderedDict[int, tuple] = OrderedDict()  # the same jobs, oldest first
         outstanding, i = 0, 0
         t0 = time.perf_counter()
         while i < len(requests) or arrival_of:
@@ -119,6 +124,7 @@ class Server:
                 cont = 0
                 if r.progressive and finished.get(key):
                     cont = finished[key].pop()
+                    del kept[cont]
                 paths = r.width * r.height * r.samples
                 if outstanding + paths > max_outstanding_paths:
                     res.rejected += 1
@@ -147,8 +153,11 @@ class Server:
                 if cont:
                     eng.release(cont)
                 finished.setdefault(key, []).append(jid)
-                while len(finished[key]) > 4:
-                    eng.release(finished[key].pop(0))
+                kept[jid] = key
+                while len(kept) > keep_finished:
+                    old_jid, old_key = kept.popitem(last=False)
+                    finished[old_key].remove(old_jid)
+                    eng.release(old_jid)
         res.wall_s = time.perf_counter() - t0
         for ids in finished.values():
             for jid in ids:
