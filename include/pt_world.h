@@ -72,6 +72,10 @@ int ptw_add_atlas_layer(ptw_world* world, int srgb, const uint8_t* rgba8, int32_
  * image.  Call before ptw_build.  On failure `error` (if given) receives the
  * reason. */
 int ptw_load_gltf(ptw_world* world, const char* path, char* error, size_t error_size);
+/* the same from a .glb (or self-contained .gltf) held in memory, as the
+ * reference's Scene::new(bytes) takes it (world.rs:890); URIs that name
+ * files cannot be resolved and fail */
+int ptw_load_gltf_bytes(ptw_world* world, const void* bytes, size_t size, char* error, size_t error_size);
 
 /* Builds the BVH over all added meshes, reorders triangles to BVH order and
  * sets the auto camera (the tail of Scene::new, world.rs:1339-1357).  Errors
@@ -90,6 +94,9 @@ int ptw_set_skybox_rgba(ptw_world* world, const float* rgba, uint32_t width, uin
  * bytes.  On failure `error` (if given) receives the reason and the skybox is
  * unchanged. */
 int ptw_set_skybox_file(ptw_world* world, const char* path, char* error, size_t error_size);
+/* the same from an image held in memory, as World::replace_skybox(bytes)
+ * takes it (world.rs:635-644) */
+int ptw_set_skybox_bytes(ptw_world* world, const void* bytes, size_t size, char* error, size_t error_size);
 
 /* Decodes the same image files to linear RGBA32F, row 0 at the top.  With
  * rgba == NULL only *width and *height are set; otherwise rgba must hold
@@ -121,6 +128,14 @@ int ptw_set_aspect_ratio(ptw_world* world, float aspect_ratio);
  * radians; pitch is clamped to [-pi/2, pi/2], fov to [0, pi). */
 int ptw_edit_camera(ptw_world* world, const float* position3, const float* yaw,
                     const float* pitch, const float* fov);
+
+/* World::edit_emission_scale (world.rs:655-692): every emissive material
+ * (luminance of the emission colour times the emission weight above 0) gets
+ * its emission strength at build time times max(scale, 0), overwriting edits
+ * of that value; ptw_emission_scale returns the last scale (1 initially).
+ * Only after ptw_build. */
+int ptw_edit_emission_scale(ptw_world* world, float scale);
+float ptw_emission_scale(const ptw_world* world);
 
 /* World::edit_material (world.rs:735-787) restricted to replacing the
  * editable prefix (everything before alpha_mode) of one material */

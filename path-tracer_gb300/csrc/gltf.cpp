@@ -394,6 +394,11 @@ struct Loader {
         if (!read_file(path, file)) return fail("cannot read " + path);
         const size_t slash = path.find_last_of('/');
         dir = slash == std::string::npos ? "" : path.substr(0, slash + 1);
+        return open_bytes(file);
+    }
+
+    // a .glb container or .gltf JSON held in memory; relative URIs resolve against `dir`
+    bool open_bytes(const std::vector<uint8_t>& file) {
         std::vector<uint8_t> bin;
         const char* json_begin;
         size_t json_size;
@@ -887,6 +892,23 @@ struct Loader {
 };
 
 }  // namespace
+
+extern "C" int ptw_load_gltf_bytes(ptw_world* world, const void* bytes, size_t size, char* error,
+                                   size_t error_size) {
+    if (!world || !bytes) return PT_ERR_INVALID_ARG;
+    Loader l;
+    l.world = world;
+    bool ok;
+    try {
+        const std::vector<uint8_t> file((const uint8_t*)bytes, (const uint8_t*)bytes + size);
+        ok = l.open_bytes(file) && l.load();
+    } catch (const std::bad_alloc&) {
+        if (error && error_size) snprintf(error, error_size, "out of host memory");
+        return PT_ERR_OOM;
+    }
+    if (!ok && error && error_size) snprintf(error, error_size, "%s", l.error.c_str());
+    return ok ? PT_OK : PT_ERR_INVALID_ARG;
+}
 
 extern "C" int ptw_load_gltf(ptw_world* world, const char* path, char* error, size_t error_size) {
     if (!world || !path) return PT_ERR_INVALID_ARG;

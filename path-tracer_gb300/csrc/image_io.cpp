@@ -1496,13 +1496,18 @@ bool decode_texture(const uint8_t* d, size_t n, std::vector<uint8_t>& rgba, uint
     return true;
 }
 
+bool decode_image(const std::vector<uint8_t>& data, std::vector<float>& rgba, uint32_t& w, uint32_t& h,
+                  std::string& err, bool size_only = false) {
+    if (data.size() >= 4 && data[0] == 0x76 && data[1] == 0x2f && data[2] == 0x31 && data[3] == 0x01)
+        return read_exr(data, rgba, w, h, err, size_only);
+    return read_hdr(data, rgba, w, h, err, size_only);
+}
+
 bool read_image(const char* path, std::vector<float>& rgba, uint32_t& w, uint32_t& h, std::string& err,
                 bool size_only = false) {
     std::vector<uint8_t> data;
     if (!read_file(path, data, err)) return false;
-    if (data.size() >= 4 && data[0] == 0x76 && data[1] == 0x2f && data[2] == 0x31 && data[3] == 0x01)
-        return read_exr(data, rgba, w, h, err, size_only);
-    return read_hdr(data, rgba, w, h, err, size_only);
+    return decode_image(data, rgba, w, h, err, size_only);
 }
 
 void put_error(char* error, size_t size, const std::string& msg) {
@@ -1548,6 +1553,25 @@ extern "C" int ptw_set_skybox_file(ptw_world* world, const char* path, char* err
     uint32_t w = 0, h = 0;
     std::string err;
     if (!read_image(path, px, w, h, err)) {
+        put_error(error, error_size, err);
+        return PT_ERR_INVALID_ARG;
+    }
+    const int rc = ptw_set_skybox_rgba(world, px.data(), w, h);
+    if (rc) put_error(error, error_size, ptw_last_error(world));
+    return rc;
+} catch (const std::bad_alloc&) {
+    put_error(error, error_size, "out of host memory");
+    return PT_ERR_OOM;
+}
+
+extern "C" int ptw_set_skybox_bytes(ptw_world* world, const void* bytes, size_t size, char* error,
+                                    size_t error_size) try {
+    if (!world || !bytes) return PT_ERR_INVALID_ARG;
+    const std::vector<uint8_t> data((const uint8_t*)bytes, (const uint8_t*)bytes + size);
+    std::vector<float> px;
+    uint32_t w = 0, h = 0;
+    std::string err;
+    if (!decode_image(data, px, w, h, err)) {
         put_error(error, error_size, err);
         return PT_ERR_INVALID_ARG;
     }

@@ -440,6 +440,8 @@ struct ptw_world {
     bool pending_luminance = false;
     float next_luminance = 0.0f;
     std::map<uint32_t, pt_material> pending_materials;
+    std::vector<float> initial_strength;  // emission strength of every material when built
+    float emission_scale = 1.0f;
     bool taken_once = false;
     // storage behind the pointers returned by take_updates
     pt_scene_upload scene_upload{};
@@ -706,6 +708,8 @@ int ptw_build(ptw_world* w) {
     w->linear_flat.clear();
     for (auto& l : w->linear_layers) w->linear_flat.insert(w->linear_flat.end(), l.begin(), l.end());
     (void)layer_bytes;
+    w->initial_strength.resize(w->materials.size());
+    for (size_t i = 0; i < w->materials.size(); ++i) w->initial_strength[i] = w->materials[i].emission_color_and_luminance[3];
     w->built = true;
     w->full_upload = true;
     return PT_OK;
@@ -778,6 +782,31 @@ int ptw_edit_material(ptw_world* w, uint32_t index, const pt_material* m) {
         w->pending_materials[index] = accepted;
     return PT_OK;
 }
+
+// World::edit_emission_scale, world.rs:655-692: every emissive material
+// (emission colour luminance times emission weight above 0) gets its initial
+// emission strength times `scale`, replacing edits of that value
+int ptw_edit_emission_scale(ptw_world* w, float scale) {
+    if (!w) return PT_ERR_INVALID_ARG;
+    if (!w->built) return w->fail(PT_ERR_STATE, "ptw_build has not run");
+    if (std::isnan(scale)) return w->fail(PT_ERR_INVALID_ARG, "scale must not be NaN");
+    scale = std::max(scale, 0.0f);
+    w->emission_scale = scale;
+    for (uint32_t i = 0; i < (uint32_t)w->materials.size(); ++i) {
+        auto it = w->pending_materials.find(i);
+        pt_material edited = it != w->pending_materials.end() ? it->second : w->materials[i];
+        const float* e = edited.emission_color_and_luminance;
+        if (luminance(e[0], e[1], e[2]) * (double)edited.emission_weight <= 0.0) continue;
+        edited.emission_color_and_luminance[3] = w->initial_strength[i] * scale;
+        if (std::memcmp(&edited, &w->materials[i], sizeof(pt_material)) == 0)
+            w->pending_materials.erase(i);
+        else
+            w->pending_materials[i] = edited;
+    }
+    return PT_OK;
+}
+
+float ptw_emission_scale(const ptw_world* w) { return w ? w->emission_scale : 0.0f; }
 
 // World::take_updates, world.rs:790-884
 int ptw_take_updates(ptw_world* w, pt_world_updates* out) {

@@ -69,6 +69,20 @@ class World:
         return w
 
     @classmethod
+    def from_gltf_bytes(cls, data: bytes, build: bool = True) -> "World":
+        """A world holding a .glb (or self-contained .gltf) given as bytes, as Scene::new(bytes) takes it."""
+        w = cls.empty()
+        err = C.create_string_buffer(512)
+        buf = C.create_string_buffer(bytes(data), len(data))
+        rc = w._lib.ptw_load_gltf_bytes(w._h, buf, len(data), err, len(err))
+        if rc != abi.PT_OK:
+            w.close()
+            raise PathTracerError(rc, f"glTF import: {err.value.decode()}")
+        if build:
+            w.build()
+        return w
+
+    @classmethod
     def cornell_box_textured(cls, seed: int = 1) -> "World":
         """The Cornell room as eight meshes, four with procedural 1024^2 textures (precision workload)."""
         lib = load()
@@ -156,6 +170,21 @@ class World:
         rc = self._lib.ptw_set_skybox_file(self._h, str(path).encode(), err, len(err))
         if rc != abi.PT_OK:
             raise PathTracerError(rc, f"skybox {path}: {err.value.decode()}")
+
+    def set_skybox_bytes(self, data: bytes) -> None:
+        """Skybox from an .hdr / .exr image given as bytes (World::replace_skybox)."""
+        err = C.create_string_buffer(512)
+        buf = C.create_string_buffer(bytes(data), len(data))
+        rc = self._lib.ptw_set_skybox_bytes(self._h, buf, len(data), err, len(err))
+        if rc != abi.PT_OK:
+            raise PathTracerError(rc, f"skybox: {err.value.decode()}")
+
+    def edit_emission_scale(self, scale: float) -> None:
+        """World::edit_emission_scale: emissive materials get their initial strength times `scale`."""
+        self._check(self._lib.ptw_edit_emission_scale(self._h, scale))
+
+    def emission_scale(self) -> float:
+        return self._lib.ptw_emission_scale(self._h)
 
     def edit_skybox_average_luminance(self, luminance: float) -> None:
         self._check(self._lib.ptw_edit_skybox_average_luminance(self._h, luminance))

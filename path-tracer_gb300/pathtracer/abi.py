@@ -232,6 +232,10 @@ SIGNATURES = {
     "ptw_add_mesh": (C.c_int, [_vp, P(Mesh)]),
     "ptw_add_atlas_layer": (C.c_int, [_vp, C.c_int, _vp, P(c_i32)]),
     "ptw_load_gltf": (C.c_int, [_vp, C.c_char_p, C.c_char_p, C.c_size_t]),
+    "ptw_load_gltf_bytes": (C.c_int, [_vp, _vp, C.c_size_t, C.c_char_p, C.c_size_t]),
+    "ptw_set_skybox_bytes": (C.c_int, [_vp, _vp, C.c_size_t, C.c_char_p, C.c_size_t]),
+    "ptw_edit_emission_scale": (C.c_int, [_vp, c_f]),
+    "ptw_emission_scale": (c_f, [_vp]),
     "ptw_build": (C.c_int, [_vp]),
     "ptw_set_skybox_rgba": (C.c_int, [_vp, _vp, c_u32, c_u32]),
     "ptw_set_skybox_file": (C.c_int, [_vp, C.c_char_p, C.c_char_p, C.c_size_t]),

@@ -181,3 +181,54 @@ def test_procedural_scene_small():
                              emissive_triangles=5, skybox_width=64, skybox_height=32)
     np.testing.assert_array_equal(w.geometries(), w2.geometries())
     np.testing.assert_array_equal(w.bvh_nodes(), w2.bvh_nodes())
+
+
+def test_edit_emission_scale():
+    # World::edit_emission_scale (world.rs:655-692)
+    w = pt.World.cornell_box()
+    mats = w.materials()
+    emissive = [i for i, m in enumerate(mats) if m.emission_weight > 0 and max(m.emission_color_and_luminance[:3]) > 0]
+    assert emissive and w.emission_scale() == 1.0
+    w.take_updates()
+    w.edit_emission_scale(3.0)
+    u = w.take_updates()
+    assert u.material_update_count == len(emissive) and u.reset_accumulation == 1
+    for k in range(u.material_update_count):
+        upd = u.materials[k]
+        assert upd.index in emissive
+        assert upd.material.emission_color_and_luminance[3] == np.float32(mats[upd.index].emission_color_and_luminance[3] * 3.0)
+    # an individual edit of the strength is overwritten by the next scale; scale 1 restores the built value
+    m = w.materials()[emissive[0]]
+    m.emission_color_and_luminance[3] = 123.0
+    w.edit_material(emissive[0], m)
+    w.edit_emission_scale(1.0)
+    u = w.take_updates()
+    assert w.materials()[emissive[0]].emission_color_and_luminance[3] == mats[emissive[0]].emission_color_and_luminance[3]
+    w.edit_emission_scale(-2.0)  # clamped at 0
+    assert w.emission_scale() == 0.0
+    u = w.take_updates()
+    assert all(w.materials()[i].emission_color_and_luminance[3] == 0.0 for i in emissive)
+    w.close()
+
+
+def test_scene_and_skybox_from_bytes(tmp_path):
+    from test_gltf import MATERIAL, write_gltf
+    from test_image_io import random_planes, write_exr
+    path = write_gltf(tmp_path, [{"mesh": 0}], [0], [MATERIAL], binary=True)
+    a = pt.World.from_gltf(path)
+    b = pt.World.from_gltf_bytes(path.read_bytes())
+    np.testing.assert_array_equal(a.geometries(), b.geometries())
+    rng = np.random.default_rng(2)
+    write_exr(tmp_path / "sky.exr", random_planes(rng, 16, 32, {"R": "half", "G": "half", "B": "half"}), 3)
+    a.set_skybox_file(tmp_path / "sky.exr")
+    b.set_skybox_bytes((tmp_path / "sky.exr").read_bytes())
+    ua, ub = a.take_updates(), b.take_updates()
+    n = 16 * 32 * 4
+    np.testing.assert_array_equal(np.ctypeslib.as_array(ua.skybox.contents.rgba, (n,)),
+                                  np.ctypeslib.as_array(ub.skybox.contents.rgba, (n,)))
+    with pytest.raises(pt.PathTracerError):
+        b.set_skybox_bytes(b"not an image")
+    with pytest.raises(pt.PathTracerError):
+        pt.World.from_gltf_bytes(b"glTF\x02\x00\x00\x00\x0c\x00\x00\x00")
+    a.close()
+    b.close()
