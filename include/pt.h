@@ -353,7 +353,7 @@ typedef struct pt_device_world {
     uint64_t triangle_count;
     const pt_material* materials;
     uint64_t material_count;
-    const pt_bvh_node* bvh_nodes;             /* 16-byte aligned */
+    const pt_bvh_node* bvh_nodes;             /* 32-byte aligned (each node is one 32-byte load) */
     uint64_t node_count;
     const uint8_t* srgb_texture_atlases;      /* srgb_atlas_count layers, may be NULL if 0 */
     uint32_t srgb_atlas_count;

@@ -139,9 +139,38 @@ struct LocalStack {
     PTD uint2 get(uint32_t i) const { return deep[i & 63u]; }
 };
 
+// 256-bit loads of a child pair (two 32-byte nodes, 64-byte aligned): one
+// ld.global.nc.v8 per node instead of two 128-bit loads
+#ifndef PT_V8_PAIRS
+#define PT_V8_PAIRS 1
+#endif
+PTD void load_node(const float4* p, float4& lo, float4& hi) {
+#if PT_V8_PAIRS
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(lo.x), "=f"(lo.y), "=f"(lo.z), "=f"(lo.w), "=f"(hi.x), "=f"(hi.y), "=f"(hi.z), "=f"(hi.w)
+        : "l"(p));
+#else
+    lo = __ldg(p);
+    hi = __ldg(p + 1);
+#endif
+}
+
+// a padded triangle (48 bytes) as one 256-bit and one 128-bit load: the
+// 32-byte aligned half comes first for even triangles, second for odd ones
+#ifndef PT_V8_TRIS
+#define PT_V8_TRIS 0
+#endif
 PTD Tri load_tri4(const Fast& f, uint32_t tri) {
     const float4* p = f.tri4 + 3 * (size_t)tri;
+#if PT_V8_TRIS
+    const bool odd = tri & 1u;
+    float4 w0, w1;
+    load_node(p + (odd ? 1 : 0), w0, w1);
+    const float4 x = __ldg(p + (odd ? 0 : 2));
+    const float4 a = odd ? x : w0, b = odd ? w0 : w1, c = odd ? w1 : x;
+#else
     const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+#endif
     Tri t;
     t.v0 = mk(a.x, a.y, a.z);
     t.v1 = mk(b.x, b.y, b.z);
@@ -250,7 +279,9 @@ struct Traverser {
             if (tc == 0u) {
                 rec.interior();
                 const float4* p = f.pairs + 2 * (size_t)lf;
-                const float4 l0 = __ldg(p), l1 = __ldg(p + 1), r0 = __ldg(p + 2), r1 = __ldg(p + 3);
+                float4 l0, l1, r0, r1;
+                load_node(p, l0, l1);
+                load_node(p + 2, r0, r1);
                 const float dl = box_test(l0, l1, nod, rcp, hit_t);
                 const float dr = box_test(r0, r1, nod, rcp, hit_t);
                 const bool hl = dl >= 0.0f, hr = dr >= 0.0f;
@@ -321,7 +352,9 @@ struct Traverser {
         } else {
             rec.interior();
             const float4* p = f.pairs + 2 * (size_t)lf;
-            const float4 l0 = __ldg(p), l1 = __ldg(p + 1), r0 = __ldg(p + 2), r1 = __ldg(p + 3);
+            float4 l0, l1, r0, r1;
+            load_node(p, l0, l1);
+            load_node(p + 2, r0, r1);
             const float dl = box_test(l0, l1, nod, rcp, hit_t);
             const float dr = box_test(r0, r1, nod, rcp, hit_t);
             const bool hl = dl >= 0.0f, hr = dr >= 0.0f;
@@ -495,7 +528,9 @@ struct WideTraverser {
     // kShadow) in bits 0..23, their count in bits 24..27
     PTD uint32_t visit(const Fast& f, uint32_t n) const {
         const float4* p = f.wide + 8 * (size_t)n;
-        const float4 h0 = __ldg(p), h1 = __ldg(p + 1), h2 = __ldg(p + 2), h3 = __ldg(p + 3);
+        float4 h0, h1, h2, h3;
+        load_node(p, h0, h1);
+        load_node(p + 2, h2, h3);
         const uint32_t meta = __float_as_uint(h0.w);
         const uint32_t count = meta >> 24;
         const AxisFrame X = axis_frame(h0.x, meta & 0xffu, rcp.x, nod.x, __float_as_uint(h1.x), __float_as_uint(h1.y),

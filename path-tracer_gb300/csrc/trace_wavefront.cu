@@ -764,8 +764,10 @@ extern "C" int pt_trace_noalloc(const pt_device_world* world, const pt_trace_par
     if (!world->geometries || !world->attributes || !world->materials || !world->bvh_nodes || !world->skybox_rgba ||
         world->triangle_count == 0 || world->node_count == 0)
         return noalloc_fail(error, error_size, PT_ERR_INVALID_ARG, "the world needs triangles, materials, BVH nodes and a skybox");
-    if (((uintptr_t)world->bvh_nodes | (uintptr_t)world->skybox_rgba | (uintptr_t)accum | (uintptr_t)image) & 15u)
-        return noalloc_fail(error, error_size, PT_ERR_INVALID_ARG, "BVH nodes, skybox, accum and image must be 16-byte aligned");
+    if (((uintptr_t)world->skybox_rgba | (uintptr_t)accum | (uintptr_t)image) & 15u)
+        return noalloc_fail(error, error_size, PT_ERR_INVALID_ARG, "skybox, accum and image must be 16-byte aligned");
+    if ((uintptr_t)world->bvh_nodes & 31u)  // nodes are read in place with 32-byte loads
+        return noalloc_fail(error, error_size, PT_ERR_INVALID_ARG, "BVH nodes must be 32-byte aligned");
     if (tile_width == 0 || tile_height == 0)
         return noalloc_fail(error, error_size, PT_ERR_OUT_OF_LIMITS, "tile size must be positive");
     if (!(params->tile_origin[0] < params->image_size[0] && params->tile_origin[1] < params->image_size[1]))

@@ -128,3 +128,24 @@ def test_noalloc_rejects_requests_beyond_its_scratch():
     rc, msg = noalloc(lib, dw, (512, 512), (0, 0), tile, 2, 1, 2, accum, out)
     assert rc == abi.PT_ERR_OUT_OF_LIMITS and "262144" in msg
     torch.cuda.synchronize()
+
+
+def test_noalloc_rejects_unaligned_nodes_on_the_host():
+    # the nodes are read in place with 32-byte loads: a 16-byte aligned array is refused before any launch
+    torch = pytest.importorskip("torch")
+    lib = pt.load()
+    world = pt.World.cornell_box()
+    updates = world.take_updates()
+    keep = []
+    dw = device_world(torch, updates, keep)
+    s = updates.scene.contents
+    host = np.ctypeslib.as_array(C.cast(s.bvh_nodes, C.POINTER(C.c_uint8)), shape=(32 * s.node_count,)).copy()
+    shifted = torch.zeros(32 * s.node_count + 16, dtype=torch.uint8, device="cuda")
+    shifted[16:] = torch.from_numpy(host).to("cuda")
+    keep.append(shifted)
+    dw.bvh_nodes = shifted.data_ptr() + 16
+    accum = torch.zeros((8, 8, 4), dtype=torch.float32, device="cuda")
+    out = torch.zeros_like(accum)
+    rc, msg = noalloc(lib, dw, (8, 8), (0, 0), (8, 8), 2, 0, 1, accum, out)
+    assert rc == abi.PT_ERR_INVALID_ARG and "32-byte aligned" in msg
+    torch.cuda.synchronize()
