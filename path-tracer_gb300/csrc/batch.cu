@@ -324,9 +324,9 @@ __global__ void pad_triangles_kernel(const pt_triangle_geometry* geo, uint64_t n
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* v = geo[i].v0;
-    tri4[3 * i + 0] = make_float4(v[0], v[1], v[2], 0.0f);
-    tri4[3 * i + 1] = make_float4(v[3], v[4], v[5], 0.0f);
-    tri4[3 * i + 2] = make_float4(v[6], v[7], v[8], 0.0f);
+    tri4[kTriStride * i + 0] = make_float4(v[0], v[1], v[2], 0.0f);
+    tri4[kTriStride * i + 1] = make_float4(v[3], v[4], v[5], 0.0f);
+    tri4[kTriStride * i + 2] = make_float4(v[6], v[7], v[8], 0.0f);
 }
 
 // ---------------------------------------------------------------- host
@@ -849,7 +849,7 @@ int upload_scene(pt_engine* e, Scene& s, const pt_world_updates* u) {
     if (!rc)
         rc = e->cuda(cudaMemcpyAsync(static_cast<char*>(s.pairs.p) + 32, s.nodes.p, sc->node_count * 32,
                                      cudaMemcpyDeviceToDevice, e->stream), "BVH layout");
-    if (!rc) rc = e->cuda(s.tri4.alloc(sc->triangle_count * 48), "triangle layout");
+    if (!rc) rc = e->cuda(s.tri4.alloc(sc->triangle_count * 16 * ptd::kTriStride), "triangle layout");
     if (!rc) {
         pad_triangles_kernel<<<(unsigned)((sc->triangle_count + 255) / 256), 256, 0, e->stream>>>(
             s.geo.as<pt_triangle_geometry>(), sc->triangle_count, s.tri4.as<float4>());
@@ -1092,7 +1092,7 @@ int pte_scene_add(pt_engine* e, const pt_world_updates* u, uint64_t* scene_id) {
     for (uint64_t i = 0; i < sc->material_count; ++i) any_alpha |= sc->materials[i].alpha_mode != PT_ALPHA_MODE_OPAQUE;
     const SceneForm form = scene_form(e, any_alpha);
     const uint64_t texels = (uint64_t)sk->uniforms.width * sk->uniforms.height;
-    uint64_t bytes = sc->triangle_count * (36 + 48) + sc->material_count * 224 + 512 +
+    uint64_t bytes = sc->triangle_count * (36 + 16 * ptd::kTriStride) + sc->material_count * 224 + 512 +
                      (sc->srgb_atlas_count + sc->linear_atlas_count) * layer + sk->alias_count * 12 +
                      u->scene_alias_count * 16 + 1024;
     bytes += form.half ? sc->triangle_count * 64 + texels * 8 : sc->triangle_count * 112 + texels * 16;

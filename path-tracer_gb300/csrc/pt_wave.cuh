@@ -160,9 +160,19 @@ PTD void load_node(const float4* p, float4& lo, float4& hi) {
 #ifndef PT_V8_TRIS
 #define PT_V8_TRIS 0
 #endif
+// float4s per padded triangle: 3 (48 bytes), or 4 (64 bytes: one 256-bit and
+// one 128-bit load, both aligned)
+#ifndef PT_TRI_STRIDE
+#define PT_TRI_STRIDE 3
+#endif
+constexpr uint32_t kTriStride = PT_TRI_STRIDE;
 PTD Tri load_tri4(const Fast& f, uint32_t tri) {
-    const float4* p = f.tri4 + 3 * (size_t)tri;
-#if PT_V8_TRIS
+    const float4* p = f.tri4 + kTriStride * (size_t)tri;
+#if PT_TRI_STRIDE == 4
+    float4 a, b;
+    load_node(p, a, b);
+    const float4 c = __ldg(p + 2);
+#elif PT_V8_TRIS
     const bool odd = tri & 1u;
     float4 w0, w1;
     load_node(p + (odd ? 1 : 0), w0, w1);

@@ -293,9 +293,9 @@ __global__ void pad_triangles_kernel(const pt_triangle_geometry* geo, uint64_t n
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* v = geo[i].v0;
-    tri4[3 * i + 0] = make_float4(v[0], v[1], v[2], 0.0f);
-    tri4[3 * i + 1] = make_float4(v[3], v[4], v[5], 0.0f);
-    tri4[3 * i + 2] = make_float4(v[6], v[7], v[8], 0.0f);
+    tri4[kTriStride * i + 0] = make_float4(v[0], v[1], v[2], 0.0f);
+    tri4[kTriStride * i + 1] = make_float4(v[3], v[4], v[5], 0.0f);
+    tri4[kTriStride * i + 2] = make_float4(v[6], v[7], v[8], 0.0f);
 }
 
 // FP32 attributes -> pt_half_attribute records (round to nearest even)
@@ -430,7 +430,7 @@ namespace {
 cudaError_t build_layouts(Wavefront* wf, const ptd::World& w, uint64_t nodes, uint64_t tris, cudaStream_t stream) {
     PTW_TRY(wf->pairs.reserve((nodes + 1) * 32 + 256));
     PTW_TRY(cudaMemcpyAsync(static_cast<char*>(wf->pairs.p) + 32, w.nodes, nodes * 32, cudaMemcpyDeviceToDevice, stream));
-    PTW_TRY(wf->tri4.reserve(tris * 48));
+    PTW_TRY(wf->tri4.reserve(tris * 16 * ptd::kTriStride));
     ptd::pad_triangles_kernel<<<(unsigned)((tris + 255) / 256), 256, 0, stream>>>(w.geo, tris, static_cast<float4*>(wf->tri4.p));
     PTW_TRY(cudaGetLastError());
     wf->stale = false;
