@@ -1,0 +1,84 @@
+"""White-furnace sanity of the shading model: a sphere under a uniform sky of
+radiance 1.  A convex object sees only the sky, so a pixel on the sphere
+converges to the directional albedo of its material; a lossless white
+material must come out near 1 and no material may create energy.  The
+reference notes that its own furnace test fails slightly for the
+energy-preserving Oren-Nayar lobe (trace.slang:1132); single-scattering GGX
+loses energy at high roughness (trace.slang:1131)."""
+import numpy as np
+import pytest
+
+import pathtracer as pt
+from pathtracer import abi
+
+pytestmark = pytest.mark.gpu
+
+
+def uv_sphere(nu=96, nv=48):
+    pos, nor, uv, tan = [], [], [], []
+    for j in range(nv + 1):
+        th = np.pi * j / nv
+        for i in range(nu + 1):
+            ph = 2 * np.pi * i / nu
+            p = [np.sin(th) * np.cos(ph), np.cos(th), np.sin(th) * np.sin(ph)]
+            pos.append(p)
+            nor.append(p)
+            uv.append([i / nu, j / nv])
+            tan.append([-np.sin(ph), 0.0, np.cos(ph), 1.0])
+    idx = []
+    for j in range(nv):
+        for i in range(nu):
+            a, b = j * (nu + 1) + i, (j + 1) * (nu + 1) + i
+            idx += [a, b, a + 1, a + 1, b, b + 1]
+    f = np.float32
+    return np.array(pos, f), np.array(nor, f), np.array(uv, f), np.array(tan, f), np.array(idx)
+
+
+def furnace(**fields):
+    w = pt.World.empty()
+    m = pt.default_material()
+    m.base_color[:] = [1.0, 1.0, 1.0, 1.0]
+    m.emission_color_and_luminance[:] = [0.0, 0.0, 0.0, 1.0]
+    for k, v in fields.items():
+        if k == "specular_weight":
+            m.specular_color_and_weight[:] = [1.0, 1.0, 1.0, v]
+        else:
+            setattr(m, k, v)
+    mi = w.add_material(m)
+    pos, nor, uv, tan, idx = uv_sphere()
+    w.add_mesh(pos, mi, normals=nor, uvs=uv, tangents=tan, indices=idx)
+    w.build()
+    w.set_skybox_rgba(np.ones((16, 32, 4), np.float32))
+    w.edit_skybox_average_luminance(1.0)
+    w.set_aspect_ratio(1.0)
+    n = 96
+    tr = pt.PathTracer(w.take_updates(), (n, n))
+    tr.set_max_bounces(4)
+    tr.set_tile((n, n), (0, 0), (n, n))
+    rec = tr.trace_recorded(16)
+    first = rec["hit"][..., 0].reshape(16, n * n)
+    on_sphere = (first >= 0).all(axis=0)  # every sample of the pixel hits the sphere
+    off_sphere = (first < 0).all(axis=0)
+    while tr.sample_count() < 256:
+        tr.trace(16)
+    acc = tr.read_tile(abi.PT_TILE_ACCUMULATION)[..., :3].reshape(-1, 3).astype(np.float64) / tr.sample_count()
+    tr.close()
+    w.close()
+    assert on_sphere.sum() > 1000 and off_sphere.sum() > 1000
+    return acc[on_sphere], acc[off_sphere]
+
+
+@pytest.mark.parametrize("name,fields,low", [
+    # lower bounds a little under the oracle's 64-spp means (0.998, 0.998, 0.998, 0.890)
+    ("diffuse, smooth", dict(base_metalness=0.0, base_diffuse_roughness=0.0, specular_weight=0.0), 0.98),
+    ("diffuse, rough", dict(base_metalness=0.0, base_diffuse_roughness=1.0, specular_weight=0.0), 0.98),
+    ("coated diffuse", dict(base_metalness=0.0, base_diffuse_roughness=0.5, specular_weight=1.0,
+                            specular_roughness=0.3, specular_ior=1.5), 0.97),
+    ("metal", dict(base_metalness=1.0, specular_weight=1.0, specular_roughness=0.5), 0.85),
+])
+def test_white_furnace(name, fields, low):
+    sphere, sky = furnace(**fields)
+    mean = sphere.mean()
+    print(f"white furnace, {name}: mean {mean:.4f}, pixel range {sphere.min():.3f}..{sphere.max():.3f}")
+    np.testing.assert_allclose(sky, 1.0, rtol=2e-6)  # the sky itself is exactly the uniform radiance
+    assert low <= mean <= 1.02, mean
