@@ -58,13 +58,16 @@ def furnace(**fields):
     rec = tr.trace_recorded(16)
     first = rec["hit"][..., 0].reshape(16, n * n)
     on_sphere = (first >= 0).all(axis=0)  # every sample of the pixel hits the sphere
-    off_sphere = (first < 0).all(axis=0)
+    # sky: the image corners, far from the silhouette for every jittered sample
+    y, x = np.mgrid[0:n, 0:n]
+    off_sphere = ((np.minimum(x, n - 1 - x) < 12) & (np.minimum(y, n - 1 - y) < 12)).ravel()
+    assert (first[:, off_sphere] < 0).all()
     while tr.sample_count() < 256:
         tr.trace(16)
     acc = tr.read_tile(abi.PT_TILE_ACCUMULATION)[..., :3].reshape(-1, 3).astype(np.float64) / tr.sample_count()
     tr.close()
     w.close()
-    assert on_sphere.sum() > 1000 and off_sphere.sum() > 1000
+    assert on_sphere.sum() > 1000
     return acc[on_sphere], acc[off_sphere]
 
 
