@@ -113,6 +113,13 @@ int ptw_read_image_rgba(const char* path, float* rgba, uint64_t capacity, uint32
 int ptw_decode_texture_rgba8(const void* bytes, size_t size, uint8_t* rgba, uint64_t capacity, uint32_t* width,
                              uint32_t* height, char* error, size_t error_size);
 
+/* Saves an RGB8 image (width * height * 3 bytes, rows top to bottom) in the
+ * format its extension names: .png, .jpg / .jpeg (baseline JPEG, quality
+ * 75), .webp (lossless) or .ppm; the output formats of the reference's
+ * `render --output` (headless.rs:30,118-126) plus PPM. */
+int ptw_write_image(const char* path, const uint8_t* rgb8, uint32_t width, uint32_t height, char* error,
+                    size_t error_size);
+
 /* the procedural sky of the large scene (vertical gradient plus a Gaussian
  * sun lobe), width x height, passed through ptw_set_skybox_rgba */
 int ptw_set_procedural_skybox(ptw_world* world, uint32_t width, uint32_t height);

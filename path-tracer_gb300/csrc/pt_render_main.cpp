@@ -7,11 +7,11 @@
 // at most 16 samples per trace call (headless.rs:207-285), each finished tile
 // tone mapped (display.wgsl) and the RGB8 image saved.
 //
-// Scenes: a glTF 2.0 file (.glb or .gltf, untextured materials; the
+// Scenes: a glTF 2.0 file (.glb or .gltf, PNG/JPEG textures; the
 // reference's default is its box.glb asset), "cornell" (36-triangle Cornell
 // box) or "procedural[:SEED]" (the ~2.1M-triangle procedural scene).
-// Skyboxes: "black", "procedural" (gradient + sun) or a Radiance .hdr file.
-// Output: .png (or .ppm); JPEG and WebP encoders are not part of this build.
+// Skyboxes: "black", "procedural" (gradient + sun), a Radiance .hdr or an
+// OpenEXR .exr file.  Output: .png, .jpg / .jpeg, .webp (lossless) or .ppm.
 #include <algorithm>
 #include <cerrno>
 #include <chrono>
@@ -42,7 +42,7 @@ struct Options {
 
 [[noreturn]] void usage_error(const std::string& msg) {
     fprintf(stderr, "error: %s\n\nusage: pt-render render [--scene S] [--skybox S] [--skybox-luminance NITS]\n"
-                    "  [--output FILE.png] [--width N] [--height N] [--samples N] [--max-bounces 0..16]\n"
+                    "  [--output FILE.{png,jpg,webp}] [--width N] [--height N] [--samples N] [--max-bounces 0..16]\n"
                     "  [--tile-size N] [--camera-position X,Y,Z] [--camera-yaw DEG] [--camera-pitch DEG]\n"
                     "  [--camera-fov DEG] [--device N]\n",
             msg.c_str());
@@ -84,8 +84,11 @@ Options parse(int argc, char** argv) {
             o.output = v;
             const auto dot = o.output.rfind('.');
             const std::string ext = dot == std::string::npos ? "" : o.output.substr(dot + 1);
-            if (ext != "png" && ext != "ppm")
-                usage_error("--output must have a .png extension (.ppm also accepted; JPEG/WebP encoders are not built)");
+            std::string lower = ext;
+            for (char& c : lower) c = (char)tolower((unsigned char)c);
+            // parse_output, headless.rs:118-126 (.ppm accepted as well)
+            if (lower != "png" && lower != "jpg" && lower != "jpeg" && lower != "webp" && lower != "ppm")
+                usage_error("--output must have a .png, .jpg, .jpeg, or .webp extension");
         } else if (f == "--width") o.width = parse_u32(f, v, 1, 0xffffffffu);
         else if (f == "--height") o.height = parse_u32(f, v, 1, 0xffffffffu);
         else if (f == "--samples") o.samples = parse_u32(f, v, 1, 0xffffffffu);
@@ -122,88 +125,6 @@ Options parse(int argc, char** argv) {
         else usage_error("unknown flag " + f);
     }
     return o;
-}
-
-uint32_t crc32(const uint8_t* d, size_t n, uint32_t c = 0xffffffffu) {
-    static uint32_t table[256];
-    static bool init = false;
-    if (!init) {
-        for (uint32_t i = 0; i < 256; ++i) {
-            uint32_t x = i;
-            for (int k = 0; k < 8; ++k) x = (x & 1) ? 0xedb88320u ^ (x >> 1) : x >> 1;
-            table[i] = x;
-        }
-        init = true;
-    }
-    for (size_t i = 0; i < n; ++i) c = table[(c ^ d[i]) & 0xff] ^ (c >> 8);
-    return c;
-}
-
-// PNG with an uncompressed (stored-block) zlib stream
-bool write_png(const std::string& path, const std::vector<uint8_t>& rgb, uint32_t w, uint32_t h, std::string& err) {
-    std::vector<uint8_t> raw;
-    raw.reserve((size_t)h * (w * 3 + 1));
-    for (uint32_t y = 0; y < h; ++y) {
-        raw.push_back(0);
-        raw.insert(raw.end(), rgb.begin() + (size_t)y * w * 3, rgb.begin() + (size_t)(y + 1) * w * 3);
-    }
-    std::vector<uint8_t> z = {0x78, 0x01};
-    uint32_t a = 1, b = 0;
-    for (uint8_t v : raw) {
-        a = (a + v) % 65521;
-        b = (b + a) % 65521;
-    }
-    for (size_t off = 0; off < raw.size() || off == 0; off += 65535) {
-        const size_t len = std::min<size_t>(65535, raw.size() - off);
-        z.push_back(off + len >= raw.size() ? 1 : 0);
-        z.push_back(len & 0xff);
-        z.push_back(len >> 8);
-        z.push_back(~len & 0xff);
-        z.push_back((~len >> 8) & 0xff);
-        z.insert(z.end(), raw.begin() + off, raw.begin() + off + len);
-        if (raw.empty()) break;
-    }
-    const uint32_t adler = (b << 16) | a;
-    for (int s = 24; s >= 0; s -= 8) z.push_back((adler >> s) & 0xff);
-    FILE* f = fopen(path.c_str(), "wb");
-    if (!f) {
-        err = "cannot save " + path + ": " + strerror(errno);
-        return false;
-    }
-    const uint8_t sig[8] = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1a, '\n'};
-    fwrite(sig, 1, 8, f);
-    auto chunk = [&](const char* type, const std::vector<uint8_t>& d) {
-        uint8_t len[4] = {(uint8_t)(d.size() >> 24), (uint8_t)(d.size() >> 16), (uint8_t)(d.size() >> 8), (uint8_t)d.size()};
-        fwrite(len, 1, 4, f);
-        std::vector<uint8_t> td(type, type + 4);
-        td.insert(td.end(), d.begin(), d.end());
-        fwrite(td.data(), 1, td.size(), f);
-        const uint32_t c = crc32(td.data(), td.size()) ^ 0xffffffffu;
-        uint8_t cb[4] = {(uint8_t)(c >> 24), (uint8_t)(c >> 16), (uint8_t)(c >> 8), (uint8_t)c};
-        fwrite(cb, 1, 4, f);
-    };
-    std::vector<uint8_t> ihdr = {(uint8_t)(w >> 24), (uint8_t)(w >> 16), (uint8_t)(w >> 8), (uint8_t)w,
-                                 (uint8_t)(h >> 24), (uint8_t)(h >> 16), (uint8_t)(h >> 8), (uint8_t)h,
-                                 8, 2, 0, 0, 0};
-    chunk("IHDR", ihdr);
-    chunk("IDAT", z);
-    chunk("IEND", {});
-    const bool ok = ferror(f) == 0;
-    fclose(f);
-    if (!ok) err = "cannot save " + path;
-    return ok;
-}
-
-bool write_ppm(const std::string& path, const std::vector<uint8_t>& rgb, uint32_t w, uint32_t h, std::string& err) {
-    FILE* f = fopen(path.c_str(), "wb");
-    if (!f) {
-        err = "cannot save " + path + ": " + strerror(errno);
-        return false;
-    }
-    fprintf(f, "P6\n%u %u\n255\n", w, h);
-    fwrite(rgb.data(), 1, rgb.size(), f);
-    fclose(f);
-    return true;
 }
 
 double now_s() {
@@ -307,11 +228,9 @@ int main(int argc, char** argv) {
         }
     }
     pt_destroy(ctx);
-    std::string err;
-    const bool ok = opt.output.size() > 4 && opt.output.substr(opt.output.size() - 4) == ".ppm"
-                        ? write_ppm(opt.output, rgb, opt.width, opt.height, err)
-                        : write_png(opt.output, rgb, opt.width, opt.height, err);
-    if (!ok) return fail("output", err);
+    char werr[512] = {0};
+    if (ptw_write_image(opt.output.c_str(), rgb.data(), opt.width, opt.height, werr, sizeof werr))
+        return fail("output", werr);
     fprintf(stderr, "Saved %s in %.1fs\n", opt.output.c_str(), now_s() - started);
     return 0;
 }

@@ -306,6 +306,15 @@ def read_image(path) -> np.ndarray:
     return out
 
 
+def write_image(path, rgb: np.ndarray) -> None:
+    """Save (height, width, 3) uint8 pixels as .png, .jpg/.jpeg, .webp (lossless) or .ppm."""
+    a = np.ascontiguousarray(rgb, dtype=np.uint8)
+    err = C.create_string_buffer(512)
+    rc = load().ptw_write_image(str(path).encode(), a.ctypes.data, a.shape[1], a.shape[0], err, len(err))
+    if rc != abi.PT_OK:
+        raise PathTracerError(rc, err.value.decode())
+
+
 def decode_texture(data: bytes) -> np.ndarray:
     """A PNG or JPEG image in memory as (height, width, 4) uint8 RGBA, converted as the glTF importer does."""
     lib = load()

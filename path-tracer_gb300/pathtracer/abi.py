@@ -240,6 +240,7 @@ SIGNATURES = {
     "ptw_set_skybox_rgba": (C.c_int, [_vp, _vp, c_u32, c_u32]),
     "ptw_set_skybox_file": (C.c_int, [_vp, C.c_char_p, C.c_char_p, C.c_size_t]),
     "ptw_read_image_rgba": (C.c_int, [C.c_char_p, _vp, c_u64, P(c_u32), P(c_u32), C.c_char_p, C.c_size_t]),
+    "ptw_write_image": (C.c_int, [C.c_char_p, _vp, c_u32, c_u32, C.c_char_p, C.c_size_t]),
     "ptw_decode_texture_rgba8": (C.c_int, [_vp, C.c_size_t, _vp, c_u64, P(c_u32), P(c_u32), C.c_char_p, C.c_size_t]),
     "ptw_set_procedural_skybox": (C.c_int, [_vp, c_u32, c_u32]),
     "ptw_edit_skybox_average_luminance": (C.c_int, [_vp, c_f]),

@@ -2,7 +2,8 @@
 subcommand, headless.rs:15-285): flag validation on the host, and on the GPU
 an image equal to the one the library renders through the same tile loop
 (render_tiles) for the built-in room and for a glTF scene under an OpenEXR
-sky, written as a PNG that decodes back to the same bytes."""
+sky, written as PNG, lossless WebP or PPM that decode back to the same
+bytes."""
 import subprocess
 
 import numpy as np
@@ -26,7 +27,7 @@ def run(*args, timeout=300):
     (["render", "--skybox-luminance", "-1"], "nonnegative"),
     (["render", "--width", "0"], "--width"),
     (["render", "--samples", "-3"], "--samples"),
-    (["render", "--output", "x.jpg"], ".png extension"),
+    (["render", "--output", "x.bmp"], "must have a .png, .jpg, .jpeg, or .webp extension"),
     (["render", "--frobnicate", "1"], "unknown flag"),
     (["render", "--scene"], "missing value"),
 ])
@@ -41,8 +42,9 @@ def _png_rgb(path):
 
 
 @pytest.mark.gpu
-def test_cornell_render_matches_library(tmp_path):
-    out = tmp_path / "room.png"
+@pytest.mark.parametrize("ext", ["png", "webp"])
+def test_cornell_render_matches_library(tmp_path, ext):
+    out = tmp_path / f"room.{ext}"
     r = run("render", "--scene", "cornell", "--width", "72", "--height", "40", "--samples", "5",
             "--max-bounces", "3", "--tile-size", "32", "--camera-yaw", "10", "--output", str(out))
     assert r.returncode == 0, r.stderr
@@ -54,7 +56,12 @@ def test_cornell_render_matches_library(tmp_path):
     tr.set_max_bounces(3)
     want = pt.render_tiles(tr, 72, 40, 5, 32)
     tr.close()
-    np.testing.assert_array_equal(_png_rgb(out), want)
+    if ext == "png":
+        got = _png_rgb(out)
+    else:
+        from test_image_out import webp_pixels
+        got = webp_pixels(out.read_bytes())
+    np.testing.assert_array_equal(got, want)
 
 
 @pytest.mark.gpu
