@@ -88,10 +88,11 @@ int ptw_build(ptw_world* world);
 int ptw_set_skybox_rgba(ptw_world* world, const float* rgba, uint32_t width, uint32_t height);
 
 /* Skybox::new on an image file (the reference decodes its skybox asset with
- * an image library, world.rs:1872-1880): Radiance RGBE (.hdr, "-Y H +X W")
- * or single-part scanline OpenEXR (HALF/FLOAT/UINT channels R, G, B [, A] or
- * Y; compression NONE, RLE, ZIPS, ZIP or PIZ), chosen by the file's magic
- * bytes.  On failure `error` (if given) receives the reason and the skybox is
+ * an image library, world.rs:1872-1880): Radiance RGBE (.hdr, "-Y H +X W"),
+ * single-part scanline OpenEXR (HALF/FLOAT/UINT channels R, G, B [, A] or
+ * Y; compression NONE, RLE, ZIPS, ZIP or PIZ), or a PNG / JPEG image (8- or
+ * 16-bit samples divided by their maximum, as the library converts them),
+ * chosen by the file's magic bytes.  On failure `error` (if given) receives the reason and the skybox is
  * unchanged. */
 int ptw_set_skybox_file(ptw_world* world, const char* path, char* error, size_t error_size);
 /* the same from an image held in memory, as World::replace_skybox(bytes)

@@ -1496,10 +1496,44 @@ bool decode_texture(const uint8_t* d, size_t n, std::vector<uint8_t>& rgba, uint
     return true;
 }
 
+// an 8- or 16-bit raster to RGBA32F as the image library's conversion does:
+// samples divided by their maximum, grey replicated to RGB, alpha 1 if absent
+void raster_to_rgba32f(const Raster& r, std::vector<float>& rgba) {
+    const float inv = 1.0f / (r.depth == 16 ? 65535.0f : 255.0f);
+    rgba.assign((size_t)r.w * r.h * 4, 1.0f);
+    for (size_t i = 0; i < (size_t)r.w * r.h; ++i) {
+        const uint16_t* s = &r.v[i * r.channels];
+        float* o = &rgba[i * 4];
+        if (r.channels <= 2) {
+            o[0] = o[1] = o[2] = s[0] * inv;
+            if (r.channels == 2) o[3] = s[1] * inv;
+        } else {
+            for (int k = 0; k < r.channels; ++k) o[k] = s[k] * inv;
+        }
+    }
+}
+
 bool decode_image(const std::vector<uint8_t>& data, std::vector<float>& rgba, uint32_t& w, uint32_t& h,
                   std::string& err, bool size_only = false) {
     if (data.size() >= 4 && data[0] == 0x76 && data[1] == 0x2f && data[2] == 0x31 && data[3] == 0x01)
         return read_exr(data, rgba, w, h, err, size_only);
+    const bool png = data.size() >= 8 && data[0] == 0x89 && data[1] == 'P' && data[2] == 'N' && data[3] == 'G';
+    const bool jpeg = data.size() >= 2 && data[0] == 0xff && data[1] == 0xd8;
+    if (png || jpeg) {  // low dynamic range skyboxes
+        Raster r;
+        constexpr uint32_t kMaxSide = 65536;
+        if (!(png ? decode_png(data.data(), data.size(), r, err, kMaxSide)
+                  : decode_jpeg(data.data(), data.size(), r, err, kMaxSide)))
+            return false;
+        w = r.w;
+        h = r.h;
+        if ((uint64_t)w * h > (uint64_t)kMaxSkyPixels) {
+            err = "image too large";
+            return false;
+        }
+        if (!size_only) raster_to_rgba32f(r, rgba);
+        return true;
+    }
     return read_hdr(data, rgba, w, h, err, size_only);
 }
 

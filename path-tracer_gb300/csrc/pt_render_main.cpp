@@ -10,8 +10,8 @@
 // Scenes: a glTF 2.0 file (.glb or .gltf, PNG/JPEG textures; the
 // reference's default is its box.glb asset), "cornell" (36-triangle Cornell
 // box) or "procedural[:SEED]" (the ~2.1M-triangle procedural scene).
-// Skyboxes: "black", "procedural" (gradient + sun), a Radiance .hdr or an
-// OpenEXR .exr file.  Output: .png, .jpg / .jpeg, .webp (lossless) or .ppm.
+// Skyboxes: "black", "procedural" (gradient + sun), or a Radiance .hdr,
+// OpenEXR .exr, PNG or JPEG file (WebP skyboxes are not decoded).  Output: .png, .jpg / .jpeg, .webp (lossless) or .ppm.
 #include <algorithm>
 #include <cerrno>
 #include <chrono>

@@ -541,3 +541,27 @@ def test_skybox_file_equals_pixels(tmp_path):
         a.set_skybox_file(tmp_path / "missing.hdr")
     a.close()
     b.close()
+
+
+def test_ldr_skybox_files(tmp_path):
+    # PNG and JPEG skyboxes, as the reference's image library loads them: samples / max, grey replicated
+    from test_texture_io import QUANT, _test_image, encode_jpeg, write_png
+    rng = np.random.default_rng(7)
+    rgb16 = rng.integers(0, 65536, size=(8, 16, 3))
+    (tmp_path / "a.png").write_bytes(write_png(rgb16, 2, 16))
+    got = read(tmp_path / "a.png")
+    want = np.concatenate([(rgb16 / 65535.0).astype(np.float32), np.ones((8, 16, 1), np.float32)], -1)
+    np.testing.assert_allclose(got, want, rtol=1e-6)
+    grey_alpha = rng.integers(0, 256, size=(8, 16, 2))
+    (tmp_path / "b.png").write_bytes(write_png(grey_alpha, 4, 8))
+    got = read(tmp_path / "b.png")
+    np.testing.assert_allclose(got[..., 0], grey_alpha[..., 0] / 255.0, rtol=1e-6)
+    np.testing.assert_allclose(got[..., 2], grey_alpha[..., 0] / 255.0, rtol=1e-6)
+    np.testing.assert_allclose(got[..., 3], grey_alpha[..., 1] / 255.0, rtol=1e-6)
+    jpg, _ = encode_jpeg(_test_image(16, 32, 2), [(1, 1), (1, 1), (1, 1)], QUANT)
+    (tmp_path / "c.jpg").write_bytes(jpg)
+    got = read(tmp_path / "c.jpg")
+    np.testing.assert_allclose(got[..., :3], pt.decode_texture(jpg)[..., :3] / 255.0, rtol=1e-6)
+    w = pt.World.cornell_box()
+    w.set_skybox_file(tmp_path / "c.jpg")  # and the world accepts it
+    w.close()
