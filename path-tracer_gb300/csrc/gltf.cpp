@@ -463,12 +463,83 @@ struct Loader {
         return true;
     }
 
+    // one component of a float accessor; normalised integers map to [0, 1] / [-1, 1]
+    static bool component(const uint8_t* e, long ctype, bool norm, float* out) {
+        float v;
+        switch (ctype) {
+            case 5126: memcpy(&v, e, 4); break;
+            case 5121: v = norm ? (float)e[0] / 255.0f : (float)e[0]; break;
+            case 5120: {
+                const int8_t s = (int8_t)e[0];
+                v = norm ? std::fmax((float)s / 127.0f, -1.0f) : (float)s;
+                break;
+            }
+            case 5123: {
+                uint16_t u;
+                memcpy(&u, e, 2);
+                v = norm ? (float)u / 65535.0f : (float)u;
+                break;
+            }
+            case 5122: {
+                int16_t s;
+                memcpy(&s, e, 2);
+                v = norm ? std::fmax((float)s / 32767.0f, -1.0f) : (float)s;
+                break;
+            }
+            case 5125: {
+                uint32_t u;
+                memcpy(&u, e, 4);
+                v = (float)u;
+                break;
+            }
+            default: return false;
+        }
+        *out = v;
+        return true;
+    }
+
+    // the sparse substitution of accessor `a` (glTF 2.0 3.6.2.3): `count`
+    // element indices (unsigned, strictly increasing) and their values
+    // replace elements of the dense (or all-zero) data; `put(i, bytes)`
+    // stores one element read from the values view
+    template <class Put>
+    bool sparse(const Json& a, size_t n, size_t elem, Put&& put) {
+        const Json* sp = a.get("sparse");
+        if (!sp) return true;
+        const size_t cnt = (size_t)sp->integer("count", 0);
+        const Json* ind = sp->get("indices");
+        const Json* val = sp->get("values");
+        if (!ind || !val || cnt == 0 || cnt > n) return fail("malformed sparse accessor");
+        const long ict = ind->integer("componentType", 0);
+        const size_t isz = ict == 5125 ? 4 : ict == 5123 ? 2 : ict == 5121 ? 1 : 0;
+        if (!isz) return fail("sparse indices must be unsigned integers");
+        const uint8_t *ib, *vb;
+        size_t ist, iav, vst, vav;
+        if (!view(ind->integer("bufferView", -1), ind->integer("byteOffset", 0), isz, &ib, &ist, &iav) ||
+            !view(val->integer("bufferView", -1), val->integer("byteOffset", 0), elem, &vb, &vst, &vav))
+            return false;
+        if (cnt * isz > iav || cnt * elem > vav) return fail("sparse accessor runs past its buffer view");
+        for (size_t k = 0; k < cnt; ++k) {
+            uint32_t i = 0;
+            if (isz == 4) memcpy(&i, ib + k * isz, 4);
+            else if (isz == 2) {
+                uint16_t u;
+                memcpy(&u, ib + k * isz, 2);
+                i = u;
+            } else {
+                i = ib[k];
+            }
+            if (i >= n) return fail("sparse index out of range");
+            if (!put(i, vb + k * elem)) return fail("unsupported accessor component type");
+        }
+        return true;
+    }
+
     // accessor i as float components (count x ncomp), normalised integers mapped to [0, 1] / [-1, 1]
     bool read_floats(long index, int want_comps, std::vector<float>& out, size_t* count) {
         const Json* accs = doc.get("accessors");
         if (!accs || index < 0 || (size_t)index >= accs->arr.size()) return fail("accessor out of range");
         const Json& a = accs->arr[(size_t)index];
-        if (a.get("sparse")) return fail("sparse accessors are not supported");
         const std::string type = a.string("type", "");
         const int comps = type == "SCALAR" ? 1 : type == "VEC2" ? 2 : type == "VEC3" ? 3 : type == "VEC4" ? 4 : 0;
         if (comps != want_comps) return fail("accessor has type " + type);
@@ -478,71 +549,59 @@ struct Loader {
         const int csize = ctype == 5126 || ctype == 5125 ? 4 : ctype == 5123 || ctype == 5122 ? 2 : 1;
         out.assign(n * comps, 0.0f);
         *count = n;
-        if (!a.get("bufferView")) return true;  // all zeros
-        const uint8_t* base;
-        size_t stride, avail;
-        if (!view(a.integer("bufferView", -1), a.integer("byteOffset", 0), (size_t)csize * comps, &base, &stride, &avail))
-            return false;
-        if (n && (n - 1) * stride + (size_t)csize * comps > avail) return fail("accessor runs past its buffer view");
-        for (size_t i = 0; i < n; ++i)
-            for (int c = 0; c < comps; ++c) {
-                const uint8_t* e = base + i * stride + (size_t)c * csize;
-                float v;
-                switch (ctype) {
-                    case 5126: memcpy(&v, e, 4); break;
-                    case 5121: v = norm ? (float)e[0] / 255.0f : (float)e[0]; break;
-                    case 5120: {
-                        const int8_t s = (int8_t)e[0];
-                        v = norm ? std::fmax((float)s / 127.0f, -1.0f) : (float)s;
-                        break;
-                    }
-                    case 5123: {
-                        uint16_t u;
-                        memcpy(&u, e, 2);
-                        v = norm ? (float)u / 65535.0f : (float)u;
-                        break;
-                    }
-                    case 5122: {
-                        int16_t s;
-                        memcpy(&s, e, 2);
-                        v = norm ? std::fmax((float)s / 32767.0f, -1.0f) : (float)s;
-                        break;
-                    }
-                    default: return fail("unsupported accessor component type");
-                }
-                out[i * comps + c] = v;
-            }
-        return true;
+        const size_t elem = (size_t)csize * comps;
+        if (a.get("bufferView")) {  // else all zeros before the sparse substitution
+            const uint8_t* base;
+            size_t stride, avail;
+            if (!view(a.integer("bufferView", -1), a.integer("byteOffset", 0), elem, &base, &stride, &avail))
+                return false;
+            if (n && (n - 1) * stride + elem > avail) return fail("accessor runs past its buffer view");
+            for (size_t i = 0; i < n; ++i)
+                for (int c = 0; c < comps; ++c)
+                    if (!component(base + i * stride + (size_t)c * csize, ctype, norm, &out[i * comps + c]))
+                        return fail("unsupported accessor component type");
+        }
+        return sparse(a, n, elem, [&](uint32_t i, const uint8_t* e) {
+            for (int c = 0; c < comps; ++c)
+                if (!component(e + (size_t)c * csize, ctype, norm, &out[(size_t)i * comps + c])) return false;
+            return true;
+        });
     }
 
     bool read_indices(long index, std::vector<uint32_t>& out) {
         const Json* accs = doc.get("accessors");
         if (!accs || index < 0 || (size_t)index >= accs->arr.size()) return fail("accessor out of range");
         const Json& a = accs->arr[(size_t)index];
-        if (a.get("sparse")) return fail("sparse accessors are not supported");
         const long ctype = a.integer("componentType", 0);
         const int csize = ctype == 5125 ? 4 : ctype == 5123 ? 2 : ctype == 5121 ? 1 : 0;
         if (!csize || a.string("type", "") != "SCALAR") return fail("index accessor must be unsigned SCALAR");
         const size_t n = (size_t)a.integer("count", 0);
         out.assign(n, 0u);
-        if (!a.get("bufferView")) return true;
-        const uint8_t* base;
-        size_t stride, avail;
-        if (!view(a.integer("bufferView", -1), a.integer("byteOffset", 0), (size_t)csize, &base, &stride, &avail))
-            return false;
-        if (n && (n - 1) * stride + (size_t)csize > avail) return fail("index accessor runs past its buffer view");
-        for (size_t i = 0; i < n; ++i) {
-            const uint8_t* e = base + i * stride;
-            if (csize == 4) memcpy(&out[i], e, 4);
-            else if (csize == 2) {
+        const auto get = [&](const uint8_t* e) -> uint32_t {
+            if (csize == 4) {
+                uint32_t u;
+                memcpy(&u, e, 4);
+                return u;
+            }
+            if (csize == 2) {
                 uint16_t u;
                 memcpy(&u, e, 2);
-                out[i] = u;
-            } else {
-                out[i] = e[0];
+                return u;
             }
+            return e[0];
+        };
+        if (a.get("bufferView")) {
+            const uint8_t* base;
+            size_t stride, avail;
+            if (!view(a.integer("bufferView", -1), a.integer("byteOffset", 0), (size_t)csize, &base, &stride, &avail))
+                return false;
+            if (n && (n - 1) * stride + (size_t)csize > avail) return fail("index accessor runs past its buffer view");
+            for (size_t i = 0; i < n; ++i) out[i] = get(base + i * stride);
         }
-        return true;
+        return sparse(a, n, (size_t)csize, [&](uint32_t i, const uint8_t* e) {
+            out[i] = get(e);
+            return true;
+        });
     }
 
     bool view(long index, long offset, size_t elem, const uint8_t** base, size_t* stride, size_t* avail) {

@@ -226,3 +226,41 @@ def write_png_solid(w, h):
     raw = (b"\0" + b"\x10\x20\x30" * w) * h
     return (b"\x89PNG\r\n\x1a\n" + _chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0))
             + _chunk(b"IDAT", zlib.compress(raw, 1)) + _chunk(b"IEND", b""))
+
+
+def test_sparse_accessors(tmp_path):
+    # POSITION with a sparse substitution of vertices 1 and 3, and a sparse-only (no bufferView) TEXCOORD_0
+    pos, nor, uv, idx = quad()
+    sp_idx = np.array([1, 3], np.uint16).tobytes()
+    sp_pos = np.array([[2, 0, 0], [0, 3, 0]], np.float32).tobytes()
+    sp_uv_idx = np.array([2], np.uint8).tobytes() + b"\0\0\0"
+    sp_uv = np.array([[0.25, 0.75]], np.float32).tobytes()
+    blobs = [pos.tobytes(), nor.tobytes(), idx.tobytes() + b"\0\0", sp_idx, sp_pos, sp_uv_idx, sp_uv]
+    views, off = [], 0
+    for b in blobs:
+        views.append({"buffer": 0, "byteOffset": off, "byteLength": len(b)})
+        off += len(b)
+    accessors = [
+        {"bufferView": 0, "componentType": 5126, "count": 4, "type": "VEC3",
+         "sparse": {"count": 2, "indices": {"bufferView": 3, "componentType": 5123},
+                    "values": {"bufferView": 4}}},
+        {"bufferView": 1, "componentType": 5126, "count": 4, "type": "VEC3"},
+        {"bufferView": 2, "componentType": 5123, "count": 6, "type": "SCALAR"},
+        {"componentType": 5126, "count": 4, "type": "VEC2",
+         "sparse": {"count": 1, "indices": {"bufferView": 5, "componentType": 5121}, "values": {"bufferView": 6}}},
+    ]
+    data = b"".join(blobs)
+    doc = {"asset": {"version": "2.0"}, "scene": 0, "scenes": [{"nodes": [0]}], "nodes": [{"mesh": 0}],
+           "meshes": [{"primitives": [{"attributes": {"POSITION": 0, "NORMAL": 1, "TEXCOORD_0": 3}, "indices": 2}]}],
+           "accessors": accessors, "bufferViews": views,
+           "buffers": [{"byteLength": len(data), "uri": "data:application/octet-stream;base64," +
+                        base64.b64encode(data).decode()}]}
+    path = tmp_path / "sparse.gltf"
+    path.write_text(json.dumps(doc))
+    w = pt.World.from_gltf(path)
+    g = w.geometries()[np.argsort(w.bvh_order())].reshape(2, 3, 3)
+    np.testing.assert_array_equal(g[0], [[0, 0, 0], [2, 0, 0], [1, 1, 0]])  # triangle (0, 1, 2)
+    np.testing.assert_array_equal(g[1], [[0, 0, 0], [1, 1, 0], [0, 3, 0]])  # triangle (0, 2, 3)
+    a = w.attributes_raw()[np.argsort(w.bvh_order())].view(np.float32).reshape(2, 28)
+    np.testing.assert_array_equal(a[0, 10:16], [0, 0, 0, 0, 0.25, 0.75])  # uv of vertex 2 from the sparse values
+    w.close()
