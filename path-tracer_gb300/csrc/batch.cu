@@ -100,6 +100,15 @@ __global__ void plan_kernel(Ctrl* ctrl, const ItemDev* ring, uint64_t ring_cap, 
 }
 
 // one block per item (grid-stride over the wave's items)
+// path order within a work item: the wavefront kernels' order (PT_PIXEL_MAJOR)
+PTD uint32_t item_path(uint32_t s, uint32_t pix, uint32_t px_count, uint32_t samples) {
+#if PT_PIXEL_MAJOR
+    return pix * samples + s;
+#else
+    return s * px_count + pix;
+#endif
+}
+
 __global__ void __launch_bounds__(256) raygen_kernel(const Ctrl* ctrl, const ItemDev* ring, const JobDev* jobs,
                                                      WaveBufs b) {
     const uint32_t n_items = ctrl->wave_items;
@@ -111,7 +120,11 @@ __global__ void __launch_bounds__(256) raygen_kernel(const Ctrl* ctrl, const Ite
         const uint32_t paths = px_count * it.samples;
         const uint32_t tag = (it.slot << 8) | job.scene;
         for (uint32_t i = threadIdx.x; i < paths; i += blockDim.x) {
+#if PT_PIXEL_MAJOR
+            const uint32_t pix = i / it.samples, s = i - pix * it.samples;  // a pixel's samples adjacent
+#else
             const uint32_t s = i / px_count, pix = i - s * px_count;
+#endif
             const uint32_t gy = pix / it.w, gx = pix - gy * it.w;
             const uint32_t px = it.x0 + gx, py = it.y0 + gy;
             const uint32_t p = off + i;
@@ -293,7 +306,7 @@ __global__ void __launch_bounds__(256) accumulate_kernel(const Ctrl* ctrl, const
                     comp = mk(k.x, k.y, k.z);
                 }
                 for (uint32_t s = 0; s < it.samples; ++s, ++n) {
-                    const float4 c = b.q.color[off + s * px_count + pix];
+                    const float4 c = b.q.color[off + item_path(s, pix, px_count, it.samples)];
                     const f3 y = mk(c.x, c.y, c.z) - comp;
                     const f3 sum = acc + y;
                     comp = (sum - acc) - y;
@@ -302,7 +315,7 @@ __global__ void __launch_bounds__(256) accumulate_kernel(const Ctrl* ctrl, const
                 job.comp[idx] = make_float4(comp.x, comp.y, comp.z, 0.0f);
             } else {
                 for (uint32_t s = 0; s < it.samples; ++s, ++n) {
-                    const float4 c = b.q.color[off + s * px_count + pix];
+                    const float4 c = b.q.color[off + item_path(s, pix, px_count, it.samples)];
                     acc = (n > 1u ? acc : mk(0.0f, 0.0f, 0.0f)) + mk(c.x, c.y, c.z);
                 }
             }

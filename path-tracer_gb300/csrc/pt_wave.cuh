@@ -100,6 +100,11 @@ constexpr uint32_t kWideLeafMerge = PT_WIDE_LEAF_MERGE;
 #ifndef PT_TRI_PER_STEP
 #define PT_TRI_PER_STEP 1
 #endif
+// 1: a pixel's samples are consecutive paths of a group / work item
+// (camera rays of a warp share their first nodes); 0: sample-major
+#ifndef PT_PIXEL_MAJOR
+#define PT_PIXEL_MAJOR 1
+#endif
 constexpr int kExtendThreads = PT_EXTEND_THREADS;
 constexpr int kShadeThreads = PT_SHADE_THREADS;
 // entries at the top of each traversal lane's stack kept in shared memory

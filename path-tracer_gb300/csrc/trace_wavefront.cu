@@ -36,6 +36,27 @@ struct Group {
     uint32_t record_sample;  // sample offset of the group within the pt_trace call
 };
 
+// Path order within a group.  Pixel-major (PT_PIXEL_MAJOR 1): a pixel's
+// samples are consecutive paths, so a warp's camera rays are 32 jittered
+// rays through two pixels and traverse almost the same nodes; sample-major:
+// consecutive pixels of one sample.  Only the order of work changes.
+PTD void split_path(uint32_t p, const Group& g, uint32_t* s, uint32_t* pix) {
+#if PT_PIXEL_MAJOR
+    *pix = p / g.samples;
+    *s = p - *pix * g.samples;
+#else
+    *s = p / g.pixels;
+    *pix = p - *s * g.pixels;
+#endif
+}
+PTD size_t path_of(uint32_t s, uint32_t pix, const Group& g) {
+#if PT_PIXEL_MAJOR
+    return (size_t)pix * g.samples + s;
+#else
+    return (size_t)s * g.pixels + pix;
+#endif
+}
+
 template <bool kRec>
 __global__ void __launch_bounds__(256) raygen_kernel(World w, ptk::Tile t, Group g, Queues q) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -44,7 +65,8 @@ __global__ void __launch_bounds__(256) raygen_kernel(World w, ptk::Tile t, Group
         q.cnt[1] = 0u;
     }
     if (p >= g.paths) return;
-    const uint32_t s = p / g.pixels, pix = p - s * g.pixels;
+    uint32_t s, pix;
+    split_path(p, g, &s, &pix);
     const uint32_t gy = pix / g.vis_w, gx = pix - gy * g.vis_w;
     const uint32_t px = gx + t.origin_x, py = gy + t.origin_y;
     Counters c;
@@ -239,7 +261,7 @@ __global__ void accumulate_kernel(ptk::Tile t, Group g, const float4* color) {
             comp = mk(k.x, k.y, k.z);
         }
         for (uint32_t s = 0; s < g.samples; ++s, ++n) {
-            const float4 c = color[(size_t)s * g.pixels + pix];
+            const float4 c = color[path_of(s, pix, g)];
             const f3 y = mk(c.x, c.y, c.z) - comp;
             const f3 sum = acc + y;
             comp = (sum - acc) - y;
@@ -248,7 +270,7 @@ __global__ void accumulate_kernel(ptk::Tile t, Group g, const float4* color) {
         t.comp[idx] = make_float4(comp.x, comp.y, comp.z, 0.0f);
     } else {
         for (uint32_t s = 0; s < g.samples; ++s, ++n) {
-            const float4 c = color[(size_t)s * g.pixels + pix];
+            const float4 c = color[path_of(s, pix, g)];
             acc = (n > 1u ? acc : mk(0.0f, 0.0f, 0.0f)) + mk(c.x, c.y, c.z);
         }
     }
@@ -261,7 +283,8 @@ __global__ void accumulate_kernel(ptk::Tile t, Group g, const float4* color) {
 __global__ void finalize_records_kernel(ptk::Tile t, Group g, Queues q, ptk::Sinks sinks) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= g.paths) return;
-    const uint32_t s = p / g.pixels, pix = p - s * g.pixels;
+    uint32_t s, pix;
+    split_path(p, g, &s, &pix);
     const uint32_t gy = pix / g.vis_w, gx = pix - gy * g.vis_w;
     const Counters c = q.rec[p];
     const float4 col = q.color[p];
