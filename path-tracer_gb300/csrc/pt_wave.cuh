@@ -32,7 +32,8 @@ struct Queues {
     uint32_t* miss_list;  // slots whose ray left the scene
     uint32_t* hit_sorted = nullptr;  // the hit list sorted by key (when cnt[7] != 0)
     uint32_t* cnt;  // [0], [1] ray queue lengths, [2] shadow length, [3] extend fetch, [4] shadow fetch,
-                    // [5] hit list length, [6] miss list length, [7] 1 if hit_sorted holds this bounce's hits
+                    // [5] hit list length, [6] miss list length, [7] 1 if hit_sorted holds this bounce's hits,
+                    // [8] 1 if hit_sorted holds the order of the current ray queue, [9] of the shadow queue
     Counters* rec;  // per path (recording variants)
     int32_t* rec_hits;
 };
@@ -99,6 +100,16 @@ constexpr uint32_t kWideLeafMerge = PT_WIDE_LEAF_MERGE;
 // 1: a traversal step tests one triangle of a leaf; 0: a whole leaf
 #ifndef PT_TRI_PER_STEP
 #define PT_TRI_PER_STEP 1
+#endif
+// order the next bounce's rays / the shadow rays by direction octant before
+// their traversal (when the hit sort is on and a queue holds at least its
+// threshold); measured slower: the octant split breaks up the origin
+// coherence the hit sort gives the next rays, so off by default
+#ifndef PT_RAY_ORDER
+#define PT_RAY_ORDER 0
+#endif
+#ifndef PT_SHADOW_ORDER
+#define PT_SHADOW_ORDER 0
 #endif
 // 1: a pixel's samples are consecutive paths of a group / work item
 // (camera rays of a warp share their first nodes); 0: sample-major
@@ -798,6 +809,76 @@ __global__ void __launch_bounds__(kSortThreads) sort_count_kernel(World w, Queue
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < kSortBuckets; i += blockDim.x)
         if (hist[i]) atomicAdd(&counts[i], hist[i]);
+}
+
+// Ray ordering: the slots of a ray queue (the next bounce's rays, or the
+// shadow rays) grouped by direction octant, written to `order`; within an
+// octant, slots keep roughly their queue order (which follows the sorted
+// hits, so origins stay close).  A warp of the traversal then holds rays
+// whose near-child choices agree more often.  Only the processing order
+// changes.  `flag` (a counter slot) is 1 when `order` is valid.
+PTD uint32_t octant(float4 d) { return (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u); }
+
+// (templates, as the other sort kernels, so that both translation units may include them)
+template <int kUnused>
+__global__ void __launch_bounds__(kSortThreads) ray_count_kernel(const float4* d, const uint32_t* count,
+                                                                 uint32_t* counts, uint32_t min_rays) {
+    __shared__ uint32_t hist[8];
+    const uint32_t n = *count;
+    if (n < min_rays) return;
+    if (threadIdx.x < 8) hist[threadIdx.x] = 0u;
+    __syncthreads();
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        atomicAdd(&hist[octant(d[j])], 1u);
+    __syncthreads();
+    if (threadIdx.x < 8 && hist[threadIdx.x]) atomicAdd(&counts[threadIdx.x], hist[threadIdx.x]);
+}
+
+template <int kUnused>
+__global__ void ray_scan_kernel(const uint32_t* count, uint32_t* counts, uint32_t* offsets, uint32_t* flag,
+                                uint32_t min_rays) {
+    if (*count < min_rays) {
+        *flag = 0u;
+        return;
+    }
+    uint32_t base = 0;
+    for (int k = 0; k < 8; ++k) {
+        offsets[k] = base;
+        base += counts[k];
+        counts[k] = 0u;
+    }
+    *flag = 1u;
+}
+
+template <int kUnused>
+__global__ void __launch_bounds__(kSortThreads) ray_scatter_kernel(const float4* d, const uint32_t* count,
+                                                                   uint32_t* offsets, uint32_t* order,
+                                                                   uint32_t min_rays) {
+    __shared__ uint32_t hist[8];
+    const uint32_t n = *count;
+    if (n < min_rays) return;
+    const uint32_t chunk = kSortThreads * kSortItems;
+    for (uint32_t c0 = blockIdx.x * chunk; c0 < n; c0 += gridDim.x * chunk) {
+        if (threadIdx.x < 8) hist[threadIdx.x] = 0u;
+        __syncthreads();
+        uint32_t keys[kSortItems];
+#pragma unroll
+        for (int k = 0; k < kSortItems; ++k) {
+            const uint32_t j = c0 + (uint32_t)k * kSortThreads + threadIdx.x;
+            keys[k] = 0xffffffffu;
+            if (j < n) {
+                keys[k] = octant(d[j]);
+                atomicAdd(&hist[keys[k]], 1u);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 8 && hist[threadIdx.x]) hist[threadIdx.x] = atomicAdd(&offsets[threadIdx.x], hist[threadIdx.x]);
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kSortItems; ++k)
+            if (keys[k] != 0xffffffffu) order[atomicAdd(&hist[keys[k]], 1u)] = c0 + (uint32_t)k * kSortThreads + threadIdx.x;
+        __syncthreads();
+    }
 }
 
 // one block of 1024 threads, kSortPerThread buckets each

@@ -99,6 +99,8 @@ __global__ void bounce_reset_kernel(uint32_t* cnt, int next) {
     cnt[5] = 0u;
     cnt[6] = 0u;
     cnt[7] = 0u;
+    cnt[8] = 0u;
+    cnt[9] = 0u;
 }
 
 // Persistent extend kernel: every lane traverses its own ray and takes a new
@@ -111,6 +113,7 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
     static_assert(!(kWide && (kRec || kAlpha)), "the wide form keeps no records and runs opaque scenes only");
     const Stage st = stage_of(q, cur);
     const uint32_t count = *st.count;
+    const bool ordered = PT_RAY_ORDER && q.cnt[8] != 0u;
     typename std::conditional<kWide, WideTraverser<false, kTri36>, Traverser<kRec, kAlpha, false, kTri36>>::type tr;
     constexpr uint32_t kShared = kWide ? kWideSmemStack : kSmemStack;
     __shared__ uint2 stack_top[kShared > 0u ? kShared * kExtendThreads : 1u];
@@ -123,8 +126,8 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
     lane_refill_loop(
         &q.cnt[3], count, kWide ? kWideStepsPerRefill : kStepsPerRefill, kRefillBelow,
         [&](uint32_t i) {
-            slot = i;
-            const float4 o4 = st.o[i], d4 = st.d[i];
+            slot = ordered ? q.hit_sorted[i] : i;
+            const float4 o4 = st.o[slot], d4 = st.d[slot];
             path = __float_as_uint(o4.w);
             tr.rng.s = __float_as_uint(d4.w);
             if constexpr (kRec) tr.c = q.rec[path];
@@ -211,6 +214,7 @@ template <bool kRec, bool kTri36 = false, bool kWide = false>
 __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : PT_EXTEND_MIN_BLOCKS) shadow_kernel(World w, Fast f, Queues q) {
     static_assert(!(kWide && kRec), "the wide form keeps no records");
     const uint32_t count = q.cnt[2];
+    const bool ordered = PT_SHADOW_ORDER && q.cnt[9] != 0u;
     typename std::conditional<kWide, WideTraverser<true, kTri36>, Traverser<kRec, false, true, kTri36>>::type tr;
     constexpr uint32_t kShared = kWide ? kWideSmemStack : kSmemStack;
     __shared__ uint2 stack_top[kShared > 0u ? kShared * kExtendThreads : 1u];
@@ -222,8 +226,9 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
     lane_refill_loop(
         &q.cnt[4], count, kWide ? kWideStepsPerRefill : kStepsPerRefill, kRefillBelow,
         [&](uint32_t i) {
-            const float4 o4 = q.so[i], d4 = q.sd[i];
-            contribution = q.sc[i];
+            const uint32_t slot = ordered ? q.hit_sorted[i] : i;
+            const float4 o4 = q.so[slot], d4 = q.sd[slot];
+            contribution = q.sc[slot];
             path = __float_as_uint(o4.w);
             if constexpr (kRec) tr.c = q.rec[path];
             tr.init(f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), d4.w, __float_as_int(contribution.w));
@@ -546,9 +551,23 @@ cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const pt
         return cudaGetLastError();
     }));
     int cur = 0;
+    const bool sorting = sort.counts && sort.min_hits != 0xffffffffu;
+    // octant order of a ray queue (current rays: flag 8, shadow rays: flag 9) into hit_sorted
+    const auto order_rays = [&](const float4* dirs, const uint32_t* count, uint32_t flag) {
+        ray_count_kernel<0><<<sms * 2, kSortThreads, 0, stream>>>(dirs, count, sort.counts, sort.min_hits);
+        ray_scan_kernel<0><<<1, 1, 0, stream>>>(count, sort.counts, sort.counts + kSortBuckets, q.cnt + flag,
+                                             sort.min_hits);
+        ray_scatter_kernel<0><<<sms * 4, kSortThreads, 0, stream>>>(dirs, count, sort.counts + kSortBuckets,
+                                                                  q.hit_sorted, sort.min_hits);
+        return cudaGetLastError();
+    };
     for (uint32_t bounce = 0; bounce <= tile.max_bounces; ++bounce) {
         bounce_reset_kernel<<<1, 1, 0, stream>>>(q.cnt, cur ^ 1);
         PTW_TRY(cudaGetLastError());
+        if (PT_RAY_ORDER && sorting && bounce > 0) {  // camera rays are coherent already (pixel-major)
+            // timed with the sorts (shading class), as the hit sort
+            PTW_TRY(timer(PT_KC_SHADE, [&] { return order_rays(cur ? q.d[1] : q.d[0], q.cnt + cur, 8u); }));
+        }
         PTW_TRY(timer(PT_KC_EXTEND, [&] {
             extend_kernel<kRec, kAlpha, kTri36, kWide><<<ext_blocks, kExtendThreads, 0, stream>>>(w, f, q, cur, bounce);
             return cudaGetLastError();
@@ -568,6 +587,9 @@ cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const pt
             return cudaGetLastError();
         }));
         if constexpr (!kAlpha) {
+            if (PT_SHADOW_ORDER && sorting) {
+                PTW_TRY(timer(PT_KC_SHADE, [&] { return order_rays(q.sd, q.cnt + 2, 9u); }));
+            }
             PTW_TRY(timer(PT_KC_SHADOW, [&] {
                 shadow_kernel<kRec, kTri36, kWide><<<shd_blocks, kExtendThreads, 0, stream>>>(w, f, q);
                 return cudaGetLastError();
