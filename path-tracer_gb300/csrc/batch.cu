@@ -926,6 +926,7 @@ bool evict_one(pt_engine* e) {
 static void pump_loop(pt_engine* e) {
     cudaSetDevice(e->cfg.device);
     while (!e->stop.load(std::memory_order_relaxed)) {
+        bool idle;
         {
             std::lock_guard<std::recursive_mutex> g(e->mu);
             if (e->sticky == PT_OK) {
@@ -933,8 +934,10 @@ static void pump_loop(pt_engine* e) {
                 if (!rc) rc = pump(e);
                 if (rc) e->sticky = rc;
             }
+            idle = e->flights.empty();  // nothing on the GPU and nothing queued by pump()
         }
-        std::this_thread::sleep_for(std::chrono::microseconds(100));
+        // while idle, a submit queues its own first wave, so a slower poll costs no latency
+        std::this_thread::sleep_for(std::chrono::microseconds(idle ? 1000 : 100));
     }
 }
 
