@@ -81,7 +81,9 @@ typedef struct pt_half_attribute {
 /* Collapse a binary BVH (the reference's layout, root at 0) into 8-wide
  * nodes: each wide node starts from a binary interior node's two children
  * and repeatedly opens its interior child of largest surface area until it
- * has 8 children or only leaves.  A binary subtree of at most
+ * has 8 children or only leaves.  The children are placed in slots so that
+ * a ray visiting slot i ^ o (i = 0..7, o = its direction's sign bits) meets
+ * them roughly nearest first.  A binary subtree of at most
  * max_leaf_triangles triangles (0: none) becomes one leaf child over its
  * contiguous triangle range.  Runs on the host.  `out` may be NULL to query
  * the count.  PT_ERR_INVALID_ARG for a malformed tree, non-finite boxes or

@@ -93,6 +93,13 @@ PTD Stage stage_of(const Queues& q, int cur) {
 #define PT_WIDE_TRI_PER_STEP 0
 #endif
 constexpr uint32_t kWideLeafMerge = PT_WIDE_LEAF_MERGE;
+// 1: the 8-wide traversal visits a node's accepted children in the order of
+// their slots XOR the ray's direction octant (the builder places children for
+// that order), with three-input min/max in the child test; 0: it sorts the
+// accepted children by entry distance
+#ifndef PT_WIDE_OCTANT
+#define PT_WIDE_OCTANT 1
+#endif
 // resident blocks per SM the 8-wide traversal kernels are compiled for
 #ifndef PT_WIDE_MIN_BLOCKS
 #define PT_WIDE_MIN_BLOCKS 8
@@ -467,11 +474,13 @@ PTD bool binary_first(const Fast& f, f3 o, f3 d, uint32_t a, uint32_t b) {
 // quantised them (origin + q * 2^e: the product exact, one rounding) and runs
 // the reference's slab test (trace.slang:597-609) on them; an axis whose
 // direction component is zero constrains nothing (the binary test's value is
-// then not a bound: 0 * inf).  The hit children, nearest first for closest
-// hit, form a list of 3-bit child indices; the deferred stack holds (node,
-// rest of its list), one entry per level.  Triangles are tested one per step
-// with the reference's watertight test, so a hit's (t, v, w) are the binary
-// traversal's for the same triangle.  Opaque scenes only.
+// then not a bound: 0 * inf).  The accepted children are visited in the
+// order of their slots XOR the ray's direction octant (the builder places
+// them for that order; PT_WIDE_OCTANT 0 sorts them by entry distance
+// instead); the deferred stack holds (node, children still to visit), one
+// entry per level.  A leaf's triangles are tested with the reference's
+// watertight test, so a hit's (t, v, w) are the binary traversal's for the
+// same triangle.  Opaque scenes only.
 // One axis of a wide node in the ray's frame.  A child bound q (8 bits) is
 // placed into the float v = 1 + q 2^-15 with one byte permute, and its slab
 // distance is t = fma(v, a15, c): a15 = 2^(e+15) rcp and c = B - a15 with
@@ -484,6 +493,19 @@ PTD bool binary_first(const Fast& f, f3 o, f3 d, uint32_t a, uint32_t b) {
 // wide interval contains the interval the reference computes for every
 // binary node under the child, and a box the reference accepts is accepted.
 // An axis the ray does not move along (rcp = 0 here) constrains nothing.
+// three-input minimum / maximum (one instruction on sm_100 and later; NaN
+// inputs are ignored as by fminf / fmaxf)
+PTD float max3f(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+PTD float min3f(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
 struct AxisFrame {
     float a15, c_near, c_far;
     uint32_t near0, near1, far0, far1;  // bound bytes of children 0-3 / 4-7
@@ -524,6 +546,9 @@ struct WideTraverser {
     Shear s;
     float hit_t, hv, hw;
     int32_t hit, light_tri;
+    // list: the accepted children still to visit in the current node (with
+    // PT_WIDE_OCTANT a mask in bits 0..7 and the ray's direction octant, bit a
+    // set when d[a] < 0, in bits 8..10)
     uint32_t node, list, lf, tri_left, sp;
     Rng<false> rng;  // unused (no alpha draws in the wide form)
     Counters c;      // unused (no records in the wide form)
@@ -547,9 +572,58 @@ struct WideTraverser {
         sp = 0u;
         tri_left = 0u;
         node = 0u;
+#if PT_WIDE_OCTANT
+        const uint32_t oct =
+            (__float_as_uint(d.x) >> 31) | ((__float_as_uint(d.y) >> 31) << 1) | ((__float_as_uint(d.z) >> 31) << 2);
+        list = visit(f, 0u, oct) | (oct << 8);
+#else
         list = visit(f, 0u);
+#endif
     }
 
+#if PT_WIDE_OCTANT
+    // the accepted children of node n as a mask: child slot i sets bit i ^ oct,
+    // so the lowest set bit is the next child in the octant order.  A child is
+    // accepted when max(near bounds, 0) <= min(far bounds, hit_t): every ray
+    // the slab test of trace.slang:597-609 accepts on the binary box (plus the
+    // boundary cases t_far = 0 and t_near = hit_t, which change no result)
+    PTD uint32_t visit(const Fast& f, uint32_t n, uint32_t oct) const {
+        const float4* p = f.wide + 8 * (size_t)n;
+        float4 h0, h1, h2, h3;
+        load_node(p, h0, h1);
+        load_node(p + 2, h2, h3);
+        const uint32_t meta = __float_as_uint(h0.w);
+        const uint32_t count = meta >> 24;
+        const AxisFrame X = axis_frame(h0.x, meta & 0xffu, rcp.x, nod.x, __float_as_uint(h1.x), __float_as_uint(h1.y),
+                                       __float_as_uint(h2.z), __float_as_uint(h2.w));
+        const AxisFrame Y = axis_frame(h0.y, (meta >> 8) & 0xffu, rcp.y, nod.y, __float_as_uint(h1.z),
+                                       __float_as_uint(h1.w), __float_as_uint(h3.x), __float_as_uint(h3.y));
+        const AxisFrame Z = axis_frame(h0.z, (meta >> 16) & 0xffu, rcp.z, nod.z, __float_as_uint(h2.x),
+                                       __float_as_uint(h2.y), __float_as_uint(h3.z), __float_as_uint(h3.w));
+        uint32_t mask = 0u;
+        const auto child = [&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            const float nx = fmaf(bound_v<i>(X.near0, X.near1), X.a15, X.c_near);
+            const float ny = fmaf(bound_v<i>(Y.near0, Y.near1), Y.a15, Y.c_near);
+            const float nz = fmaf(bound_v<i>(Z.near0, Z.near1), Z.a15, Z.c_near);
+            const float fx = fmaf(bound_v<i>(X.far0, X.far1), X.a15, X.c_far);
+            const float fy = fmaf(bound_v<i>(Y.far0, Y.far1), Y.a15, Y.c_far);
+            const float fz = fmaf(bound_v<i>(Z.far0, Z.far1), Z.a15, Z.c_far);
+            const float t_near = max3f(nx, ny, fmaxf(nz, 0.0f));
+            const float t_far = min3f(fx, fy, fminf(fz, hit_t));
+            if ((uint32_t)i < count && t_near <= t_far) mask |= 1u << ((uint32_t)i ^ oct);
+        };
+        child(std::integral_constant<int, 0>());
+        child(std::integral_constant<int, 1>());
+        child(std::integral_constant<int, 2>());
+        child(std::integral_constant<int, 3>());
+        child(std::integral_constant<int, 4>());
+        child(std::integral_constant<int, 5>());
+        child(std::integral_constant<int, 6>());
+        child(std::integral_constant<int, 7>());
+        return mask;
+    }
+#else
     // the hit children of node n as 3-bit indices (nearest first unless
     // kShadow) in bits 0..23, their count in bits 24..27
     PTD uint32_t visit(const Fast& f, uint32_t n) const {
@@ -603,6 +677,7 @@ struct WideTraverser {
             }
         return l | (cnt << 24);
     }
+#endif
 
     PTD bool test_triangle(const World& w, const Fast& f, uint32_t tri) {
         float t, v, wb;
@@ -635,6 +710,19 @@ struct WideTraverser {
     template <class S>
     PTD bool step(const World& w, const Fast& f, S& stack, uint32_t*) {
         if (tri_left == 0u) {
+#if PT_WIDE_OCTANT
+            if ((list & 0xffu) == 0u) {
+                if (sp == 0u) return true;
+                sp -= 1u;
+                const uint2 e = stack.get(sp);
+                node = e.x;
+                list = e.y;
+            }
+            const uint32_t oct = list >> 8;
+            const uint32_t k = (uint32_t)(__ffs(list) - 1) ^ oct;
+            list &= list - 1u;  // the lowest set bit is in the mask: it is not empty
+            const bool more = (list & 0xffu) != 0u;
+#else
             uint32_t cnt = list >> 24;
             if (cnt == 0u) {
                 if (sp == 0u) return true;
@@ -646,16 +734,22 @@ struct WideTraverser {
             }
             const uint32_t k = list & 7u;
             list = ((list & 0xffffffu) >> 3) | ((cnt - 1u) << 24);
+            const bool more = cnt > 1u;
+#endif
             const float4* p = f.wide + 8 * (size_t)node;
             const uint32_t child = __ldg(reinterpret_cast<const uint32_t*>(p + 4) + k);
             const uint32_t tc = __ldg(reinterpret_cast<const unsigned short*>(p + 6) + k);
             if (tc == 0u) {
-                if (cnt > 1u) {
+                if (more) {
                     stack.put(sp, make_uint2(node, list));
                     sp += 1u;
                 }
                 node = child;
+#if PT_WIDE_OCTANT
+                list = visit(f, child, oct) | (oct << 8);
+#else
                 list = visit(f, child);
+#endif
                 return false;
             }
             lf = child;
