@@ -174,6 +174,7 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
             const float4 o4 = st.o[i], d4 = st.d[i];
             sc = scenes + (b.tag[__float_as_uint(o4.w)] & 0xffu);
             tr.rng.s = __float_as_uint(d4.w);
+            stack.reset();
             tr.init(sc->f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), kFltMax, -1);
         },
         [&]() {
@@ -266,6 +267,7 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
             contribution = b.q.sc[i];
             path = __float_as_uint(o4.w);
             sc = scenes + (b.tag[path] & 0xffu);
+            stack.reset();
             tr.init(sc->f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), d4.w, __float_as_int(contribution.w));
         },
         [&]() {

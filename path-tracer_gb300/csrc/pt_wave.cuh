@@ -136,13 +136,49 @@ constexpr uint32_t kSmemStack = PT_SMEM_STACK;
 #endif
 constexpr uint32_t kWideSmemStack = PT_WIDE_SMEM_STACK;
 
+// 1: the shared-memory part of a traversal lane's stack holds its top
+// entries (a ring); 0: its bottom entries.  Measured slower on the 2.1M
+// triangle scene (extend 384 against 369 ms over three 64-spp images: the
+// ring's extra shared accesses and branches cost more than the local-memory
+// traffic they save), so off by default
+#ifndef PT_STACK_RING
+#define PT_STACK_RING 0
+#endif
+
 // The deferred stack of one traversal lane: 64 entries in the lane's local
-// memory, of which the first kShared live in the block's shared memory
-// instead (one column per thread, so a warp touches consecutive words).
+// memory, kShared of them in the block's shared memory instead (one column
+// per thread, so a warp touches consecutive words).  With PT_STACK_RING the
+// shared column is a ring over the top of the stack: entries [lo, sp) live
+// there, a push onto a full ring first moves the oldest ring entry to local
+// memory, and a pop below lo reads it back from there, so the pushes and pops
+// of a traversal moving about one depth stay in shared memory.  reset()
+// before each traversal (an any-hit traversal may stop with entries left).
+// Otherwise the shared column holds entries 0..kShared-1.
 template <uint32_t kThreads, uint32_t kShared>
 struct LaneStack {
-    uint2* col;  // &shared[threadIdx.x]; entry i at col[i * kThreads]
+    uint2* col;  // &shared[threadIdx.x]; ring slot j at col[j * kThreads]
     uint2 deep[64];
+#if PT_STACK_RING
+    uint32_t lo = 0u;
+    PTD void reset() { lo = 0u; }
+    PTD void put(uint32_t i, uint2 e) {
+        if (kShared == 0u) {
+            deep[i & 63u] = e;
+            return;
+        }
+        if (i - lo >= kShared) {  // the ring is full: its oldest entry moves out
+            deep[lo & 63u] = col[(lo % kShared) * kThreads];
+            lo += 1u;
+        }
+        col[(i % kShared) * kThreads] = e;
+    }
+    PTD uint2 get(uint32_t i) {
+        if (kShared > 0u && i >= lo) return col[(i % kShared) * kThreads];
+        lo = i;
+        return deep[i & 63u];
+    }
+#else
+    PTD void reset() {}
     PTD void put(uint32_t i, uint2 e) {
         if (kShared > 0u && i < kShared)
             col[i * kThreads] = e;
@@ -153,11 +189,13 @@ struct LaneStack {
         if (kShared > 0u && i < kShared) return col[i * kThreads];
         return deep[i & 63u];
     }
+#endif
 };
 
 // the whole stack in local memory
 struct LocalStack {
     uint2 deep[64];
+    PTD void reset() {}
     PTD void put(uint32_t i, uint2 e) { deep[i & 63u] = e; }
     PTD uint2 get(uint32_t i) const { return deep[i & 63u]; }
 };

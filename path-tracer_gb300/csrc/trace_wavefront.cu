@@ -131,6 +131,7 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
             path = __float_as_uint(o4.w);
             tr.rng.s = __float_as_uint(d4.w);
             if constexpr (kRec) tr.c = q.rec[path];
+            stack.reset();
             tr.init(f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), kFltMax, -1);
         },
         [&]() {
@@ -231,6 +232,7 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
             contribution = q.sc[slot];
             path = __float_as_uint(o4.w);
             if constexpr (kRec) tr.c = q.rec[path];
+            stack.reset();
             tr.init(f, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), d4.w, __float_as_int(contribution.w));
         },
         [&]() {
