@@ -9,6 +9,7 @@ import pytest
 import pathtracer as pt
 from pathtracer import abi
 from pathtracer.engine import Engine
+from worlds import non_opaque_world
 
 pytestmark = pytest.mark.gpu
 
@@ -84,6 +85,41 @@ def test_mixed_jobs_equal_alone(scenes):
         eng.wait_idle(timeout_ms=300000)
         np.testing.assert_array_equal(eng.read(solo, w, h, abi.PT_TILE_ACCUMULATION),
                                       eng.read(jid, w, h, abi.PT_TILE_ACCUMULATION))
+    eng.close()
+
+
+
+def test_non_opaque_jobs_equal_alone(scenes):
+    """Jobs on a scene with BLEND and MASK materials (random numbers drawn inside traversal, so the engine
+    runs them in its non-opaque waves) beside opaque Cornell jobs: each equals its pt_trace render alone."""
+    w = non_opaque_world()
+    full = w.take_updates()
+    cam = abi.Camera.from_buffer_copy(full.camera.contents)
+    eng = Engine(wave_paths=1 << 15, tile_size=16)
+    nid = eng.add_scene(full)
+    cid = eng.add_scene(scenes.full["cornell"])
+    ccam = scenes.camera("cornell", 64, 48)
+    spec = [(nid, cam, 96, 96, 3, 8), (cid, ccam, 64, 48, 2, 6), (nid, cam, 40, 40, 5, 12)]
+    jobs = [eng.submit(sid, c, wd, ht, spp, b) for sid, c, wd, ht, spp, b in spec]
+    eng.wait_idle(timeout_ms=300000)
+    for (sid, c, wd, ht, spp, b), jid in zip(spec, jobs):
+        assert eng.status(jid) == (abi.PT_JOB_DONE, spp)
+        if sid == cid:
+            want_acc, want_img = render_alone(scenes, "cornell", c, wd, ht, spp, b)
+        else:
+            u = abi.WorldUpdates.from_buffer_copy(full)
+            u.camera = C.pointer(c)
+            tr = pt.PathTracer(u, (wd, ht))
+            tr.set_max_bounces(b)
+            tr.set_tile((wd, ht), (0, 0), (wd, ht))
+            while tr.sample_count() < spp:
+                tr.trace(spp - tr.sample_count())
+            want_acc, want_img = tr.read_tile(abi.PT_TILE_ACCUMULATION), tr.read_tile(abi.PT_TILE_IMAGE)
+            tr.close()
+        np.testing.assert_array_equal(eng.read(jid, wd, ht, abi.PT_TILE_ACCUMULATION).view(np.uint32),
+                                      want_acc.view(np.uint32))
+        np.testing.assert_array_equal(eng.read(jid, wd, ht, abi.PT_TILE_IMAGE).view(np.uint32),
+                                      want_img.view(np.uint32))
     eng.close()
 
 

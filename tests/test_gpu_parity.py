@@ -11,6 +11,7 @@ import pytest
 import oracle
 import pathtracer as pt
 from pathtracer import abi
+from worlds import non_opaque_world
 
 pytestmark = pytest.mark.gpu
 
@@ -260,4 +261,34 @@ def test_large_scene_fp64_rmse(large_world, kernel):
     rel_rmse = np.sqrt(np.mean((acc - ref) ** 2)) / np.sqrt(np.mean(ref ** 2))
     print(f"config 2 relative RMSE vs FP64 oracle ({spp} spp, 48x48 crop, kernel {kernel}): {rel_rmse:.3e}")
     assert rel_rmse < 1e-2
+    tr.close()
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_non_opaque_tile_bit_exact(kernel):
+    """BLEND and MASK materials: per-path visit order, hits, random-number draws (including those drawn
+    inside the extend and shadow traversals) and radiance identical to the oracle."""
+    w = non_opaque_world()
+    u = w.take_updates()
+    ow = oracle.world_from_updates(u)
+    tr = pt.PathTracer(u, (48, 48))
+    tr.set_kernel(kernel)
+    tr.set_max_bounces(8)
+    draws = 0
+    for origin in ((40, 60), (100, 100)):
+        tr.set_tile((128, 128), origin, (48, 48))
+        gpu = tr.trace_recorded(4).reshape(4, 48, 48)
+        vis = (min(48, 128 - origin[0]), min(48, 128 - origin[1]))
+        gpu = gpu[:, :vis[1], :vis[0]].reshape(-1)
+        px = pixels_of(origin, (48, 48), (128, 128))
+        _, ref = oracle.trace_paths(ow, (128, 128), 8, px, 1, 4, records=True)
+        assert_records_equal(gpu, ref)
+        draws += int(ref["rand_draws"].sum())
+    assert draws > 0
+    # the paths' hits include surfaces of both non-opaque kinds
+    mats = w.materials()
+    mat_of_tri = np.frombuffer(w.attributes_raw().tobytes(), np.uint32).reshape(w.triangle_count(), -1)[:, 0]
+    hits = ref["hit"][ref["hit"] >= 0]
+    modes = {int(mats[int(mat_of_tri[t])].alpha_mode) for t in hits}
+    assert {abi.PT_ALPHA_MODE_BLEND, abi.PT_ALPHA_MODE_MASK} <= modes
     tr.close()
