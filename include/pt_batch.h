@@ -55,6 +55,9 @@ typedef struct pt_engine_config {
     uint32_t sort_min_hits;     /* a bounce with at least this many hits sorts them by triangle bucket
                                    (1024 triangles each, BVH order) before shading; 0 = 65536,
                                    0xffffffff = never */
+    uint32_t traversal_threads; /* threads per block of the extend and shadow kernels: 64, 128 or 256
+                                   (the register budget per thread stays the same); 0 = 128 */
+    uint32_t shade_threads;     /* threads per block of the shading kernel: 64, 128 or 256; 0 = 128 */
 } pt_engine_config;
 
 int pte_create(const pt_engine_config* config, pt_engine** out);
@@ -113,13 +116,15 @@ typedef struct pt_engine_stats {
     uint64_t hbm_budget;
     double gpu_ms;               /* device time of all finished waves (CUDA events) */
     uint32_t wave_paths, tile_size, steps_per_refill, use_graphs, precision, sort_min_hits;
+    uint32_t traversal_threads, shade_threads;
 } pt_engine_stats;
 int pte_stats(pt_engine* engine, pt_engine_stats* stats);
 
 /* Autotuner: renders the given jobs once per candidate configuration
- * (wave_paths x tile_size x steps_per_refill x sort on/off) and keeps the one with the
- * highest paths per second of device time; writes it to *chosen.  The jobs'
- * results are discarded. */
+ * (wave_paths x tile_size x steps_per_refill x sort on/off, then, with the
+ * best of those, the block shapes traversal_threads x shade_threads) and
+ * keeps the one with the highest paths per second of device time; writes it
+ * to *chosen.  The jobs' results are discarded. */
 int pte_autotune(pt_engine* engine, const pt_job_desc* jobs, uint32_t count, pt_engine_config* chosen);
 
 #ifdef __cplusplus

@@ -17,6 +17,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <utility>
 #include <thread>
 #include <vector>
 
@@ -151,21 +152,25 @@ __global__ void reset_kernel(uint32_t* cnt, int next) {
     cnt[7] = 0u;  // set again by the sort when it runs
 }
 
-template <bool kAlpha, bool kWide>
-__global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : PT_EXTEND_MIN_BLOCKS) extend_kernel(const SceneDev* scenes, WaveBufs b, int cur,
-                                                                uint32_t steps_per_refill) {
+// resident blocks per SM a kernel of kThreads threads is compiled for: the
+// same registers per thread as kMinBlocks blocks of 128 threads
+constexpr int blocks_for(int kMinBlocks, int kThreads) { return kMinBlocks * 128 / kThreads > 0 ? kMinBlocks * 128 / kThreads : 1; }
+
+template <bool kAlpha, bool kWide, int kThreads = kExtendThreads>
+__global__ void __launch_bounds__(kThreads, blocks_for(kWide ? PT_WIDE_MIN_BLOCKS : PT_EXTEND_MIN_BLOCKS, kThreads))
+    extend_kernel(const SceneDev* scenes, WaveBufs b, int cur, uint32_t steps_per_refill) {
     static_assert(!(kAlpha && kWide), "the wide form runs opaque scenes only");
     const Stage st = stage_of(b.q, cur);
     const uint32_t count = *st.count;
     typename std::conditional<kWide, WideTraverser<false>, Traverser<false, kAlpha, false>>::type tr;
     constexpr uint32_t kShared = kWide ? kWideSmemStack : kSmemStack;
-    __shared__ uint2 stack_top[kShared > 0u ? kShared * kExtendThreads : 1u];
-    LaneStack<kExtendThreads, kShared> stack;
+    __shared__ uint2 stack_top[kShared > 0u ? kShared * kThreads : 1u];
+    LaneStack<kThreads, kShared> stack;
     stack.col = stack_top + threadIdx.x;
     uint32_t istack[1];
     const SceneDev* sc = scenes;
     uint32_t slot = 0;
-    __shared__ FilerSlots<kExtendThreads> filer_slots;
+    __shared__ FilerSlots<kThreads> filer_slots;
     ResultFiler filer = filer_slots.of_warp(lane_id());
     lane_refill_loop(
         &b.q.cnt[3], count, kWide ? (uint32_t)kWideStepsPerRefill : steps_per_refill, kRefillBelow,
@@ -187,10 +192,9 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
         [&]() { filer.flush(b.q, lane_id()); });
 }
 
-template <bool kAlpha>
-__global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kernel(const SceneDev* scenes,
-                                                                                   const JobDev* jobs, WaveBufs b,
-                                                                                   int cur, uint32_t bounce) {
+template <bool kAlpha, int kThreads = kShadeThreads>
+__global__ void __launch_bounds__(kThreads, blocks_for(PT_SHADE_MIN_BLOCKS, kThreads))
+    shade_kernel(const SceneDev* scenes, const JobDev* jobs, WaveBufs b, int cur, uint32_t bounce) {
     const Stage st = stage_of(b.q, cur);
     const ShadeRange range(b.q);
     const uint32_t count = range.count();
@@ -247,14 +251,14 @@ __global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kern
     }
 }
 
-template <bool kWide>
-__global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : PT_EXTEND_MIN_BLOCKS) shadow_kernel(const SceneDev* scenes, WaveBufs b,
-                                                                uint32_t steps_per_refill) {
+template <bool kWide, int kThreads = kExtendThreads>
+__global__ void __launch_bounds__(kThreads, blocks_for(kWide ? PT_WIDE_MIN_BLOCKS : PT_EXTEND_MIN_BLOCKS, kThreads))
+    shadow_kernel(const SceneDev* scenes, WaveBufs b, uint32_t steps_per_refill) {
     const uint32_t count = b.q.cnt[2];
     typename std::conditional<kWide, WideTraverser<true>, Traverser<false, false, true>>::type tr;
     constexpr uint32_t kShared = kWide ? kWideSmemStack : kSmemStack;
-    __shared__ uint2 stack_top[kShared > 0u ? kShared * kExtendThreads : 1u];
-    LaneStack<kExtendThreads, kShared> stack;
+    __shared__ uint2 stack_top[kShared > 0u ? kShared * kThreads : 1u];
+    LaneStack<kThreads, kShared> stack;
     stack.col = stack_top + threadIdx.x;
     uint32_t istack[1];
     const SceneDev* sc = scenes;
@@ -594,6 +598,12 @@ int occupancy(K kernel, int threads) {
     return blocks > 0 ? blocks : 1;
 }
 
+// one launch of a persistent stage kernel: the blocks that stay resident on every SM
+template <class... P, class... A>
+void launch_persistent(void (*kernel)(P...), pt_engine* e, int threads, A&&... args) {
+    kernel<<<e->sms * occupancy(kernel, threads), threads, 0, e->stream>>>(std::forward<A>(args)...);
+}
+
 // the launches of one wave (captured into a graph, or issued directly)
 template <bool kAlpha, bool kWideBvh>
 cudaError_t issue_wave(pt_engine* e) {
@@ -606,13 +616,27 @@ cudaError_t issue_wave(pt_engine* e) {
     plan_kernel<<<1, 32, 0, s>>>(ctrl, ring, e->ring_cap, e->cfg.wave_paths, e->max_items, e->wb);
     raygen_kernel<<<per_wave_blocks, 256, 0, s>>>(ctrl, ring, jobs, e->wb);
     constexpr bool kWide = kWideBvh && !kAlpha;
-    const int ext = e->sms * occupancy(extend_kernel<kAlpha, kWide>, kExtendThreads);
-    const int sha = e->sms * occupancy(shade_kernel<kAlpha>, kShadeThreads);
-    const int shd = e->sms * occupancy(shadow_kernel<kWide>, kExtendThreads);
+    const uint32_t tt = e->cfg.traversal_threads, st = e->cfg.shade_threads;
+    // persistent launches: as many blocks as stay resident, for the block shape of the configuration
+    const auto extend = [&](int cur) {
+        if (tt == 64u) return launch_persistent(extend_kernel<kAlpha, kWide, 64>, e, 64, scenes, e->wb, cur, e->cfg.steps_per_refill);
+        if (tt == 256u) return launch_persistent(extend_kernel<kAlpha, kWide, 256>, e, 256, scenes, e->wb, cur, e->cfg.steps_per_refill);
+        return launch_persistent(extend_kernel<kAlpha, kWide, 128>, e, 128, scenes, e->wb, cur, e->cfg.steps_per_refill);
+    };
+    const auto shade = [&](int cur, uint32_t bounce) {
+        if (st == 64u) return launch_persistent(shade_kernel<kAlpha, 64>, e, 64, scenes, jobs, e->wb, cur, bounce);
+        if (st == 256u) return launch_persistent(shade_kernel<kAlpha, 256>, e, 256, scenes, jobs, e->wb, cur, bounce);
+        return launch_persistent(shade_kernel<kAlpha, 128>, e, 128, scenes, jobs, e->wb, cur, bounce);
+    };
+    const auto shadow = [&]() {
+        if (tt == 64u) return launch_persistent(shadow_kernel<kWide, 64>, e, 64, scenes, e->wb, e->cfg.steps_per_refill);
+        if (tt == 256u) return launch_persistent(shadow_kernel<kWide, 256>, e, 256, scenes, e->wb, e->cfg.steps_per_refill);
+        return launch_persistent(shadow_kernel<kWide, 128>, e, 128, scenes, e->wb, e->cfg.steps_per_refill);
+    };
     int cur = 0;
     for (uint32_t bounce = 0; bounce < kRounds; ++bounce) {
         reset_kernel<<<1, 1, 0, s>>>(e->wb.q.cnt, cur ^ 1);
-        extend_kernel<kAlpha, kWide><<<ext, kExtendThreads, 0, s>>>(scenes, e->wb, cur, e->cfg.steps_per_refill);
+        extend(cur);
         if (e->cfg.sort_min_hits != 0xffffffffu) {
             // hits of all jobs by triangle bucket (1024 triangles per bucket)
             sort_count_kernel<1><<<e->sms * 4, kSortThreads, 0, s>>>(World{}, e->wb.q, e->sort_counts,
@@ -622,8 +646,8 @@ cudaError_t issue_wave(pt_engine* e) {
             sort_scatter_kernel<1><<<e->sms * 4, kSortThreads, 0, s>>>(World{}, e->wb.q, e->sort_counts + kSortBuckets,
                                                                      e->cfg.sort_min_hits, kEngineSortShift);
         }
-        shade_kernel<kAlpha><<<sha, kShadeThreads, 0, s>>>(scenes, jobs, e->wb, cur, bounce);
-        if constexpr (!kAlpha) shadow_kernel<kWide><<<shd, kExtendThreads, 0, s>>>(scenes, e->wb, e->cfg.steps_per_refill);
+        shade(cur, bounce);
+        if constexpr (!kAlpha) shadow();
         cur ^= 1;
     }
     accumulate_kernel<<<per_wave_blocks, 256, 0, s>>>(ctrl, ring, jobs, e->wb, e->d_done.as<uint32_t>());
@@ -955,12 +979,17 @@ int pte_create(const pt_engine_config* cfg, pt_engine** out) {
     if (e->cfg.tile_size == 0) e->cfg.tile_size = 32;
     if (e->cfg.steps_per_refill == 0) e->cfg.steps_per_refill = 32;
     if (e->cfg.sort_min_hits == 0) e->cfg.sort_min_hits = 65536u;
+    if (e->cfg.traversal_threads == 0) e->cfg.traversal_threads = 128;
+    if (e->cfg.shade_threads == 0) e->cfg.shade_threads = 128;
     e->budget = e->cfg.hbm_budget_bytes ? e->cfg.hbm_budget_bytes : 150ull << 30;
     int rc = PT_OK;
     if (e->cfg.tile_size > 256 || e->cfg.wave_paths < (1u << 12) || e->cfg.wave_paths > (1u << 28))
         rc = e->fail(PT_ERR_INVALID_ARG, "tile_size must be at most 256 and wave_paths in [4096, 2^28]");
     if (!rc && (e->cfg.precision & ~PT_PRECISION_COMPRESSED))
         rc = e->fail(PT_ERR_INVALID_ARG, "unknown precision bits");
+    const auto shape_ok = [](uint32_t t) { return t == 64u || t == 128u || t == 256u; };
+    if (!rc && !(shape_ok(e->cfg.traversal_threads) && shape_ok(e->cfg.shade_threads)))
+        rc = e->fail(PT_ERR_INVALID_ARG, "traversal_threads and shade_threads must be 64, 128 or 256");
     if (!rc) rc = e->cuda(cudaSetDevice(e->cfg.device), "cudaSetDevice");
     if (!rc) rc = e->cuda(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "stream");
     if (!rc) rc = e->cuda(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, e->cfg.device), "SM count");
@@ -1338,6 +1367,8 @@ int pte_stats(pt_engine* e, pt_engine_stats* s) {
     s->precision = e->cfg.precision;
     s->sort_min_hits = e->cfg.sort_min_hits;
     s->use_graphs = e->cfg.use_graphs;
+    s->traversal_threads = e->cfg.traversal_threads;
+    s->shade_threads = e->cfg.shade_threads;
     return PT_OK;
 }
 
@@ -1352,8 +1383,35 @@ int pte_autotune(pt_engine* e, const pt_job_desc* jobs, uint32_t count, pt_engin
     const uint32_t tiles[] = {16, 32, 64};
     const uint32_t steps[] = {16, 32};
     const uint32_t sorts[] = {0xffffffffu, 65536u};
+    const uint32_t shapes[] = {64, 128, 256};
     pt_engine_config best = e->cfg;
     double best_rate = -1.0;
+    // renders the jobs under e->cfg: one untimed pass to capture graphs, then the timed pass
+    const auto measure = [&]() -> int {
+        drop_graphs(e);
+        for (int pass = 0; pass < 2; ++pass) {
+            const double ms0 = e->stats.gpu_ms;
+            const uint64_t paths0 = e->stats.paths;
+            std::vector<uint64_t> ids;
+            for (uint32_t k = 0; k < count; ++k) {
+                pt_job_desc d = jobs[k];
+                d.continue_job = 0;
+                uint64_t id = 0;
+                if (int r = pte_submit(e, &d, &id)) return r;
+                ids.push_back(id);
+            }
+            if (int r = pte_wait_idle(e, 0)) return r;
+            for (uint64_t id : ids) pte_job_release(e, id);
+            e->done_unreported.clear();
+            const double ms = e->stats.gpu_ms - ms0;
+            const double rate = (double)(e->stats.paths - paths0) / (ms > 0 ? ms : 1e-9);
+            if (pass == 1 && rate > best_rate) {
+                best_rate = rate;
+                best = e->cfg;
+            }
+        }
+        return PT_OK;
+    };
     for (uint32_t W : waves)
         for (uint32_t T : tiles)
             for (uint32_t S : steps)
@@ -1368,30 +1426,22 @@ int pte_autotune(pt_engine* e, const pt_job_desc* jobs, uint32_t count, pt_engin
                 e->cfg.tile_size = T;
                 e->cfg.steps_per_refill = S;
                 e->cfg.sort_min_hits = H;
-                drop_graphs(e);
-                // one untimed pass to capture graphs, then the timed pass
-                for (int pass = 0; pass < 2; ++pass) {
-                    const double ms0 = e->stats.gpu_ms;
-                    const uint64_t paths0 = e->stats.paths;
-                    std::vector<uint64_t> ids;
-                    for (uint32_t k = 0; k < count; ++k) {
-                        pt_job_desc d = jobs[k];
-                        d.continue_job = 0;
-                        uint64_t id = 0;
-                        if ((rc = pte_submit(e, &d, &id))) return rc;
-                        ids.push_back(id);
-                    }
-                    if ((rc = pte_wait_idle(e, 0))) return rc;
-                    for (uint64_t id : ids) pte_job_release(e, id);
-                    e->done_unreported.clear();
-                    const double ms = e->stats.gpu_ms - ms0;
-                    const double rate = (double)(e->stats.paths - paths0) / (ms > 0 ? ms : 1e-9);
-                    if (pass == 1 && rate > best_rate) {
-                        best_rate = rate;
-                        best = e->cfg;
-                    }
-                }
+                if ((rc = measure())) return rc;
             }
+    // block shapes, with the best of the above
+    if (best.wave_paths != e->cfg.wave_paths) {
+        e->cfg.wave_paths = best.wave_paths;
+        if ((rc = setup_wave(e))) return rc;
+    }
+    const pt_engine_config base = best;
+    for (uint32_t TT : shapes)
+        for (uint32_t ST : shapes) {
+            if (TT == base.traversal_threads && ST == base.shade_threads) continue;  // measured above
+            e->cfg = base;
+            e->cfg.traversal_threads = TT;
+            e->cfg.shade_threads = ST;
+            if ((rc = measure())) return rc;
+        }
     if (best.wave_paths != e->cfg.wave_paths) {
         e->cfg.wave_paths = best.wave_paths;
         if ((rc = setup_wave(e))) return rc;

@@ -300,7 +300,8 @@ PT_JOB_DONE = 2
 
 class EngineConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("hbm_budget_bytes", c_u64), ("wave_paths", c_u32), ("tile_size", c_u32),
-                ("steps_per_refill", c_u32), ("use_graphs", c_u32), ("precision", c_u32), ("sort_min_hits", c_u32)]
+                ("steps_per_refill", c_u32), ("use_graphs", c_u32), ("precision", c_u32), ("sort_min_hits", c_u32),
+                ("traversal_threads", c_u32), ("shade_threads", c_u32)]
 
 
 class JobDesc(C.Structure):
@@ -313,7 +314,7 @@ class EngineStats(C.Structure):
                 ("jobs_done", c_u64), ("scenes_cached", c_u64), ("scene_hits", c_u64), ("scenes_evicted", c_u64),
                 ("hbm_used", c_u64), ("hbm_budget", c_u64), ("gpu_ms", C.c_double), ("wave_paths", c_u32),
                 ("tile_size", c_u32), ("steps_per_refill", c_u32), ("use_graphs", c_u32), ("precision", c_u32),
-                ("sort_min_hits", c_u32)]
+                ("sort_min_hits", c_u32), ("traversal_threads", c_u32), ("shade_threads", c_u32)]
 
 
 SIGNATURES.update({

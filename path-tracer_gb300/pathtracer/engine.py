@@ -13,13 +13,15 @@ class Engine:
     """Many render jobs of uneven size, samples, depth and scene traced together on one GPU."""
 
     def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, wave_paths: int = 0, tile_size: int = 0,
-                 steps_per_refill: int = 0, use_graphs: bool = True, precision: int = 0, sort_min_hits: int = 0):
+                 steps_per_refill: int = 0, use_graphs: bool = True, precision: int = 0, sort_min_hits: int = 0,
+                 traversal_threads: int = 0, shade_threads: int = 0):
         """precision: PT_PRECISION_* bits (0 = the reference's FP32 buffers, 7 = the compressed form);
         sort_min_hits: hits of a bounce are sorted by triangle bucket before shading from this many on
-        (0 = the default 65536, 0xffffffff = never)."""
+        (0 = the default 65536, 0xffffffff = never); traversal_threads / shade_threads: threads per block
+        of the traversal and shading kernels, 64, 128 or 256 (0 = 128)."""
         self._lib = load()
         cfg = abi.EngineConfig(device, hbm_budget_bytes, wave_paths, tile_size, steps_per_refill, int(use_graphs),
-                               precision, sort_min_hits)
+                               precision, sort_min_hits, traversal_threads, shade_threads)
         h = C.c_void_p()
         rc = self._lib.pte_create(C.byref(cfg), C.byref(h))
         if rc != abi.PT_OK:

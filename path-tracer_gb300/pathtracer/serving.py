@@ -231,8 +231,8 @@ def main(argv=None) -> None:
                    help="engine form: the reference's FP32 buffers, the 8-wide BVH, or the compressed form "
                         "(8-wide BVH + FP16 attributes / BF16 skybox + Kahan sums)")
     p.add_argument("--autotune", action="store_true",
-                   help="with --compare: let the engine's autotuner pick wave size, tile size, refill steps and the "
-                        "hit-sort threshold on 16 of the requests first")
+                   help="with --compare: let the engine's autotuner pick wave size, tile size, refill steps, the "
+                        "hit-sort threshold and the kernels' block shapes on 16 of the requests first")
     p.add_argument("--compare", type=int, default=0,
                    help="instead of serving: render this many requests of the mix back to back with the plain "
                         "kernel, the wavefront kernel (one job per call) and the batched engine")

@@ -123,6 +123,26 @@ def test_non_opaque_jobs_equal_alone(scenes):
     eng.close()
 
 
+
+@pytest.mark.parametrize("shapes", [(64, 256), (256, 64)])
+def test_block_shapes_keep_bits(scenes, shapes):
+    """Other threads-per-block choices for the traversal and shading kernels give the same bits."""
+    eng = Engine(wave_paths=1 << 15, tile_size=16, traversal_threads=shapes[0], shade_threads=shapes[1])
+    assert (eng.stats()["traversal_threads"], eng.stats()["shade_threads"]) == shapes
+    ids = {name: eng.add_scene(scenes.full[name]) for name in scenes.full}
+    spec = JOBS[:3]
+    cams = [scenes.camera(n, w, h, yaw) for n, w, h, _, _, yaw in spec]
+    jobs = [eng.submit(ids[n], cam, w, h, spp, b) for (n, w, h, spp, b, _), cam in zip(spec, cams)]
+    eng.wait_idle(timeout_ms=300000)
+    for (n, w, h, spp, b, _), cam, jid in zip(spec, cams, jobs):
+        want_acc, _ = render_alone(scenes, n, cam, w, h, spp, b)
+        np.testing.assert_array_equal(eng.read(jid, w, h, abi.PT_TILE_ACCUMULATION).view(np.uint32),
+                                      want_acc.view(np.uint32))
+    eng.close()
+    with pytest.raises(pt.PathTracerError):
+        Engine(traversal_threads=96)
+
+
 def test_progressive_refinement(scenes):
     eng = Engine(wave_paths=1 << 16, tile_size=32)
     sid = eng.add_scene(scenes.full["terrain"])
@@ -215,6 +235,9 @@ def test_autotune_picks_a_candidate(scenes):
     assert cfg["wave_paths"] in (1 << 20, 1 << 21, 1 << 22, 1 << 23)
     assert cfg["tile_size"] in (16, 32, 64) and cfg["steps_per_refill"] in (16, 32)
     assert cfg["sort_min_hits"] in (65536, 0xFFFFFFFF)
+    assert cfg["traversal_threads"] in (64, 128, 256) and cfg["shade_threads"] in (64, 128, 256)
+    st = eng.stats()
+    assert (st["traversal_threads"], st["shade_threads"]) == (cfg["traversal_threads"], cfg["shade_threads"])
     j = eng.submit(sid, cam, 64, 64, 2, 4)
     eng.wait_idle(timeout_ms=300000)
     assert eng.status(j)[0] == abi.PT_JOB_DONE
