@@ -106,11 +106,14 @@ class Server:
         return abi.Camera.from_buffer_copy(self._last[name])
 
     def run(self, requests: list[Request], max_outstanding_paths: int = 2_000_000_000,
-            keep_finished: int = 256) -> ServeResult:
+            keep_finished: int = 256, on_done=None) -> ServeResult:
         """Serve the stream.  The `keep_finished` most recently finished jobs stay resident (their
-        accumulations can be refined by later progressive requests); older ones are released."""
+        accumulations can be refined by later progressive requests, which keep the refined job's
+        camera); older ones are released.  on_done(job_id, request, camera, total_samples), if
+        given, is called when a job finishes, while its result is still resident."""
         eng, res = self.engine, ServeResult()
         arrival_of, is_512_16, paths_of = {}, {}, {}
+        camera_of, samples_of = {}, {}  # resident jobs: camera and samples in the accumulation
         finished: dict[tuple, list[int]] = {}  # (scene, w, h, depth) -> finished job ids to refine
         kept: OrderedDict[int, tuple] = OrderedDict()  # the same jobs, oldest first
         outstanding, i = 0, 0
@@ -129,19 +132,24 @@ class Server:
                 if outstanding + paths > max_outstanding_paths:
                     res.rejected += 1
                     continue
+                cam = camera_of[cont] if cont else self.camera(r.scene, r)
                 try:
-                    jid = eng.submit(self.scene_ids[r.scene], self.camera(r.scene, r), r.width, r.height, r.samples,
+                    jid = eng.submit(self.scene_ids[r.scene], cam, r.width, r.height, r.samples,
                                      r.max_bounces, continue_job=cont)
                 except pt.PathTracerError:
                     res.rejected += 1
                     continue
-                arrival_of[jid] = (r.arrival, key, cont)
+                camera_of[jid] = cam
+                samples_of[jid] = r.samples + (samples_of[cont] if cont else 0)
+                arrival_of[jid] = (r.arrival, key, cont, r)
                 is_512_16[jid] = (r.width, r.height, r.samples) == (512, 512, 16)
                 paths_of[jid] = paths
                 outstanding += paths
             for jid in eng.poll(timeout_ms=1):
                 done_at = time.perf_counter() - t0
-                arrival, key, cont = arrival_of.pop(jid)
+                arrival, key, cont, req = arrival_of.pop(jid)
+                if on_done is not None:
+                    on_done(jid, req, camera_of[jid], samples_of[jid])
                 lat = (done_at - arrival) * 1e3
                 res.latencies_ms.append(lat)
                 if is_512_16.pop(jid):
@@ -152,12 +160,16 @@ class Server:
                 outstanding -= p
                 if cont:
                     eng.release(cont)
+                    camera_of.pop(cont, None)
+                    samples_of.pop(cont, None)
                 finished.setdefault(key, []).append(jid)
                 kept[jid] = key
                 while len(kept) > keep_finished:
                     old_jid, old_key = kept.popitem(last=False)
                     finished[old_key].remove(old_jid)
                     eng.release(old_jid)
+                    camera_of.pop(old_jid, None)
+                    samples_of.pop(old_jid, None)
         res.wall_s = time.perf_counter() - t0
         for ids in finished.values():
             for jid in ids:

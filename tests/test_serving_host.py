@@ -88,3 +88,27 @@ def test_outstanding_path_cap_rejects():
     res = server.run(reqs, max_outstanding_paths=3 * 100 * 100 * 16)
     assert res.completed == 3 and res.rejected == 7
     assert np.all(np.array(res.latencies_ms) >= 0)
+
+
+def test_refinements_keep_the_camera_and_count_samples():
+    """A progressive request adds samples to the refined job's view: same camera, samples summed."""
+    s = _server()
+    cams = {}
+    orig = s.engine.submit
+
+    def submit(scene_id, camera, width, height, samples, max_bounces, continue_job=0):
+        jid = orig(scene_id, camera, width, height, samples, max_bounces, continue_job)
+        cams[jid] = bytes(camera)
+        return jid
+
+    s.engine.submit = submit
+    seen = {}
+    reqs = [Request(0.0, "room", 32, 32, 4, 6, 0.1, -0.3),
+            Request(0.0, "room", 32, 32, 2, 6, -0.4, -0.2, progressive=True),
+            Request(0.0, "room", 32, 32, 3, 6, 0.5, -0.4, progressive=True)]
+    # the refinements arrive after the first job has finished
+    reqs[1].arrival, reqs[2].arrival = 0.05, 0.1
+    s.run(reqs, on_done=lambda jid, req, cam, total: seen.__setitem__(jid, (bytes(cam), total)))
+    assert [c for _, c in s.engine.continued] == [1, 2]
+    assert seen[1][1] == 4 and seen[2][1] == 6 and seen[3][1] == 9
+    assert cams[1] == cams[2] == cams[3] == seen[3][0]
