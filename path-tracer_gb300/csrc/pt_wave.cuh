@@ -533,19 +533,6 @@ PTD bool binary_first(const Fast& f, f3 o, f3 d, uint32_t a, uint32_t b) {
 // wide interval contains the interval the reference computes for every
 // binary node under the child, and a box the reference accepts is accepted.
 // An axis the ray does not move along (rcp = 0 here) constrains nothing.
-// three-input minimum / maximum (one instruction on sm_100 and later; NaN
-// inputs are ignored as by fminf / fmaxf)
-PTD float max3f(float a, float b, float c) {
-    float r;
-    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
-PTD float min3f(float a, float b, float c) {
-    float r;
-    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
-
 struct AxisFrame {
     float a15, c_near, c_far;
     uint32_t near0, near1, far0, far1;  // bound bytes of children 0-3 / 4-7
@@ -649,8 +636,13 @@ struct WideTraverser {
             const float fx = fmaf(bound_v<i>(X.far0, X.far1), X.a15, X.c_far);
             const float fy = fmaf(bound_v<i>(Y.far0, Y.far1), Y.a15, Y.c_far);
             const float fz = fmaf(bound_v<i>(Z.far0, Z.far1), Z.a15, Z.c_far);
+#if PT_WIDE_MINMAX3
             const float t_near = max3f(nx, ny, fmaxf(nz, 0.0f));
             const float t_far = min3f(fx, fy, fminf(fz, hit_t));
+#else
+            const float t_near = fmaxf(fmaxf(nx, ny), fmaxf(nz, 0.0f));
+            const float t_far = fminf(fminf(fx, fy), fminf(fz, hit_t));
+#endif
             if ((uint32_t)i < count && t_near <= t_far) mask |= 1u << ((uint32_t)i ^ oct);
         };
         child(std::integral_constant<int, 0>());
