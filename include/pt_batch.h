@@ -57,7 +57,8 @@ typedef struct pt_engine_config {
                                    0xffffffff = never */
     uint32_t traversal_threads; /* threads per block of the extend and shadow kernels: 64, 128 or 256
                                    (the register budget per thread stays the same); 0 = 128 */
-    uint32_t shade_threads;     /* threads per block of the shading kernel: 64, 128 or 256; 0 = 128 */
+    uint32_t shade_threads;     /* threads per block of the shading kernel: 128, 256, 512 or 1024
+                                   (64 registers per thread); 0 = 1024 */
 } pt_engine_config;
 
 int pte_create(const pt_engine_config* config, pt_engine** out);

@@ -155,7 +155,7 @@ __global__ void reset_kernel(uint32_t* cnt, int next) {
 // resident blocks per SM a kernel of kThreads threads is compiled for: the
 // same registers per thread as kMinBlocks blocks of kBaseThreads threads
 static_assert((kExtendThreads == 64 || kExtendThreads == 128 || kExtendThreads == 256) &&
-                  (kShadeThreads == 64 || kShadeThreads == 128 || kShadeThreads == 256),
+                  (kShadeThreads == 128 || kShadeThreads == 256 || kShadeThreads == 512 || kShadeThreads == 1024),
               "the engine's default block shapes must be among its compiled ones");
 constexpr int blocks_for(int kMinBlocks, int kBaseThreads, int kThreads) {
     return kMinBlocks * kBaseThreads / kThreads > 0 ? kMinBlocks * kBaseThreads / kThreads : 1;
@@ -629,9 +629,10 @@ cudaError_t issue_wave(pt_engine* e) {
         return launch_persistent(extend_kernel<kAlpha, kWide, 128>, e, 128, scenes, e->wb, cur, e->cfg.steps_per_refill);
     };
     const auto shade = [&](int cur, uint32_t bounce) {
-        if (st == 64u) return launch_persistent(shade_kernel<kAlpha, 64>, e, 64, scenes, jobs, e->wb, cur, bounce);
+        if (st == 128u) return launch_persistent(shade_kernel<kAlpha, 128>, e, 128, scenes, jobs, e->wb, cur, bounce);
         if (st == 256u) return launch_persistent(shade_kernel<kAlpha, 256>, e, 256, scenes, jobs, e->wb, cur, bounce);
-        return launch_persistent(shade_kernel<kAlpha, 128>, e, 128, scenes, jobs, e->wb, cur, bounce);
+        if (st == 512u) return launch_persistent(shade_kernel<kAlpha, 512>, e, 512, scenes, jobs, e->wb, cur, bounce);
+        return launch_persistent(shade_kernel<kAlpha, 1024>, e, 1024, scenes, jobs, e->wb, cur, bounce);
     };
     const auto shadow = [&]() {
         if (tt == 64u) return launch_persistent(shadow_kernel<kWide, 64>, e, 64, scenes, e->wb, e->cfg.steps_per_refill);
@@ -992,9 +993,9 @@ int pte_create(const pt_engine_config* cfg, pt_engine** out) {
         rc = e->fail(PT_ERR_INVALID_ARG, "tile_size must be at most 256 and wave_paths in [4096, 2^28]");
     if (!rc && (e->cfg.precision & ~PT_PRECISION_COMPRESSED))
         rc = e->fail(PT_ERR_INVALID_ARG, "unknown precision bits");
-    const auto shape_ok = [](uint32_t t) { return t == 64u || t == 128u || t == 256u; };
-    if (!rc && !(shape_ok(e->cfg.traversal_threads) && shape_ok(e->cfg.shade_threads)))
-        rc = e->fail(PT_ERR_INVALID_ARG, "traversal_threads and shade_threads must be 64, 128 or 256");
+    const uint32_t tt = e->cfg.traversal_threads, st = e->cfg.shade_threads;
+    if (!rc && !((tt == 64u || tt == 128u || tt == 256u) && (st == 128u || st == 256u || st == 512u || st == 1024u)))
+        rc = e->fail(PT_ERR_INVALID_ARG, "traversal_threads must be 64, 128 or 256 and shade_threads 128, 256, 512 or 1024");
     if (!rc) rc = e->cuda(cudaSetDevice(e->cfg.device), "cudaSetDevice");
     if (!rc) rc = e->cuda(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "stream");
     if (!rc) rc = e->cuda(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, e->cfg.device), "SM count");
@@ -1388,7 +1389,8 @@ int pte_autotune(pt_engine* e, const pt_job_desc* jobs, uint32_t count, pt_engin
     const uint32_t tiles[] = {16, 32, 64};
     const uint32_t steps[] = {16, 32};
     const uint32_t sorts[] = {0xffffffffu, 65536u};
-    const uint32_t shapes[] = {64, 128, 256};
+    const uint32_t traversal_shapes[] = {64, 128, 256};
+    const uint32_t shade_shapes[] = {128, 256, 512, 1024};
     pt_engine_config best = e->cfg;
     double best_rate = -1.0;
     // renders the jobs under e->cfg: one untimed pass to capture graphs, then the timed pass
@@ -1439,8 +1441,8 @@ int pte_autotune(pt_engine* e, const pt_job_desc* jobs, uint32_t count, pt_engin
         if ((rc = setup_wave(e))) return rc;
     }
     const pt_engine_config base = best;
-    for (uint32_t TT : shapes)
-        for (uint32_t ST : shapes) {
+    for (uint32_t TT : traversal_shapes)
+        for (uint32_t ST : shade_shapes) {
             if (TT == base.traversal_threads && ST == base.shade_threads) continue;  // measured above
             e->cfg = base;
             e->cfg.traversal_threads = TT;

@@ -18,7 +18,8 @@ class Engine:
         """precision: PT_PRECISION_* bits (0 = the reference's FP32 buffers, 7 = the compressed form);
         sort_min_hits: hits of a bounce are sorted by triangle bucket before shading from this many on
         (0 = the default 65536, 0xffffffff = never); traversal_threads / shade_threads: threads per block
-        of the traversal and shading kernels, 64, 128 or 256 (0 = 128)."""
+        of the traversal kernels (64, 128 or 256; 0 = 128) and of the shading kernel (128, 256, 512 or 1024;
+        0 = 1024)."""
         self._lib = load()
         cfg = abi.EngineConfig(device, hbm_budget_bytes, wave_paths, tile_size, steps_per_refill, int(use_graphs),
                                precision, sort_min_hits, traversal_threads, shade_threads)

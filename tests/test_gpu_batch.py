@@ -124,7 +124,7 @@ def test_non_opaque_jobs_equal_alone(scenes):
 
 
 
-@pytest.mark.parametrize("shapes", [(64, 256), (256, 64)])
+@pytest.mark.parametrize("shapes", [(64, 256), (256, 128), (128, 512)])
 def test_block_shapes_keep_bits(scenes, shapes):
     """Other threads-per-block choices for the traversal and shading kernels give the same bits."""
     eng = Engine(wave_paths=1 << 15, tile_size=16, traversal_threads=shapes[0], shade_threads=shapes[1])
@@ -235,7 +235,7 @@ def test_autotune_picks_a_candidate(scenes):
     assert cfg["wave_paths"] in (1 << 20, 1 << 21, 1 << 22, 1 << 23)
     assert cfg["tile_size"] in (16, 32, 64) and cfg["steps_per_refill"] in (16, 32)
     assert cfg["sort_min_hits"] in (65536, 0xFFFFFFFF)
-    assert cfg["traversal_threads"] in (64, 128, 256) and cfg["shade_threads"] in (64, 128, 256)
+    assert cfg["traversal_threads"] in (64, 128, 256) and cfg["shade_threads"] in (128, 256, 512, 1024)
     st = eng.stats()
     assert (st["traversal_threads"], st["shade_threads"]) == (cfg["traversal_threads"], cfg["shade_threads"])
     j = eng.submit(sid, cam, 64, 64, 2, 4)
