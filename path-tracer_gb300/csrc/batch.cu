@@ -287,7 +287,8 @@ __global__ void __launch_bounds__(kThreads, blocks_for(kWide ? PT_WIDE_MIN_BLOCK
                 b.q.color[path] = make_float4(sum.x, sum.y, sum.z, 0.0f);
             }
             return true;
-        });
+        },
+        NoRound(), step_kind<PT_MAJORITY_SHADOW && !kWide>(tr));
 }
 
 // accumulate, trace.slang:1299-1308: one block per item, samples in order;
