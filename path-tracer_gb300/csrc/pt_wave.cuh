@@ -106,6 +106,12 @@ constexpr uint32_t kWideLeafMerge = PT_WIDE_LEAF_MERGE;
 #ifndef PT_WIDE_OCTANT
 #define PT_WIDE_OCTANT 1
 #endif
+// 1: the accepted children are collected in slot order and the 8-bit mask is
+// permuted to octant order once per node; 0: each child sets its octant-order
+// bit directly
+#ifndef PT_WIDE_MASK_PERMUTE
+#define PT_WIDE_MASK_PERMUTE 1
+#endif
 // resident blocks per SM the 8-wide traversal kernels are compiled for
 #ifndef PT_WIDE_MIN_BLOCKS
 #define PT_WIDE_MIN_BLOCKS 8
@@ -650,7 +656,11 @@ struct WideTraverser {
             const float t_near = fmaxf(fmaxf(nx, ny), fmaxf(nz, 0.0f));
             const float t_far = fminf(fminf(fx, fy), fminf(fz, hit_t));
 #endif
+#if PT_WIDE_MASK_PERMUTE
+            if (t_near <= t_far) mask |= 1u << i;
+#else
             if ((uint32_t)i < count && t_near <= t_far) mask |= 1u << ((uint32_t)i ^ oct);
+#endif
         };
         child(std::integral_constant<int, 0>());
         child(std::integral_constant<int, 1>());
@@ -660,6 +670,13 @@ struct WideTraverser {
         child(std::integral_constant<int, 5>());
         child(std::integral_constant<int, 6>());
         child(std::integral_constant<int, 7>());
+#if PT_WIDE_MASK_PERMUTE
+        // slot order -> octant order: bit i moves to bit i ^ oct
+        mask &= (1u << count) - 1u;
+        if (oct & 1u) mask = ((mask & 0x55u) << 1) | ((mask >> 1) & 0x55u);
+        if (oct & 2u) mask = ((mask & 0x33u) << 2) | ((mask >> 2) & 0x33u);
+        if (oct & 4u) mask = ((mask & 0x0fu) << 4) | ((mask >> 4) & 0x0fu);
+#endif
         return mask;
     }
 #else
