@@ -260,7 +260,7 @@ template <bool kWide, int kThreads = kExtendThreads>
 __global__ void __launch_bounds__(kThreads, blocks_for(kWide ? PT_WIDE_MIN_BLOCKS : PT_EXTEND_MIN_BLOCKS, kExtendThreads, kThreads))
     shadow_kernel(const SceneDev* scenes, WaveBufs b, uint32_t steps_per_refill) {
     const uint32_t count = b.q.cnt[2];
-    typename std::conditional<kWide, WideTraverser<true>, Traverser<false, false, true>>::type tr;
+    typename std::conditional<kWide, WideTraverser<true>, Traverser<false, false, true, false, PT_SHADOW_TRI_PER_STEP != 0>>::type tr;
     constexpr uint32_t kShared = kWide ? kWideSmemStack : kSmemStack;
     __shared__ uint2 stack_top[kShared > 0u ? kShared * kThreads : 1u];
     LaneStack<kThreads, kShared> stack;

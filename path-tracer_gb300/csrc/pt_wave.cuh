@@ -120,6 +120,11 @@ constexpr uint32_t kWideLeafMerge = PT_WIDE_LEAF_MERGE;
 #ifndef PT_TRI_PER_STEP
 #define PT_TRI_PER_STEP 1
 #endif
+// the same for the binary shadow (any-hit) traversal, whose warps run the
+// majority kind of step: there whole leaves per step measured 6 % faster
+#ifndef PT_SHADOW_TRI_PER_STEP
+#define PT_SHADOW_TRI_PER_STEP 0
+#endif
 // order the next bounce's rays / the shadow rays by direction octant before
 // their traversal (when the hit sort is on and a queue holds at least its
 // threshold); measured slower: the octant split breaks up the origin
@@ -272,7 +277,7 @@ PTD float box_test(float4 lo, float4 hi, f3 nod, f3 rcp, float hit_t) {
 // tri_count) of each node, so a pop needs no memory access.  Node visits
 // happen in exactly the reference's order.  The stacks live outside the
 // object so its scalar state can stay in registers.
-template <bool kRec, bool kAlpha, bool kShadow, bool kTri36 = false>
+template <bool kRec, bool kAlpha, bool kShadow, bool kTri36 = false, bool kTriStep = (PT_TRI_PER_STEP != 0)>
 struct Traverser {
     f3 o, d, rcp, nod;
     Shear s;
@@ -350,16 +355,27 @@ struct Traverser {
         return false;
     }
 
-#if PT_TRI_PER_STEP
-    // whether the next step() is an interior visit (else a triangle test)
-    PTD bool next_is_interior() const { return tri_left == 0u && tc == 0u; }
+    // whether the next step() is an interior visit (else a triangle test, or
+    // a whole leaf)
+    PTD bool next_is_interior() const { return kTriStep ? (tri_left == 0u && tc == 0u) : tc == 0u; }
+
+    // kTriStep: one interior visit or one triangle of a leaf per step, else
+    // one interior visit or a whole leaf
+    template <class S>
+    PTD bool step(const World& w, const Fast& f, S& stack, uint32_t* istack) {
+        if constexpr (kTriStep)
+            return step_tri(w, f, stack, istack);
+        else
+            return step_leaf(w, f, stack, istack);
+    }
+
 
     // one interior node visit or one triangle test; true when the traversal
     // has finished (for kShadow, hit == 1 marks an occluder).  Testing a
     // leaf's triangles one per step keeps the two divergent paths of a warp
     // (box pair vs triangle) about equally long.
     template <class S>
-    PTD bool step(const World& w, const Fast& f, S& stack, uint32_t* istack) {
+    PTD bool step_tri(const World& w, const Fast& f, S& stack, uint32_t* istack) {
         if (tri_left == 0u) {
             rec.visit(idx);
             if (tc == 0u) {
@@ -399,11 +415,10 @@ struct Traverser {
         if (tri_left > 0u) return false;
         return pop(stack, istack);
     }
-#else
     // one node visit; true when the traversal has finished (for kShadow,
     // hit == 1 marks an occluder)
     template <class S>
-    PTD bool step(const World& w, const Fast& f, S& stack, uint32_t* istack) {
+    PTD bool step_leaf(const World& w, const Fast& f, S& stack, uint32_t* istack) {
         rec.visit(idx);
         if (tc > 0u) {
             rec.leaf();
@@ -461,7 +476,6 @@ struct Traverser {
         }
         return pop(stack, istack);
     }
-#endif
 };
 
 // Sort 8 keys ascending (a 19-comparator network: no dynamic indexing, so the

@@ -216,7 +216,8 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
     static_assert(!(kWide && kRec), "the wide form keeps no records");
     const uint32_t count = q.cnt[2];
     const bool ordered = PT_SHADOW_ORDER && q.cnt[9] != 0u;
-    typename std::conditional<kWide, WideTraverser<true, kTri36>, Traverser<kRec, false, true, kTri36>>::type tr;
+    typename std::conditional<kWide, WideTraverser<true, kTri36>,
+                              Traverser<kRec, false, true, kTri36, PT_SHADOW_TRI_PER_STEP != 0>>::type tr;
     constexpr uint32_t kShared = kWide ? kWideSmemStack : kSmemStack;
     __shared__ uint2 stack_top[kShared > 0u ? kShared * kExtendThreads : 1u];
     LaneStack<kExtendThreads, kShared> stack;
