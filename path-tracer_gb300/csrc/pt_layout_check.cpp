@@ -4,6 +4,7 @@
 #include <cstddef>
 
 #include "../../include/pt.h"
+#include "../../include/pt_batch.h"
 
 #define CHECK_SIZE(T, n) static_assert(sizeof(T) == (n), #T " size")
 #define CHECK_OFF(T, f, n) static_assert(offsetof(T, f) == (n), #T "." #f " offset")
@@ -40,5 +41,15 @@ CHECK_SIZE(pt_skybox_uniforms, 16);
 CHECK_SIZE(pt_skybox_alias_entry, 12);
 CHECK_SIZE(pt_trace_parameters, 32);
 CHECK_SIZE(pt_path_record, 144);
+// the batched engine's structs, mirrored by the Python binding
+CHECK_SIZE(pt_engine_config, 48);
+CHECK_OFF(pt_engine_config, hbm_budget_bytes, 8);
+CHECK_OFF(pt_engine_config, traversal_threads, 40);
+CHECK_OFF(pt_engine_config, shade_threads, 44);
+CHECK_SIZE(pt_job_desc, 96);
+CHECK_OFF(pt_job_desc, continue_job, 88);
+CHECK_SIZE(pt_engine_stats, 120);
+CHECK_OFF(pt_engine_stats, gpu_ms, 80);
+CHECK_OFF(pt_engine_stats, shade_threads, 116);
 
 extern "C" int pt_layout_checked(void) { return 1; }

@@ -317,6 +317,9 @@ class EngineStats(C.Structure):
                 ("sort_min_hits", c_u32), ("traversal_threads", c_u32), ("shade_threads", c_u32)]
 
 
+STRUCT_SIZES.update({EngineConfig: 48, JobDesc: 96, EngineStats: 120})
+
+
 SIGNATURES.update({
     "pte_create": (C.c_int, [P(EngineConfig), P(_vp)]),
     "pte_destroy": (None, [_vp]),

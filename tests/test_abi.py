@@ -15,7 +15,7 @@ def declared_functions():
     names = set()
     for header in (ROOT / "include").glob("*.h"):
         text = re.sub(r"/\*.*?\*/", "", header.read_text(), flags=re.S)
-        for m in re.finditer(r"\b(pt[w]?_[a-z0-9_]+)\s*\(", text):
+        for m in re.finditer(r"\b(pt[we]?_[a-z0-9_]+)\s*\(", text):
             names.add(m.group(1))
     return names
 
@@ -31,6 +31,9 @@ def test_field_offsets():
     assert abi.Material.specular_weight_uv.offset == 208
     assert abi.TriangleAttribute.t0.offset == 64
     assert abi.BvhNode.tri_count.offset == 28
+    assert abi.EngineConfig.shade_threads.offset == 44
+    assert abi.JobDesc.continue_job.offset == 88
+    assert abi.EngineStats.gpu_ms.offset == 80 and abi.EngineStats.shade_threads.offset == 116
 
 
 def test_library_exports_every_declared_symbol():
