@@ -239,3 +239,26 @@ def test_wide_box_test_accepts_whatever_the_binary_test_accepts():
         wid = wide_accept(origin, ebyte, qlo, qhi, rcp, nod, hit_t)
         misses += int(np.count_nonzero(ref & ~wid))
     assert misses == 0
+
+
+def test_wide_children_placed_for_octant_order():
+    """Eight clusters at the corners of a cube: the root wide node holds one cluster per slot, and slot s
+    holds the cluster lying furthest back along octant s's direction (minus on the axes of s's set bits),
+    so a ray with direction signs o that visits slots i ^ o, i = 0..7, meets the nearest cluster first."""
+    rng = np.random.default_rng(5)
+    tris = []
+    for corner in range(8):
+        c = np.array([(1 if corner & (1 << a) else -1) * 10.0 for a in range(3)])
+        tris.append(c + rng.normal(0, 0.5, (6, 3, 3)))
+    tris = np.concatenate(tris).astype(np.float32).reshape(-1, 9)
+    nodes, _ = pt.build_bvh(tris)
+    wide = check_wide(nodes, tris.shape[0])
+    root = wide[0]
+    assert int(root["child_count"]) == 8
+    for s in range(8):
+        center = [float(decode(root["origin"][a], root["lo"][a][s:s + 1], root["exponent"][a:a + 1])[0] +
+                        decode(root["origin"][a], root["hi"][a][s:s + 1], root["exponent"][a:a + 1])[0]) / 2
+                  for a in range(3)]
+        for a in range(3):
+            # D(s)[a] = -1 when bit a of s is set, so the slot's cluster sits at +10 there, else at -10
+            assert (center[a] > 0) == bool(s & (1 << a)), (s, a, center)
