@@ -869,12 +869,11 @@ int upload_scene(pt_engine* e, Scene& s, const pt_world_updates* u) {
         }
     }
     if (!rc && form.wide) {
-        uint64_t count = 0;
         uint32_t depth = 0;
-        if (pt_build_wide_bvh(sc->bvh_nodes, sc->node_count, kWideLeafMerge, nullptr, 0, &count, &depth) != PT_OK)
+        std::vector<pt_wide_node> wide;
+        if (ptw::build_wide_bvh(sc->bvh_nodes, sc->node_count, kWideLeafMerge, wide, &depth) != PT_OK)
             return e->fail(PT_ERR_INVALID_ARG, "the BVH cannot be collapsed into 8-wide nodes");
-        std::vector<pt_wide_node> wide(count);
-        pt_build_wide_bvh(sc->bvh_nodes, sc->node_count, kWideLeafMerge, wide.data(), count, &count, &depth);
+        const uint64_t count = wide.size();
         std::vector<uint32_t> links(sc->node_count + sc->triangle_count);
         if (!ptw::build_bvh_links(sc->bvh_nodes, sc->node_count, sc->triangle_count, links.data(),
                                   links.data() + sc->node_count))

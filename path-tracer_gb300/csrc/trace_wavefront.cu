@@ -479,13 +479,11 @@ cudaError_t build_wide(Wavefront* wf, const ptd::World& w, uint64_t nodes, uint6
     std::vector<pt_bvh_node> host(nodes);
     PTW_TRY(cudaMemcpyAsync(host.data(), w.nodes, nodes * sizeof(pt_bvh_node), cudaMemcpyDeviceToHost, stream));
     PTW_TRY(cudaStreamSynchronize(stream));
-    uint64_t count = 0;
     uint32_t depth = 0;
-    if (pt_build_wide_bvh(host.data(), nodes, ptd::kWideLeafMerge, nullptr, 0, &count, &depth) != PT_OK)
+    std::vector<pt_wide_node> wide;
+    if (ptw::build_wide_bvh(host.data(), nodes, ptd::kWideLeafMerge, wide, &depth) != PT_OK)
         return cudaErrorInvalidValue;
-    std::vector<pt_wide_node> wide(count);
-    if (pt_build_wide_bvh(host.data(), nodes, ptd::kWideLeafMerge, wide.data(), count, &count, &depth) != PT_OK)
-        return cudaErrorInvalidValue;
+    const uint64_t count = wide.size();
     std::vector<uint32_t> links(nodes + tris);
     if (!ptw::build_bvh_links(host.data(), nodes, tris, links.data(), links.data() + nodes)) return cudaErrorInvalidValue;
     PTW_TRY(wf->wide.reserve(count * sizeof(pt_wide_node)));

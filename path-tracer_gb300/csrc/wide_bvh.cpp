@@ -14,6 +14,7 @@
 // bounds, a wide box test accepts every ray the binary node's test accepts.
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "../../include/pt_precision.h"
@@ -86,31 +87,35 @@ bool quantise_axis(float origin, const float* lo, const float* hi, int n, uint8_
     return false;
 }
 
-// Places the n children of a wide node into slots 0..n-1 so that a ray whose
+// Places the children of a wide node into slots 0..n-1 so that a ray whose
 // direction has sign bits o (bit a set when d[a] < 0) meets them roughly
 // nearest first when it visits slot i ^ o for i = 0, 1, ..., 7: slot s should
 // hold the child lying furthest back along the direction of octant s, D(s) =
 // (+-1, +-1, +-1) with a minus for each set bit of s.  Cost of child c in slot s
-// = dot(centre(c) - centre(parent), D(s)); pairs are taken greedily, lowest
-// cost first (the assignment of Ylitie, Karras and Laine, "Efficient
-// Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs", HPG 2017).
-// The order changes no result: every accepted child is still visited and
-// exact-t ties are resolved by the binary traversal's order.
-void order_by_octant(const pt_bvh_node* nodes, uint32_t* kids, int n) {
+// = dot(centre(c) - centre(node), D(s)) over the decoded child boxes; pairs
+// are taken greedily, lowest cost first (the assignment of Ylitie, Karras and
+// Laine, "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide
+// BVHs", HPG 2017).  A slot carries its box bytes, child index and triangle
+// count, so the permutation keeps the tree; the order changes no result:
+// every accepted child is still visited and exact-t ties are resolved by the
+// binary traversal's order.
+void order_by_octant(pt_wide_node& node) {
+    const int n = node.child_count;
     if (n < 2) return;
-    for (int i = 0; i < n; ++i)
-        if (!finite_box(nodes[kids[i]])) return;  // rejected by the caller
-    double cen[8][3], pc[3] = {0.0, 0.0, 0.0};
-    for (int i = 0; i < n; ++i)
-        for (int a = 0; a < 3; ++a) {
-            cen[i][a] = 0.5 * ((double)nodes[kids[i]].aabb_min[a] + (double)nodes[kids[i]].aabb_max[a]);
-            pc[a] += cen[i][a] / n;
+    float cen[8][3], pc[3] = {0.0f, 0.0f, 0.0f};
+    for (int a = 0; a < 3; ++a) {
+        const float s = std::ldexp(1.0f, (int)node.exponent[a] - 127);
+        for (int i = 0; i < n; ++i) {
+            cen[i][a] = 0.5f * s * ((float)node.lo[a][i] + (float)node.hi[a][i]);  // relative to the origin
+            pc[a] += cen[i][a];
         }
-    double cost[8][8];
+        pc[a] /= (float)n;
+    }
+    float cost[8][8];
     for (int i = 0; i < n; ++i)
         for (int s = 0; s < n; ++s) {
-            double c = 0.0;
-            for (int a = 0; a < 3; ++a) c += ((s >> a) & 1 ? -1.0 : 1.0) * (cen[i][a] - pc[a]);
+            float c = 0.0f;
+            for (int a = 0; a < 3; ++a) c += ((s >> a) & 1 ? -1.0f : 1.0f) * (cen[i][a] - pc[a]);
             cost[i][s] = c;
         }
     int slot_of[8];
@@ -128,9 +133,34 @@ void order_by_octant(const pt_bvh_node* nodes, uint32_t* kids, int n) {
         child_done[bi] = slot_done[bs] = true;
         slot_of[bi] = bs;
     }
-    uint32_t out[8];
-    for (int i = 0; i < n; ++i) out[slot_of[i]] = kids[i];
-    for (int i = 0; i < n; ++i) kids[i] = out[i];
+    const pt_wide_node in = node;
+    for (int i = 0; i < n; ++i) {
+        const int s = slot_of[i];
+        for (int a = 0; a < 3; ++a) {
+            node.lo[a][s] = in.lo[a][i];
+            node.hi[a][s] = in.hi[a][i];
+        }
+        node.child[s] = in.child[i];
+        node.tri_count[s] = in.tri_count[i];
+    }
+}
+
+// order_by_octant over all nodes, on up to 16 host threads (nodes are independent)
+void order_all_by_octant(std::vector<pt_wide_node>& wide) {
+    const size_t count = wide.size();
+    unsigned threads = std::thread::hardware_concurrency();
+    threads = threads == 0 ? 1 : (threads > 16 ? 16 : threads);
+    if (count < 4096) threads = 1;
+    const size_t per = (count + threads - 1) / threads;
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < threads; ++t) {
+        const size_t lo = t * per, hi = lo + per < count ? lo + per : count;
+        if (lo >= hi) break;
+        pool.emplace_back([&wide, lo, hi]() {
+            for (size_t k = lo; k < hi; ++k) order_by_octant(wide[k]);
+        });
+    }
+    for (auto& th : pool) th.join();
 }
 
 struct Work {
@@ -141,8 +171,11 @@ struct Work {
 
 }  // namespace
 
-extern "C" int pt_build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, uint32_t max_leaf_triangles,
-                                 pt_wide_node* out, uint64_t capacity, uint64_t* wide_count, uint32_t* wide_depth) {
+namespace {
+
+// the collapse proper, without the octant placement
+int collapse(const pt_bvh_node* nodes, uint64_t node_count, uint32_t max_leaf_triangles,
+             std::vector<pt_wide_node>& wide, uint32_t* wide_depth) {
     if (!nodes || node_count == 0 || node_count > 0xffffffffull) return PT_ERR_INVALID_ARG;
     // triangle range of every binary subtree (children follow their parent in
     // the reference's layout, so one backward pass suffices); a subtree of at
@@ -176,7 +209,7 @@ extern "C" int pt_build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, 
     const auto as_leaf = [&](uint32_t b) {
         return nodes[b].tri_count != 0 || (max_leaf_triangles > 0 && sub_count[b] <= max_leaf_triangles);
     };
-    std::vector<pt_wide_node> wide(1);
+    wide.assign(1, pt_wide_node{});
     std::memset(wide.data(), 0, sizeof(pt_wide_node));
     std::vector<Work> stack{{0u, 0u, 1u}};
     uint32_t max_depth = 0;
@@ -218,7 +251,6 @@ extern "C" int pt_build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, 
             kids[best + 1] = nodes[open].left_first + 1;
             ++n;
         }
-        order_by_octant(nodes, kids, n);
         float lo[3][8], hi[3][8];
         for (int i = 0; i < n; ++i) {
             const pt_bvh_node& c = nodes[kids[i]];
@@ -262,10 +294,28 @@ extern "C" int pt_build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, 
         for (int i = n - 1; i >= 0; --i)
             if (node.tri_count[i] == 0) stack.push_back({kids[i], node.child[i], wk.depth + 1});
     }
-    if (wide_count) *wide_count = wide.size();
     if (wide_depth) *wide_depth = max_depth;
+    return PT_OK;
+}
+
+}  // namespace
+
+int ptw::build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, uint32_t max_leaf_triangles,
+                        std::vector<pt_wide_node>& wide, uint32_t* wide_depth) {
+    const int rc = collapse(nodes, node_count, max_leaf_triangles, wide, wide_depth);
+    if (rc == PT_OK) order_all_by_octant(wide);
+    return rc;
+}
+
+extern "C" int pt_build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, uint32_t max_leaf_triangles,
+                                 pt_wide_node* out, uint64_t capacity, uint64_t* wide_count, uint32_t* wide_depth) {
+    std::vector<pt_wide_node> wide;
+    const int rc = collapse(nodes, node_count, max_leaf_triangles, wide, wide_depth);
+    if (rc != PT_OK) return rc;
+    if (wide_count) *wide_count = wide.size();
     if (!out) return PT_OK;
     if (capacity < wide.size()) return PT_ERR_OUT_OF_LIMITS;
+    order_all_by_octant(wide);
     std::memcpy(out, wide.data(), wide.size() * sizeof(pt_wide_node));
     return PT_OK;
 }
