@@ -53,9 +53,9 @@ KERNEL_NAMES = {"wavefront": 0, "plain": 1}
 # compressed form (wide BVH + FP16 attributes / BF16 skybox + Kahan sums)
 PRECISIONS = {"fp32": 0, "wide": 1, "compressed": 7}
 # DRAM bytes (read + write) per launch of the dominant kernel on this workload
-# (1920x1080, 64 spp, FP32 form), from the single-pass ncu capture of the
-# first 16-spp group's 9 launches summarised in
-# profiles/wavefront_procedural_1920x1080.md
+# (1920x1080, 64 spp, FP32 form), measured by a single-pass ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum) of the first 16-spp group's
+# 9 extend launches
 TRAFFIC_PER_LAUNCH: dict = {("wavefront", "extend", "fp32"): 549.0e6}
 
 

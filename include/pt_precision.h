@@ -106,6 +106,22 @@ uint32_t pt_precision_active(const pt_ctx* ctx);
  * zeros unless PT_PRECISION_KAHAN is set. */
 #define PT_TILE_COMPENSATION 2
 
+/* FP64 reference render of the current tile: the image error of every form
+ * above is stated against it.  Traces the samples sample_first ..
+ * sample_first + sample_count - 1 (1-based sample indices n of the seed,
+ * trace.slang:736-737) of every tile pixel inside the image, one thread per
+ * path, in double arithmetic with CUDA's double-precision math functions,
+ * from the same FP32 world buffers (binary BVH, FP32 attributes and skybox,
+ * whatever precision form is selected), with the shader's own f32 random
+ * numbers.  Writes per-pixel radiance SUMS over those samples to
+ * host_rgb_sums (tile_w * tile_h * 3 doubles, row stride tile_w; pixels
+ * outside the image are 0).  The accumulation buffer, storage texture and
+ * sample count are not touched.  This is the only code of the library that
+ * computes in FP64; no counterpart in the reference.
+ * PT_ERR_INVALID_ARG for sample_first == 0, sample_count == 0 or a range
+ * past 2^32 - 1; PT_ERR_STATE without a world. */
+int pt_render_fp64(pt_ctx* ctx, uint32_t sample_first, uint32_t sample_count, double* host_rgb_sums);
+
 #ifdef __cplusplus
 }
 #endif

@@ -65,6 +65,12 @@ def load() -> C.CDLL:
         lib.oracle_fmath.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64]
         lib.oracle_max_threads.restype = C.c_int
         lib.oracle_max_threads.argtypes = []
+        lib.oracle_elementary.restype = C.c_int
+        lib.oracle_elementary.argtypes = [C.c_int, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.oracle_shade_cases.restype = C.c_int
+        lib.oracle_shade_cases.argtypes = [C.c_int, C.c_void_p, C.c_uint64, C.c_void_p]
+        lib.oracle_sample_lights.restype = C.c_int
+        lib.oracle_sample_lights.argtypes = [P(OracleWorld), C.c_int, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p]
         _LIB = lib
     return _LIB
 
@@ -148,6 +154,60 @@ def fmath(name: str, x, y=None) -> np.ndarray:
     return out
 
 
+# oracle_elementary operations (oracle.h ORACLE_OP_*): name -> (op, inputs, output components)
+ELEMENTARY = {"normalize": 0, "dot": 1, "mix": 2, "reflect": 3, "fract": 4, "min": 5, "max": 6, "clamp": 7,
+              "rsqrt": 8, "to_u32": 9, "srgb": 10, "slab": 11, "camera_ray": 12}
+_ELEM_OUT = {"normalize": 3, "reflect": 3, "camera_ray": 3}
+
+
+def elementary(name: str, a, b=None, c=None) -> np.ndarray:
+    """One of the parity mode's elementary operations over n elements (vectors as n x 3)."""
+    op = ELEMENTARY[name]
+    aa = np.ascontiguousarray(a, dtype=np.float32)
+    n = aa.shape[0]
+    ba = np.ascontiguousarray(b, dtype=np.float32) if b is not None else None
+    ca = np.ascontiguousarray(c, dtype=np.float32) if c is not None else None
+    k = _ELEM_OUT.get(name, 1)
+    out = np.zeros((n, k) if k > 1 else n, dtype=np.float32)
+    rc = load().oracle_elementary(op, n, aa.ctypes.data, ba.ctypes.data if ba is not None else None,
+                                  ca.ctypes.data if ca is not None else None, out.ctypes.data)
+    if rc != 0:
+        raise ValueError("oracle_elementary rejected its arguments")
+    return out.view(np.uint32) if name == "to_u32" else out
+
+
+SHADE_CASE = np.dtype([("base_color", "<f4", 3), ("base_weight", "<f4"), ("base_metalness", "<f4"),
+                       ("base_diffuse_roughness", "<f4"), ("specular_color", "<f4", 3), ("specular_weight", "<f4"),
+                       ("specular_roughness", "<f4"), ("specular_anisotropy", "<f4"), ("specular_ior", "<f4"),
+                       ("wo", "<f4", 3), ("wi", "<f4", 3), ("rng", "<u4")])
+SHADE_RESULT = np.dtype([("e_dielectric", "<f8", 3), ("p_ggx", "<f8"), ("p_u", "<f8"), ("f", "<f8", 3),
+                         ("pdf", "<f8"), ("sampled_wi", "<f8", 3), ("sampled_f", "<f8", 3), ("sampled_pdf", "<f8"),
+                         ("rng_after", "<u4"), ("pad", "<u4")])
+LIGHT_RESULT = np.dtype([("direction", "<f8", 3), ("distance", "<f8"), ("emission", "<f8", 3), ("pdf", "<f8"),
+                         ("triangle_index", "<i4"), ("rng_after", "<u4")])
+assert SHADE_CASE.itemsize == 80 and SHADE_RESULT.itemsize == 136 and LIGHT_RESULT.itemsize == 72
+
+
+def shade_cases(cases: np.ndarray, precision: int = 32) -> np.ndarray:
+    """Shading points (SHADE_CASE records) -> SHADE_RESULT records (oracle_shade_cases)."""
+    cs = np.ascontiguousarray(cases, dtype=SHADE_CASE)
+    out = np.zeros(cs.shape[0], dtype=SHADE_RESULT)
+    if load().oracle_shade_cases(precision, cs.ctypes.data, cs.shape[0], out.ctypes.data) != 0:
+        raise ValueError("oracle_shade_cases rejected its arguments")
+    return out
+
+
+def sample_lights(world: OracleWorld, origins, rng_states, precision: int = 32) -> np.ndarray:
+    """sample_light from each origin with its RNG state -> LIGHT_RESULT records."""
+    o = np.ascontiguousarray(origins, dtype=np.float32).reshape(-1, 3)
+    r = np.ascontiguousarray(rng_states, dtype=np.uint32)
+    out = np.zeros(o.shape[0], dtype=LIGHT_RESULT)
+    if load().oracle_sample_lights(C.byref(world), precision, o.shape[0], o.ctypes.data, r.ctypes.data,
+                                   out.ctypes.data) != 0:
+        raise ValueError("oracle_sample_lights rejected its arguments")
+    return out
+
+
 def max_threads() -> int:
     return load().oracle_max_threads()
 
@@ -163,4 +223,4 @@ def accumulate(radiance: np.ndarray) -> np.ndarray:
 
 
 __all__ = ["OracleWorld", "world_from_updates", "trace_paths", "intersect", "rand_sequence", "seed", "fmath",
-           "accumulate", "max_threads", "load"]
+           "accumulate", "max_threads", "load", "elementary", "shade_cases", "sample_lights", "SHADE_CASE"]

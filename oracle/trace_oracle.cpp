@@ -680,20 +680,94 @@ struct Tracer {
         return {f_total, b.p_ggx * pdf_ggx + b.p_diffuse * pdf_eon};
     }
 
-    // compute_main, trace.slang:721-1297: radiance of one sample
-    V3<T> trace(uint32_t px, uint32_t py, const uint32_t image_size[2], uint32_t sample_count, uint32_t max_bounces) {
-        rng = (px * 0x9E3779B9u) ^ (py * 0x85EBCA6Bu) ^ (0u * 0xC2B2AE35u) ^ (sample_count * 0x27D4EB2Du) ^ 0xA511E9B3u;
-        rng |= 1u;
+    // OpenPBR setup of one shading point, trace.slang:1097-1181 (draws the 32
+    // random numbers of estimate_e_dielectric)
+    Bsdf setup_bsdf(V3<T> base_color, T base_weight, T base_metalness, T base_diffuse_roughness, V3<T> specular_color,
+                    T specular_weight, T specular_roughness, T specular_anisotropy, T specular_ior, V3<T> wo) {
+        Bsdf b;
+        b.alpha = alpha_anisotropic(specular_roughness, specular_anisotropy);
+        b.ior_m = specular_ior_modulated(specular_ior, specular_weight);
+        b.f0 = base_weight * base_color;
+        b.opl = T(1) + ggx_lambda(wo, b.alpha);
+        const T r = base_diffuse_roughness;
+        const T z = wo.z;
+        b.ltc.x = T(1) + r * (K(0.303392) + (K(-0.518982) + K(0.111709) * z) * z + (K(-0.276266) + K(0.335918) * z) * r);
+        b.ltc.y = r * (K(-1.16407) + K(1.15859) * z + (K(0.150815) - K(0.150105) * z) * r) / (z * z * z - K(1.43545));
+        b.ltc.z = T(1) + r * (K(0.20013) + (K(-0.506373) + K(0.261777) * z) * z);
+        b.ltc.w = r * (K(0.540852) + (K(-1.01625) + K(0.475392) * z) * z) / (K(-1.0743) + (K(0.0725628) + z) * z);
+        const T ls = wo.x * wo.x + wo.y * wo.y;
+        V3<T> bx{T(1), T(0), T(0)};
+        if (ls > T(0)) bx = V3<T>{wo.x, wo.y, T(0)} * rsqrt(ls);
+        b.bx = bx;
+        b.by = V3<T>{-bx.y, bx.x, T(0)};
+        b.bz = V3<T>{T(0), T(0), T(1)};
+        b.e_dielectric = estimate_e_dielectric(wo, b.opl, b.alpha, b.ior_m, specular_color);
+        const V3<T> luma{K(0.2126), K(0.7152), K(0.0722)};
+        const T albedo_gloss = dot(b.e_dielectric, luma);
+        const T albedo_diffuse = (T(1) - albedo_gloss) * base_weight * dot(base_color, luma);
+        const V3<T> fsm = b.f0 + (T(1) - b.f0) * fifth_power(T(1) - wo.z);
+        const T albedo_metal = dot(fsm, luma);
+        const T w_ggx = lerp(albedo_gloss, albedo_metal, base_metalness);
+        const T w_diffuse = (T(1) - base_metalness) * albedo_diffuse;
+        b.p_ggx = clamp(w_ggx / M<T>::fmax(w_ggx + w_diffuse, K(1e-7)), K(0.1), K(0.9));
+        b.p_diffuse = T(1) - b.p_ggx;
+        b.p_u = M<T>::pow(r, K(0.1)) * (K(0.162925) + (K(-0.372058) + (K(0.538233) - K(0.290822) * z) * z) * z);
+        b.p_c = T(1) - b.p_u;
+        b.base_color = base_color;
+        b.base_weight = base_weight;
+        b.base_metalness = base_metalness;
+        b.base_diffuse_roughness = base_diffuse_roughness;
+        b.specular_color = specular_color;
+        b.specular_weight = specular_weight;
+        return b;
+    }
+
+    // BSDF sampling, trace.slang:1212-1260 (3 random numbers)
+    V3<T> sample_bsdf(V3<T> wo, const Bsdf& b) {
+        const T two_pi_r = T(2.0f * kPi) * rand();
+        const T r1 = rand();
+        V3<T> wi;
+        if (rand() < b.p_ggx) {
+            wi = reflect(-wo, sample_vndf(wo, b.alpha, r1, two_pi_r));
+        } else if (r1 < b.p_u) {
+            const T u1 = r1 / b.p_u;
+            const T sin_theta = M<T>::sqrt(T(1) - u1 * u1);
+            wi = {sin_theta * M<T>::cos(two_pi_r), sin_theta * M<T>::sin(two_pi_r), u1};
+        } else {
+            const T u1 = (r1 - b.p_u) / b.p_c;
+            const T a = b.ltc.x, bb = b.ltc.y, c = b.ltc.z, dd = b.ltc.w;
+            const T R = M<T>::sqrt(u1);
+            const T y = R * M<T>::sin(two_pi_r);
+            const T s = M<T>::fma(K(0.5), rsqrt(M<T>::fma(dd, dd, T(1))), K(0.5));
+            const T x = -lerp(M<T>::sqrt(M<T>::fma(-y, y, T(1))), R * M<T>::cos(two_pi_r), s);
+            const V3<T> wh{x, y, M<T>::sqrt(M<T>::fmax(T(1) - (x * x + y * y), T(0)))};
+            const V3<T> wu{a * wh.x + bb * wh.z, c * wh.y, dd * wh.x + wh.z};
+            wi = normalize(wu.x * b.bx + wu.y * b.by + wu.z * b.bz);
+        }
+        return wi;
+    }
+
+    // camera ray, trace.slang:739-748: the jitter takes the first two draws,
+    // x then y (float2(rand(), rand()) evaluated left to right)
+    void camera_ray(const pt_camera& cam, uint32_t px, uint32_t py, const uint32_t image_size[2], V3<T>* o,
+                    V3<T>* d) {
         const T jx = rand();
         const T jy = rand();
         const V2<T> puv{(T((float)px) + jx) / T((float)image_size[0]), (T((float)py) + jy) / T((float)image_size[1])};
-        const pt_camera& cam = w.camera;
-        V3<T> o{T(cam.position[0]), T(cam.position[1]), T(cam.position[2])};
+        *o = V3<T>{T(cam.position[0]), T(cam.position[1]), T(cam.position[2])};
         const V3<T> llc{T(cam.lower_left_corner_minus_position[0]), T(cam.lower_left_corner_minus_position[1]),
                         T(cam.lower_left_corner_minus_position[2])};
         const V3<T> hor{T(cam.horizontal[0]), T(cam.horizontal[1]), T(cam.horizontal[2])};
         const V3<T> ver{T(cam.vertical[0]), T(cam.vertical[1]), T(cam.vertical[2])};
-        V3<T> d = normalize(llc + puv.x * hor + puv.y * ver);
+        *d = normalize(llc + puv.x * hor + puv.y * ver);
+    }
+
+    // compute_main, trace.slang:721-1297: radiance of one sample
+    V3<T> trace(uint32_t px, uint32_t py, const uint32_t image_size[2], uint32_t sample_count, uint32_t max_bounces) {
+        rng = (px * 0x9E3779B9u) ^ (py * 0x85EBCA6Bu) ^ (0u * 0xC2B2AE35u) ^ (sample_count * 0x27D4EB2Du) ^ 0xA511E9B3u;
+        rng |= 1u;
+        V3<T> o, d;
+        camera_ray(w.camera, px, py, image_size, &o, &d);
         V3<T> rcp = T(1) / d;
         V3<T> throughput{T(1), T(1), T(1)};
         V3<T> color{T(0), T(0), T(0)};
@@ -794,42 +868,9 @@ struct Tracer {
             }
 
             // OpenPBR setup, trace.slang:1097-1181
-            Bsdf b;
-            b.alpha = alpha_anisotropic(specular_roughness, specular_anisotropy);
-            b.ior_m = specular_ior_modulated(specular_ior, specular_weight);
-            b.f0 = base_weight * base_color;
             const V3<T> wo{dot(Tn, V), dot(Bn, V), ndotv};
-            b.opl = T(1) + ggx_lambda(wo, b.alpha);
-            const T r = base_diffuse_roughness;
-            const T z = wo.z;
-            b.ltc.x = T(1) + r * (K(0.303392) + (K(-0.518982) + K(0.111709) * z) * z + (K(-0.276266) + K(0.335918) * z) * r);
-            b.ltc.y = r * (K(-1.16407) + K(1.15859) * z + (K(0.150815) - K(0.150105) * z) * r) / (z * z * z - K(1.43545));
-            b.ltc.z = T(1) + r * (K(0.20013) + (K(-0.506373) + K(0.261777) * z) * z);
-            b.ltc.w = r * (K(0.540852) + (K(-1.01625) + K(0.475392) * z) * z) / (K(-1.0743) + (K(0.0725628) + z) * z);
-            const T ls = wo.x * wo.x + wo.y * wo.y;
-            V3<T> bx{T(1), T(0), T(0)};
-            if (ls > T(0)) bx = V3<T>{wo.x, wo.y, T(0)} * rsqrt(ls);
-            b.bx = bx;
-            b.by = V3<T>{-bx.y, bx.x, T(0)};
-            b.bz = V3<T>{T(0), T(0), T(1)};
-            b.e_dielectric = estimate_e_dielectric(wo, b.opl, b.alpha, b.ior_m, specular_color);
-            const V3<T> luma{K(0.2126), K(0.7152), K(0.0722)};
-            const T albedo_gloss = dot(b.e_dielectric, luma);
-            const T albedo_diffuse = (T(1) - albedo_gloss) * base_weight * dot(base_color, luma);
-            const V3<T> fsm = b.f0 + (T(1) - b.f0) * fifth_power(T(1) - wo.z);
-            const T albedo_metal = dot(fsm, luma);
-            const T w_ggx = lerp(albedo_gloss, albedo_metal, base_metalness);
-            const T w_diffuse = (T(1) - base_metalness) * albedo_diffuse;
-            b.p_ggx = clamp(w_ggx / M<T>::fmax(w_ggx + w_diffuse, K(1e-7)), K(0.1), K(0.9));
-            b.p_diffuse = T(1) - b.p_ggx;
-            b.p_u = M<T>::pow(r, K(0.1)) * (K(0.162925) + (K(-0.372058) + (K(0.538233) - K(0.290822) * z) * z) * z);
-            b.p_c = T(1) - b.p_u;
-            b.base_color = base_color;
-            b.base_weight = base_weight;
-            b.base_metalness = base_metalness;
-            b.base_diffuse_roughness = base_diffuse_roughness;
-            b.specular_color = specular_color;
-            b.specular_weight = specular_weight;
+            const Bsdf b = setup_bsdf(base_color, base_weight, base_metalness, base_diffuse_roughness, specular_color,
+                                      specular_weight, specular_roughness, specular_anisotropy, specular_ior, wo);
 
             // next-event estimation, trace.slang:1187-1206
             const V3<T> next_origin = hit_point + flat_n * M<T>::fmax(K(1e-4), K(1e-4) * length(hit_point));
@@ -845,26 +886,7 @@ struct Tracer {
             if (bounce == max_bounces) break;
 
             // BSDF sampling, trace.slang:1212-1260
-            const T two_pi_r = T(2.0f * kPi) * rand();
-            const T r1 = rand();
-            V3<T> wi;
-            if (rand() < b.p_ggx) {
-                wi = reflect(-wo, sample_vndf(wo, b.alpha, r1, two_pi_r));
-            } else if (r1 < b.p_u) {
-                const T u1 = r1 / b.p_u;
-                const T sin_theta = M<T>::sqrt(T(1) - u1 * u1);
-                wi = {sin_theta * M<T>::cos(two_pi_r), sin_theta * M<T>::sin(two_pi_r), u1};
-            } else {
-                const T u1 = (r1 - b.p_u) / b.p_c;
-                const T a = b.ltc.x, bb = b.ltc.y, c = b.ltc.z, dd = b.ltc.w;
-                const T R = M<T>::sqrt(u1);
-                const T y = R * M<T>::sin(two_pi_r);
-                const T s = M<T>::fma(K(0.5), rsqrt(M<T>::fma(dd, dd, T(1))), K(0.5));
-                const T x = -lerp(M<T>::sqrt(M<T>::fma(-y, y, T(1))), R * M<T>::cos(two_pi_r), s);
-                const V3<T> wh{x, y, M<T>::sqrt(M<T>::fmax(T(1) - (x * x + y * y), T(0)))};
-                const V3<T> wu{a * wh.x + bb * wh.z, c * wh.y, dd * wh.x + wh.z};
-                wi = normalize(wu.x * b.bx + wu.y * b.by + wu.z * b.bz);
-            }
+            const V3<T> wi = sample_bsdf(wo, b);
             if (wi.z <= T(0)) break;
             const Lobes lobes = evaluate_lobes(wo, wi, b);
             if (lobes.pdf <= T(0)) break;
@@ -887,6 +909,56 @@ void init_record(pt_path_record* r) {
     std::memset(r, 0, sizeof(*r));
     r->visit_hash = kFnvBasis;
     for (int i = 0; i < PT_RECORD_MAX_BOUNCES; ++i) r->hit[i] = -2;
+}
+
+// one shading point per case: setup (32 draws), the lobes at case.wi, and a
+// BSDF sample (the next 3 draws) with its lobes
+template <class T>
+void shade_case(const oracle_shade_case& k, oracle_shade_result* r) {
+    oracle_world dummy{};
+    Tracer<T> t(dummy);
+    t.rng = k.rng;
+    auto v = [](const float* p) { return V3<T>{T(p[0]), T(p[1]), T(p[2])}; };
+    const V3<T> wo = v(k.wo);
+    const typename Tracer<T>::Bsdf b =
+        t.setup_bsdf(v(k.base_color), T(k.base_weight), T(k.base_metalness), T(k.base_diffuse_roughness),
+                     v(k.specular_color), T(k.specular_weight), T(k.specular_roughness), T(k.specular_anisotropy),
+                     T(k.specular_ior), wo);
+    const auto lobes = Tracer<T>::evaluate_lobes(wo, v(k.wi), b);
+    const V3<T> ws = t.sample_bsdf(wo, b);
+    const auto slobes = Tracer<T>::evaluate_lobes(wo, ws, b);
+    const T ed[3] = {b.e_dielectric.x, b.e_dielectric.y, b.e_dielectric.z};
+    const T f[3] = {lobes.f.x, lobes.f.y, lobes.f.z};
+    const T sw[3] = {ws.x, ws.y, ws.z};
+    const T sf[3] = {slobes.f.x, slobes.f.y, slobes.f.z};
+    for (int j = 0; j < 3; ++j) {
+        r->e_dielectric[j] = (double)ed[j];
+        r->f[j] = (double)f[j];
+        r->sampled_wi[j] = (double)sw[j];
+        r->sampled_f[j] = (double)sf[j];
+    }
+    r->p_ggx = (double)b.p_ggx;
+    r->p_u = (double)b.p_u;
+    r->pdf = (double)lobes.pdf;
+    r->sampled_pdf = (double)slobes.pdf;
+    r->rng_after = t.rng;
+}
+
+template <class T>
+void light_case(const oracle_world& w, const float* origin, uint32_t rng, oracle_light_result* r) {
+    Tracer<T> t(w);
+    t.rng = rng;
+    const auto s = t.sample_light(V3<T>{T(origin[0]), T(origin[1]), T(origin[2])});
+    const T d[3] = {s.direction.x, s.direction.y, s.direction.z};
+    const T e[3] = {s.emission.x, s.emission.y, s.emission.z};
+    for (int j = 0; j < 3; ++j) {
+        r->direction[j] = (double)d[j];
+        r->emission[j] = (double)e[j];
+    }
+    r->distance = (double)s.distance;
+    r->pdf = (double)s.pdf;
+    r->triangle_index = s.triangle_index;
+    r->rng_after = t.rng;
 }
 
 }  // namespace
@@ -978,6 +1050,85 @@ int oracle_intersect(const oracle_world* world, uint64_t n, const float* origins
         hit[i] = h;
         hit_t[i] = ht;
         if (records) records[i] = local;
+    }
+    return 0;
+}
+
+// elementary operations of the parity mode, for the semantic pin tests
+int oracle_elementary(int op, uint64_t n, const float* a, const float* b, const float* c, float* out) {
+    if (!a || !out) return -1;
+    using F = float;
+    auto v3 = [](const float* p, uint64_t i) { return V3<F>{p[3 * i], p[3 * i + 1], p[3 * i + 2]}; };
+    auto put3 = [&](uint64_t i, V3<F> v) {
+        out[3 * i] = v.x;
+        out[3 * i + 1] = v.y;
+        out[3 * i + 2] = v.z;
+    };
+    for (uint64_t i = 0; i < n; ++i) {
+        switch (op) {
+            case ORACLE_OP_NORMALIZE: put3(i, normalize(v3(a, i))); break;
+            case ORACLE_OP_DOT: out[i] = dot(v3(a, i), v3(b, i)); break;
+            case ORACLE_OP_MIX: out[i] = lerp(a[i], b[i], c[i]); break;
+            case ORACLE_OP_REFLECT: put3(i, reflect(v3(a, i), v3(b, i))); break;
+            case ORACLE_OP_FRACT: out[i] = frac(a[i]); break;
+            case ORACLE_OP_MIN: out[i] = M<F>::fmin(a[i], b[i]); break;
+            case ORACLE_OP_MAX: out[i] = M<F>::fmax(a[i], b[i]); break;
+            case ORACLE_OP_CLAMP: out[i] = clamp(a[i], b[i], c[i]); break;
+            case ORACLE_OP_RSQRT: out[i] = rsqrt(a[i]); break;
+            case ORACLE_OP_TO_U32: {
+                const uint32_t u = to_u32(a[i]);
+                std::memcpy(&out[i], &u, 4);
+                break;
+            }
+            case ORACLE_OP_SRGB: out[i] = kSrgb.v[(uint8_t)a[i]]; break;
+            case ORACLE_OP_SLAB: {  // a: node min xyz, max xyz (6); b: origin xyz, direction xyz (6); c: hit_t
+                pt_bvh_node node{};
+                for (int k = 0; k < 3; ++k) {
+                    node.aabb_min[k] = a[6 * i + k];
+                    node.aabb_max[k] = a[6 * i + 3 + k];
+                }
+                const V3<F> o{b[6 * i], b[6 * i + 1], b[6 * i + 2]}, d{b[6 * i + 3], b[6 * i + 4], b[6 * i + 5]};
+                const V3<F> rcp = F(1) / d;
+                out[i] = Tracer<F>::intersect_aabb(node, -o * rcp, rcp, c[i]);
+                break;
+            }
+            case ORACLE_OP_CAMERA_RAY: {  // a = camera (16 floats); b = px, py, width, height; c = RNG state bits
+                pt_camera cam;
+                std::memcpy(&cam, a + 16 * i, sizeof cam);
+                uint32_t st;
+                std::memcpy(&st, c + i, 4);
+                oracle_world dummy{};
+                Tracer<F> t(dummy);
+                t.rng = st;
+                const uint32_t img[2] = {(uint32_t)b[4 * i + 2], (uint32_t)b[4 * i + 3]};
+                V3<F> o, d;
+                t.camera_ray(cam, (uint32_t)b[4 * i], (uint32_t)b[4 * i + 1], img, &o, &d);
+                put3(i, d);
+                break;
+            }
+            default: return -1;
+        }
+    }
+    return 0;
+}
+
+int oracle_shade_cases(int precision, const oracle_shade_case* cases, uint64_t n, oracle_shade_result* out) {
+    if (!cases || !out || (precision != 32 && precision != 64)) return -1;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        if (precision == 32) shade_case<float>(cases[i], &out[i]);
+        else shade_case<double>(cases[i], &out[i]);
+    }
+    return 0;
+}
+
+int oracle_sample_lights(const oracle_world* world, int precision, uint64_t n, const float* origins,
+                         const uint32_t* rng_states, oracle_light_result* out) {
+    if (!world || !origins || !rng_states || !out || (precision != 32 && precision != 64)) return -1;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        if (precision == 32) light_case<float>(*world, origins + 3 * i, rng_states[i], &out[i]);
+        else light_case<double>(*world, origins + 3 * i, rng_states[i], &out[i]);
     }
     return 0;
 }

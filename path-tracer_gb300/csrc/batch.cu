@@ -18,6 +18,7 @@
 #include <mutex>
 #include <string>
 #include <utility>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -405,6 +406,7 @@ struct StreamBuf {
 
 struct Scene {
     uint64_t id = 0;
+    uint64_t check = 0;  // second content hash (see hash_buffers)
     uint32_t slot = 0;
     uint64_t bytes = 0;
     bool any_alpha = false;
@@ -449,22 +451,85 @@ int hbm_fail(std::string& err, const char* what, uint64_t need, uint64_t used, u
     return PT_ERR_OOM;
 }
 
-// content hash of a scene: 64-bit multiply-xorshift over every buffer, 8 bytes at a time
-uint64_t hash_bytes(uint64_t h, const void* data, size_t n) {
-    const unsigned char* p = static_cast<const unsigned char*>(data);
+// Content identity of a scene: two independent 64-bit hashes over every
+// uploaded byte.  The first names the scene in the cache; a cache hit also
+// needs the second to match, so two different uploads share a cache entry
+// only if both hashes collide at once.
+struct Digest {
+    uint64_t a = 0x5EED5EEDull, b = 0x243F6A8885A308D3ull;
+};
+
+inline uint64_t rotl64(uint64_t x, int r) { return (x << r) | (x >> (64 - r)); }
+
+// both hashes of one byte range: a multiply-xorshift chain and an
+// add-multiply-rotate chain with different constants
+Digest hash_range(const unsigned char* p, size_t n) {
+    Digest d;
     size_t i = 0;
     for (; i + 8 <= n; i += 8) {
         uint64_t w;
         memcpy(&w, p + i, 8);
-        h ^= w;
-        h *= 0x9E3779B97F4A7C15ull;
-        h ^= h >> 29;
+        d.a ^= w;
+        d.a *= 0x9E3779B97F4A7C15ull;
+        d.a ^= d.a >> 29;
+        d.b = rotl64(d.b + w * 0xC2B2AE3D27D4EB4Full, 31) * 0x165667B19E3779F9ull;
     }
     for (; i < n; ++i) {
-        h ^= p[i];
-        h *= 0x100000001B3ull;
+        d.a ^= p[i];
+        d.a *= 0x100000001B3ull;
+        d.b = rotl64(d.b + p[i] * 0x27D4EB2F165667C5ull, 23) * 0x9E3779B185EBCA87ull;
     }
-    return h ^ (uint64_t)n;
+    d.a ^= (uint64_t)n;
+    d.b ^= rotl64((uint64_t)n, 17);
+    return d;
+}
+
+// Digest of a sequence of buffers: each is cut into 8 MiB chunks hashed in
+// parallel on up to 16 host threads, and the chunk digests are folded in
+// order together with each buffer's length, so the result depends on every
+// byte, the order of the buffers and their boundaries.
+Digest hash_buffers(const std::vector<std::pair<const void*, size_t>>& bufs) {
+    constexpr size_t kChunk = 8u << 20;
+    struct Piece {
+        const unsigned char* p;
+        size_t n;
+        size_t buffer;
+    };
+    std::vector<Piece> pieces;
+    for (size_t k = 0; k < bufs.size(); ++k) {
+        const unsigned char* p = static_cast<const unsigned char*>(bufs[k].first);
+        const size_t n = bufs[k].second;
+        if (n == 0) pieces.push_back({p, 0, k});
+        for (size_t o = 0; o < n; o += kChunk) pieces.push_back({p + o, n - o < kChunk ? n - o : kChunk, k});
+    }
+    std::vector<Digest> parts(pieces.size());
+    std::atomic<size_t> next{0};
+    const auto worker = [&]() {
+        for (size_t i; (i = next.fetch_add(1)) < pieces.size();) parts[i] = hash_range(pieces[i].p, pieces[i].n);
+    };
+    const unsigned hw = std::thread::hardware_concurrency();
+    const size_t threads = std::min<size_t>(pieces.size(), std::max(1u, std::min(hw, 16u)));
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < threads; ++t) {
+        try {
+            pool.emplace_back(worker);
+        } catch (const std::system_error&) {
+            break;  // the calling thread takes the remaining chunks
+        }
+    }
+    worker();
+    for (auto& th : pool) th.join();
+    Digest d;
+    for (size_t i = 0; i < pieces.size(); ++i) {
+        d.a = (d.a ^ parts[i].a ^ (pieces[i].buffer << 48)) * 0x9E3779B97F4A7C15ull;
+        d.a ^= d.a >> 31;
+        d.b = rotl64(d.b + parts[i].b + pieces[i].buffer, 27) * 0xC2B2AE3D27D4EB4Full;
+    }
+    for (const auto& b : bufs) {
+        d.a = (d.a ^ (uint64_t)b.second) * 0xFF51AFD7ED558CCDull;
+        d.b = rotl64(d.b ^ (uint64_t)b.second, 13) * 0xC4CEB9FE1A85EC53ull;
+    }
+    return d;
 }
 
 }  // namespace ptb
@@ -1031,7 +1096,13 @@ int pte_create(const pt_engine_config* cfg, pt_engine** out) {
         pte_destroy(e);
         return rc;
     }
-    e->pumper = std::thread(pump_loop, e);
+    try {
+        e->pumper = std::thread(pump_loop, e);
+    } catch (const std::system_error&) {
+        fprintf(stderr, "pte_create: the engine's background thread could not be started\n");
+        pte_destroy(e);
+        return PT_ERR_STATE;
+    }
     *out = e;
     return PT_OK;
 }
@@ -1117,29 +1188,34 @@ int pte_scene_add(pt_engine* e, const pt_world_updates* u, uint64_t* scene_id) {
     for (uint64_t i = 0; i < sk->alias_count; ++i)
         if (sk->alias_table[i].alias_index >= sk->alias_count)
             return e->fail(PT_ERR_INVALID_ARG, "skybox alias index out of range");
-    // content hash
+    // content identity
     const size_t layer = (size_t)PT_ATLAS_SIZE * PT_ATLAS_SIZE * 4;
-    uint64_t h = 0x5EED5EEDull;
-    h = hash_bytes(h, sc->geometries, sc->triangle_count * 36);
-    h = hash_bytes(h, sc->attributes, sc->triangle_count * 112);
-    h = hash_bytes(h, sc->materials, sc->material_count * 224);
-    h = hash_bytes(h, sc->bvh_nodes, sc->node_count * 32);
-    if (sc->srgb_atlas_count) h = hash_bytes(h, sc->srgb_texture_atlases, sc->srgb_atlas_count * layer);
-    if (sc->linear_atlas_count) h = hash_bytes(h, sc->linear_texture_atlases, sc->linear_atlas_count * layer);
-    h = hash_bytes(h, sk->rgba, (size_t)sk->uniforms.width * sk->uniforms.height * 16);
-    if (sk->alias_count) h = hash_bytes(h, sk->alias_table, sk->alias_count * 12);
-    if (u->scene_alias_count) h = hash_bytes(h, u->scene_alias_table, u->scene_alias_count * 16);
-    h = hash_bytes(h, u->scene_uniforms, 16);
-    h = hash_bytes(h, u->skybox_uniforms, 16);
-    if (h == 0) h = 1;
+    const Digest dg = hash_buffers({
+        {sc->geometries, sc->triangle_count * 36},
+        {sc->attributes, sc->triangle_count * 112},
+        {sc->materials, sc->material_count * 224},
+        {sc->bvh_nodes, sc->node_count * 32},
+        {sc->srgb_texture_atlases, sc->srgb_atlas_count * layer},
+        {sc->linear_texture_atlases, sc->linear_atlas_count * layer},
+        {sk->rgba, (size_t)sk->uniforms.width * sk->uniforms.height * 16},
+        {sk->alias_table, sk->alias_count * 12},
+        {u->scene_alias_table, u->scene_alias_count * 16},
+        {u->scene_uniforms, 16},
+        {u->skybox_uniforms, 16},
+    });
     e->use_clock += 1;
-    auto it = e->scenes.find(h);
-    if (it != e->scenes.end()) {
-        it->second->caller_refs += 1;
-        it->second->last_use = e->use_clock;
-        e->stats.scene_hits += 1;
-        *scene_id = h;
-        return PT_OK;
+    // the first hash names the scene; an entry whose second hash differs is a
+    // different scene, so probe on to the next free name (ids are never 0)
+    uint64_t h = dg.a ? dg.a : 1;
+    for (auto it = e->scenes.find(h); it != e->scenes.end(); it = e->scenes.find(h)) {
+        if (it->second->check == dg.b) {
+            it->second->caller_refs += 1;
+            it->second->last_use = e->use_clock;
+            e->stats.scene_hits += 1;
+            *scene_id = h;
+            return PT_OK;
+        }
+        h = h + 1 ? h + 1 : 1;
     }
     bool any_alpha = false;
     for (uint64_t i = 0; i < sc->material_count; ++i) any_alpha |= sc->materials[i].alpha_mode != PT_ALPHA_MODE_OPAQUE;
@@ -1171,6 +1247,7 @@ int pte_scene_add(pt_engine* e, const pt_world_updates* u, uint64_t* scene_id) {
     }
     auto s = std::make_unique<Scene>();
     s->id = h;
+    s->check = dg.b;
     s->slot = slot;
     s->bytes = bytes;
     s->caller_refs = 1;

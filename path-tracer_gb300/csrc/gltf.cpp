@@ -26,6 +26,7 @@
 #include <memory>
 #include <set>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -690,7 +691,13 @@ struct Loader {
         };
         const size_t nt = std::min<size_t>(n, std::max(1u, std::min(std::thread::hardware_concurrency(), 16u)));
         std::vector<std::thread> pool;
-        for (size_t t = 1; t < nt; ++t) pool.emplace_back(worker);
+        for (size_t t = 1; t < nt; ++t) {
+            try {
+                pool.emplace_back(worker);
+            } catch (const std::system_error&) {
+                break;  // the calling thread's worker takes the remaining images
+            }
+        }
         worker();
         for (auto& t : pool) t.join();
         for (size_t i = 0; i < n; ++i)

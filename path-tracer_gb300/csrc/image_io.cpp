@@ -20,6 +20,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -761,7 +762,13 @@ bool read_exr(const std::vector<uint8_t>& d, std::vector<float>& rgba, uint32_t&
         for (int64_t k; !errors[(size_t)t] && (k = next.fetch_add(1)) < chunks;) errors[(size_t)t] = decode_chunk(k, raw);
     };
     std::vector<std::thread> pool;
-    for (int64_t t = 1; t < nthreads; ++t) pool.emplace_back(worker, t);
+    for (int64_t t = 1; t < nthreads; ++t) {
+        try {
+            pool.emplace_back(worker, t);
+        } catch (const std::system_error&) {
+            break;  // worker 0 takes the remaining chunks
+        }
+    }
     worker(0);
     for (auto& th : pool) th.join();
     for (const char* e : errors)

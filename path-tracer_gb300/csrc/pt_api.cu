@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -73,6 +74,7 @@ struct pt_ctx {
     // tile (bind group 0)
     DevBuf accum, image, display, records, totals;
     DevBuf comp;  // Kahan compensation (PT_PRECISION_KAHAN)
+    DevBuf fp64;  // FP64 reference render sums (pt_render_fp64)
     uint32_t tile_w = 0, tile_h = 0;
     pt_trace_parameters params{};
     int kernel = PT_KERNEL_WAVEFRONT;
@@ -232,8 +234,15 @@ bool materials_in_range(const pt_triangle_attribute* attrs, uint64_t n, uint64_t
     if (threads == 1) return scan(0, n);
     std::vector<std::thread> pool;
     std::vector<char> ok(threads, 1);
-    for (unsigned t = 0; t < threads; ++t)
-        pool.emplace_back([&, t] { ok[t] = scan(n * t / threads, n * (t + 1) / threads); });
+    unsigned started = 1;  // range 0 runs on the calling thread, with any range a refused thread leaves
+    for (; started < threads; ++started) {
+        try {
+            pool.emplace_back([&, t = started] { ok[t] = scan(n * t / threads, n * (t + 1) / threads); });
+        } catch (const std::system_error&) {
+            break;
+        }
+    }
+    ok[0] = scan(0, n / threads) && scan(n * started / threads, n);
     for (auto& th : pool) th.join();
     for (char v : ok)
         if (!v) return false;
@@ -544,7 +553,7 @@ void pt_destroy(pt_ctx* c) {
     for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
     if (c->wavefront) ptw::destroy(c->wavefront);
     for (DevBuf* b : {&c->geo, &c->attr, &c->mat, &c->nodes, &c->srgb, &c->linear, &c->sky, &c->sky_alias,
-                      &c->scene_alias, &c->srgb_lut, &c->accum, &c->image, &c->comp, &c->display, &c->records, &c->totals,
+                      &c->scene_alias, &c->srgb_lut, &c->accum, &c->image, &c->comp, &c->fp64, &c->display, &c->records, &c->totals,
                       &c->stage_geo, &c->stage_attr, &c->stage_mat, &c->stage_nodes, &c->stage_srgb, &c->stage_linear})
         b->release();
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -713,6 +722,24 @@ int pt_reset_kernel_times(pt_ctx* c) {
 }
 
 uint64_t pt_launch_count(const pt_ctx* c) { return c ? c->launch_count : 0; }
+
+int pt_render_fp64(pt_ctx* c, uint32_t sample_first, uint32_t sample_count, double* host_rgb_sums) {
+    if (!c || !host_rgb_sums) return PT_ERR_INVALID_ARG;
+    if (sample_first == 0 || sample_count == 0 || sample_count - 1u > 0xffffffffu - sample_first)
+        return c->fail(PT_ERR_INVALID_ARG, "FP64 render needs a non-empty range of 1-based sample indices");
+    if (!c->world_ready) return c->fail(PT_ERR_STATE, "no world uploaded");
+    cudaSetDevice(c->device);
+    const size_t bytes = (size_t)c->tile_w * c->tile_h * 3 * sizeof(double);
+    int rc = c->cuda(c->fp64.reserve(bytes), "FP64 sums");
+    if (!rc) rc = c->cuda(cudaMemsetAsync(c->fp64.p, 0, bytes, c->stream), "FP64 sums");
+    const ptd::World w = c->view();
+    const ptk::Tile t = tile_of(c);
+    for (uint32_t s = 0; !rc && s < sample_count; ++s)
+        rc = c->cuda(ptk::launch_fp64(w, t, sample_first + s, c->fp64.as<double>(), c->stream), "FP64 render launch");
+    if (!rc) rc = c->cuda(cudaMemcpyAsync(host_rgb_sums, c->fp64.p, bytes, cudaMemcpyDeviceToHost, c->stream), "FP64 readback");
+    if (!rc) rc = c->cuda(cudaStreamSynchronize(c->stream), "FP64 render");
+    return rc;
+}
 
 int pt_debug_intersect(pt_ctx* c, uint64_t n, const float* origins, const float* directions, const float* t_max,
                        int32_t* hit, float* hit_t, pt_path_record* records) {

@@ -36,6 +36,10 @@ cudaError_t launch_debug_intersect(const ptd::World& w, uint64_t n, const float*
                                    const float* t_max, int32_t* hit, float* hit_t, pt_path_record* records,
                                    cudaStream_t stream);
 
+// FP64 reference render: one launch per sample (1-based index `sample`),
+// adds each visible tile pixel's radiance to sums[3 * (y * tile_w + x) ..]
+cudaError_t launch_fp64(const ptd::World& w, const Tile& t, uint32_t sample, double* sums, cudaStream_t stream);
+
 // display.wgsl:19-46 on the storage texture -> RGBA8
 cudaError_t launch_display(const float4* image, uint32_t count, uchar4* out, cudaStream_t stream);
 

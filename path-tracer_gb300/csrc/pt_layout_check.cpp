@@ -41,6 +41,29 @@ CHECK_SIZE(pt_skybox_uniforms, 16);
 CHECK_SIZE(pt_skybox_alias_entry, 12);
 CHECK_SIZE(pt_trace_parameters, 32);
 CHECK_SIZE(pt_path_record, 144);
+// the upload descriptors (64-bit pointers), mirrored by the Rust binding include/pt_ffi.rs
+CHECK_SIZE(pt_scene_upload, 88);
+CHECK_OFF(pt_scene_upload, srgb_atlas_count, 64);
+CHECK_OFF(pt_scene_upload, linear_atlas_count, 80);
+CHECK_SIZE(pt_skybox_upload, 40);
+CHECK_OFF(pt_skybox_upload, alias_table, 24);
+CHECK_SIZE(pt_material_update, 228);
+CHECK_OFF(pt_material_update, material, 4);
+CHECK_SIZE(pt_world_updates, 80);
+CHECK_OFF(pt_world_updates, material_update_count, 32);
+CHECK_OFF(pt_world_updates, skybox_uniforms, 64);
+CHECK_OFF(pt_world_updates, reset_accumulation, 72);
+// the caller-owned device world of pt_trace_noalloc (64-bit pointers)
+CHECK_SIZE(pt_device_world, 216);
+CHECK_OFF(pt_device_world, triangle_count, 16);
+CHECK_OFF(pt_device_world, bvh_nodes, 40);
+CHECK_OFF(pt_device_world, srgb_atlas_count, 64);
+CHECK_OFF(pt_device_world, linear_texture_atlases, 72);
+CHECK_OFF(pt_device_world, skybox_rgba, 88);
+CHECK_OFF(pt_device_world, camera, 112);
+CHECK_OFF(pt_device_world, scene_uniforms, 176);
+CHECK_OFF(pt_device_world, skybox_uniforms, 192);
+CHECK_OFF(pt_device_world, any_non_opaque, 208);
 // the batched engine's structs, mirrored by the Python binding
 CHECK_SIZE(pt_engine_config, 48);
 CHECK_OFF(pt_engine_config, hbm_budget_bytes, 8);

@@ -825,11 +825,12 @@ extern "C" int pt_trace_noalloc(const pt_device_world* world, const pt_trace_par
                                ? tile_width : params->image_size[0] - params->tile_origin[0];
     const uint32_t vis_h = tile_height < params->image_size[1] - params->tile_origin[1]
                                ? tile_height : params->image_size[1] - params->tile_origin[1];
-    const uint64_t pixels = (uint64_t)vis_w * vis_h;
-    if (pixels * samples > kNoAllocPaths) {
+    const uint64_t pixels = (uint64_t)vis_w * vis_h;  // >= 1: the origin lies inside the image
+    // two comparisons, so that no product can wrap before the check
+    if (pixels > kNoAllocPaths || samples > kNoAllocPaths / pixels) {
         char msg[200];
-        snprintf(msg, sizeof msg, "%llu paths (%u x %u visible pixels x %u samples) exceed the %u paths one call can hold",
-                 (unsigned long long)(pixels * samples), vis_w, vis_h, samples, PT_NOALLOC_MAX_PATHS);
+        snprintf(msg, sizeof msg, "%u x %u visible pixels x %u samples exceed the %u paths one call can hold",
+                 vis_w, vis_h, samples, PT_NOALLOC_MAX_PATHS);
         return noalloc_fail(error, error_size, PT_ERR_OUT_OF_LIMITS, msg);
     }
     if (samples == 0) return PT_OK;

@@ -14,6 +14,7 @@
 // bounds, a wide box test accepts every ray the binary node's test accepts.
 #include <cmath>
 #include <cstring>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -145,21 +146,30 @@ void order_by_octant(pt_wide_node& node) {
     }
 }
 
-// order_by_octant over all nodes, on up to 16 host threads (nodes are independent)
+// order_by_octant over all nodes, on up to 16 host threads (nodes are
+// independent).  A host that refuses a new thread gets the remaining ranges
+// done on the calling thread: no exception leaves the C ABI.
 void order_all_by_octant(std::vector<pt_wide_node>& wide) {
     const size_t count = wide.size();
     unsigned threads = std::thread::hardware_concurrency();
     threads = threads == 0 ? 1 : (threads > 16 ? 16 : threads);
     if (count < 4096) threads = 1;
     const size_t per = (count + threads - 1) / threads;
+    const auto range = [&wide](size_t lo, size_t hi) {
+        for (size_t k = lo; k < hi; ++k) order_by_octant(wide[k]);
+    };
     std::vector<std::thread> pool;
-    for (unsigned t = 0; t < threads; ++t) {
-        const size_t lo = t * per, hi = lo + per < count ? lo + per : count;
-        if (lo >= hi) break;
-        pool.emplace_back([&wide, lo, hi]() {
-            for (size_t k = lo; k < hi; ++k) order_by_octant(wide[k]);
-        });
+    size_t next = 0;  // first node no thread has taken
+    for (unsigned t = 1; t < threads && next + per < count; ++t) {
+        const size_t lo = next, hi = lo + per;
+        try {
+            pool.emplace_back(range, lo, hi);
+        } catch (const std::system_error&) {
+            break;
+        }
+        next = hi;
     }
+    range(next, count);
     for (auto& th : pool) th.join();
 }
 

@@ -437,6 +437,14 @@ class PathTracer:
             out[k] = out.get(k, 0) + int(v)
         return traced.value, out
 
+    def render_fp64(self, sample_first: int, sample_count: int) -> np.ndarray:
+        """FP64 reference render of the current tile (pt_render_fp64): per-pixel radiance sums over
+        samples sample_first .. sample_first + sample_count - 1, shape (tile_h, tile_w, 3) float64."""
+        tw, th = self.tile_size
+        out = np.zeros((th, tw, 3), dtype=np.float64)
+        self._check(self._lib.pt_render_fp64(self._h, sample_first, sample_count, out.ctypes.data))
+        return out
+
     def synchronize(self, timeout_ms: int = 0) -> None:
         self._check(self._lib.pt_synchronize(self._h, timeout_ms))
 

@@ -185,7 +185,7 @@ PT_NOALLOC_SCRATCH_BYTES = 48 << 20
 STRUCT_SIZES = {
     TriangleGeometry: 36, TriangleAttribute: 112, BvhNode: 32, Material: 224, Camera: 64,
     SceneUniforms: 16, SceneAliasEntry: 16, SkyboxUniforms: 16, SkyboxAliasEntry: 12,
-    TraceParameters: 32, PathRecord: 144, WideNode: 128, HalfAttribute: 64,
+    TraceParameters: 32, PathRecord: 144, WideNode: 128, HalfAttribute: 64, DeviceWorld: 216,
 }
 
 P = C.POINTER
@@ -223,6 +223,7 @@ SIGNATURES = {
     "pt_set_precision": (C.c_int, [_vp, c_u32]),
     "pt_precision": (c_u32, [_vp]),
     "pt_precision_active": (c_u32, [_vp]),
+    "pt_render_fp64": (C.c_int, [_vp, c_u32, c_u32, _vp]),
     # pt_world.h
     "ptw_create": (C.c_int, [P(_vp)]),
     "ptw_destroy": (None, [_vp]),

@@ -34,6 +34,10 @@ def test_field_offsets():
     assert abi.EngineConfig.shade_threads.offset == 44
     assert abi.JobDesc.continue_job.offset == 88
     assert abi.EngineStats.gpu_ms.offset == 80 and abi.EngineStats.shade_threads.offset == 116
+    dw = abi.DeviceWorld
+    assert (dw.triangle_count.offset, dw.bvh_nodes.offset, dw.srgb_atlas_count.offset) == (16, 40, 64)
+    assert (dw.linear_texture_atlases.offset, dw.skybox_rgba.offset, dw.camera.offset) == (72, 88, 112)
+    assert (dw.scene_uniforms.offset, dw.skybox_uniforms.offset, dw.any_non_opaque.offset) == (176, 192, 208)
 
 
 def test_library_exports_every_declared_symbol():

@@ -212,6 +212,28 @@ def test_scene_cache_budget_and_eviction(scenes):
     small.close()
 
 
+def test_scene_identity_is_content(scenes):
+    """The cache keys scenes by their bytes, not their host pointers: a copy of a scene is a hit, and one
+    changed texel of the sky (the last float of the last buffer hashed before the uniforms) is a new scene."""
+    eng = Engine(wave_paths=1 << 13, tile_size=16)
+    full = scenes.full["terrain"]
+    a = eng.add_scene(full)
+    k = full.skybox.contents
+    n = 4 * k.uniforms.width * k.uniforms.height
+    sky = np.ctypeslib.as_array(k.rgba, shape=(n,)).copy()
+    u = abi.WorldUpdates.from_buffer_copy(full)
+    up = abi.SkyboxUpload.from_buffer_copy(k)
+    up.rgba = sky.ctypes.data_as(C.POINTER(C.c_float))
+    u.skybox = C.pointer(up)
+    assert eng.add_scene(u) == a  # same bytes at another address
+    sky[n - 2] = np.nextafter(sky[n - 2], np.float32(np.inf))
+    b = eng.add_scene(u)
+    assert b != a
+    st = eng.stats()
+    assert st["scene_hits"] == 1 and st["scenes_cached"] == 2
+    eng.close()
+
+
 def test_poll_reports_each_job_once(scenes):
     eng = Engine(wave_paths=1 << 14, tile_size=16)
     sid = eng.add_scene(scenes.full["cornell"])
