@@ -77,6 +77,11 @@ def parse_args():
                    help="only the timed steps (no counting pass, e2e or CPU baseline): for ncu captures")
     p.add_argument("--no-latency", action="store_true",
                    help="skip the request-latency measurement (batched engine vs the plain path)")
+    p.add_argument("--no-mix", action="store_true",
+                   help="skip the batching / serving measurement on the mixed request stream")
+    p.add_argument("--no-fp64", action="store_true",
+                   help="skip the image error against the FP64 reference render")
+    p.add_argument("--mix-seconds", type=float, default=10.0, help="seconds of arrivals of the serving stream")
     p.add_argument("--image", type=int, nargs=2, metavar=("W", "H"), default=None,
                    help="image size (default 1920 1080); smaller sizes are for ncu captures, not bench lines")
     args = p.parse_args()
@@ -252,6 +257,77 @@ def latency_report(updates, precision: int, rate: float = 20.0, seconds: float =
     return {"workload": f"{size}x{size}, {spp} spp, max_bounces {depth}, Poisson {rate:g} req/s for {seconds:g} s "
                         f"on this scene (seed 3)",
             "engine_ms": percentiles(lat), "plain_ms": percentiles(plat)}
+
+
+MIX_SCENES = ["10k", "100k", "1M", "4M"]
+
+
+def mixed_stream_report(seconds: float = 10.0, rate: float = 50.0, jobs: int = 256) -> dict:
+    """The batching and serving workloads on one GPU, against the plain one-job-per-launch path.
+
+    Scenes: procedural, about 10k / 100k / 1M / 4M triangles (pathtracer/serving.py SCENE_SIZES).
+    * batching: `jobs` requests of the mix (sides log-uniform 64-1024, aspect 1:1-16:9, spp in
+      {1,4,16,64}, max_bounces 4-12, random camera poses) rendered back to back: samples/s through
+      the plain kernel (one pt_trace of <= 16 samples per call, the host waiting on each call:
+      the reference's dispatch shape, FP32), the wavefront kernels one job per call (FP32), and the
+      batched engine in the compressed form with the settings its autotuner chose
+      (pathtracer/engine_tuned.json).
+    * serving: Poisson arrivals at `rate` req/s for `seconds` s, 10 % progressive refinements, a
+      fifth of the requests 512x512 x 16 spp x max_bounces 8; latency from arrival to result
+      through the serving loop (continuous batching) on the same engine, overall and for the
+      512x512x16 requests inside the mix; the plain path's latencies for the same stream are
+      replayed from its measured per-request service times."""
+    from pathtracer.engine import Engine
+    from pathtracer.serving import (Server, build_scene, closed_loop, percentiles, replay_latencies,
+                                    request_stream)
+    t0 = time.perf_counter()
+    worlds = {n: build_scene(n) for n in MIX_SCENES}
+    build_s = time.perf_counter() - t0
+    eng = Engine.tuned(hbm_budget_bytes=150 << 30)
+    server = Server(eng, worlds)
+    reqs = request_stream(1000.0, jobs / 1000.0 * 2.0 + 1.0, MIX_SCENES, seed=4, progressive_fraction=0.0)[:jobs]
+    warm = [eng.submit(server.scene_ids[r.scene], server.camera(r.scene, r), r.width, r.height, r.samples,
+                       r.max_bounces) for r in reqs[:8]]  # graph capture, layouts
+    eng.wait_idle(timeout_ms=0)
+    eng.poll(timeout_ms=0)  # take the warm-up jobs' completion reports
+    for j in warm:
+        eng.release(j)
+    batch = {mode: closed_loop(server, reqs, mode) for mode in ("engine", "wavefront", "plain")}
+    samples = batch["plain"]["samples"]
+    stream = request_stream(rate, seconds, MIX_SCENES, seed=5, progressive_fraction=0.1, fixed=(512, 512, 16, 8),
+                            fixed_share=0.2)
+    g0 = eng.stats()["gpu_ms"]
+    res = server.run(stream)
+    busy = (eng.stats()["gpu_ms"] - g0) / 1e3 / res.wall_s
+    # the plain path on the same stream (refinements as fresh renders of their samples)
+    plain_all = closed_loop(server, stream, "plain")
+    plain_lat = replay_latencies(stream, plain_all["service_s"])
+    plain_fixed = [lat for r, lat in zip(stream, plain_lat) if (r.width, r.height, r.samples) == (512, 512, 16)]
+    eng.close()
+    rate_of = {m: batch[m]["samples_per_s"] for m in batch}
+    return {
+        "workload": f"{jobs} jobs of the mix on procedural scenes of "
+                    f"{', '.join(str(w.triangle_count()) for w in worlds.values())} triangles "
+                    f"({samples} samples); serving: Poisson {rate:g} req/s for {seconds:g} s, 10% progressive, "
+                    f"20% 512x512x16 spp depth 8",
+        "engine": eng_config_of(Engine.tuned_config()),
+        "batching_samples_per_s": rate_of,
+        "engine_over_plain": rate_of["engine"] / rate_of["plain"],
+        "wavefront_over_plain": rate_of["wavefront"] / rate_of["plain"],
+        "serving": {"requests": len(stream), "completed": res.completed, "rejected": res.rejected,
+                    "latency_ms": percentiles(res.latencies_ms),
+                    "latency_512x512x16_ms": percentiles(res.latencies_512_16_ms),
+                    "samples_per_s": res.paths / res.wall_s, "gpu_busy": busy,
+                    "plain_latency_ms": percentiles(plain_lat),
+                    "plain_latency_512x512x16_ms": percentiles(plain_fixed)},
+        "scene_build_s": build_s,
+    }
+
+
+def eng_config_of(cfg: dict) -> dict:
+    keep = ("wave_paths", "tile_size", "steps_per_refill", "sort_min_hits", "traversal_threads", "shade_threads",
+            "precision")
+    return {k: cfg[k] for k in keep if k in cfg}
 
 
 def pinned_updates(updates):
@@ -440,6 +516,18 @@ def run_ours(args):
                 "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs), of measured" if peaks else "fallback 6.8 TB/s"}
 
+    # image error of the step's image (its accumulation holds samples 1..spp)
+    # against the FP64 reference render of the same paths on the GPU
+    rmse = None
+    if rank == 0 and not args.no_fp64:
+        acc = tracer.read_tile(abi.PT_TILE_ACCUMULATION)[..., :3].astype(np.float64) / spp
+        t64 = time.perf_counter()
+        ref = tracer.render_fp64(1, spp) / spp
+        rmse = {"value": float(np.sqrt(np.mean((acc - ref) ** 2)) / np.sqrt(np.mean(ref ** 2))),
+                "definition": "sqrt(mean((img - fp64)^2)) / sqrt(mean(fp64^2)) over the whole image, per-pixel means",
+                "image": [WIDTH, HEIGHT], "spp": spp, "precision": args.precision,
+                "fp64_render_s": time.perf_counter() - t64}
+
     # end to end through the C ABI: world upload from pinned host memory, the
     # render, and the RGBA8 result read back, every step
     pinned, keep, h2d = pinned_updates(updates)
@@ -462,6 +550,10 @@ def run_ours(args):
     if rank == 0 and world_size == 1 and not args.no_latency:
         latency = latency_report(updates, PRECISIONS[args.precision])
 
+    mix = None
+    if rank == 0 and world_size == 1 and not args.no_mix and WORKLOAD == "procedural":
+        mix = mixed_stream_report(seconds=args.mix_seconds)
+
     cpu = None
     if rank == 0 and world_size == 1 and not args.no_cpu_baseline:
         v, threads, desc, _ = oracle_sample(updates, args.cpu_seconds)
@@ -483,6 +575,7 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": WIDTH * HEIGHT * 4},
             "gpu_launches": launches, "clocks": clocks.summary(), "latency": latency,
+            "rmse_vs_fp64": rmse, "mixed_stream": mix,
             "kernel_ms": {k: v for k, v in times.milliseconds.items() if times.launches[k]},
         }
         print(json.dumps(line), flush=True)

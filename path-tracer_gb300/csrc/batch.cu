@@ -436,6 +436,11 @@ struct Job {
     uint32_t samples = 0;
     int status = PT_JOB_QUEUED;
     uint64_t items_target = 0;  // cumulative item count of the slot at which this job is done
+    std::deque<ItemDev> pending;  // work items not yet handed to a wave
+    uint64_t pending_paths = 0;
+    uint32_t rounds = 0;  // bounce rounds its paths can take (max_bounces + 1)
+    bool alpha = false;   // its scene has non-opaque materials
+    std::chrono::steady_clock::time_point submitted;
 };
 
 struct Flight {
@@ -568,7 +573,8 @@ struct pt_engine {
     ptb::WaveBufs wb{};
     uint32_t max_items = 0;
     bool wave_ready = false;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};  // opaque, alpha
+    // one captured wave per kind (opaque / non-opaque) and number of bounce rounds
+    cudaGraphExec_t graph[2][kRounds] = {};
     std::deque<Flight> flights;
     std::vector<cudaEvent_t> event_pool;
     pt_engine_stats stats{};
@@ -607,11 +613,12 @@ uint64_t wave_bytes(uint32_t paths) {
 }
 
 void drop_graphs(pt_engine* e) {
-    for (auto& g : e->graph)
-        if (g) {
-            cudaGraphExecDestroy(g);
-            g = nullptr;
-        }
+    for (auto& kind : e->graph)
+        for (auto& g : kind)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
 }
 
 int setup_wave(pt_engine* e) {
@@ -677,7 +684,7 @@ void launch_persistent(void (*kernel)(P...), pt_engine* e, int threads, A&&... a
 
 // the launches of one wave (captured into a graph, or issued directly)
 template <bool kAlpha, bool kWideBvh>
-cudaError_t issue_wave(pt_engine* e) {
+cudaError_t issue_wave(pt_engine* e, uint32_t rounds) {
     const cudaStream_t s = e->stream;
     const ItemDev* ring = e->d_ring.as<const ItemDev>();
     Ctrl* ctrl = e->d_ctrl.as<Ctrl>();
@@ -706,7 +713,7 @@ cudaError_t issue_wave(pt_engine* e) {
         return launch_persistent(shadow_kernel<kWide, 128>, e, 128, scenes, e->wb, e->cfg.steps_per_refill);
     };
     int cur = 0;
-    for (uint32_t bounce = 0; bounce < kRounds; ++bounce) {
+    for (uint32_t bounce = 0; bounce < rounds; ++bounce) {
         reset_kernel<<<1, 1, 0, s>>>(e->wb.q.cnt, cur ^ 1);
         extend(cur);
         if (e->cfg.sort_min_hits != 0xffffffffu) {
@@ -728,23 +735,28 @@ cudaError_t issue_wave(pt_engine* e) {
     return cudaGetLastError();
 }
 
-cudaError_t issue_any_wave(pt_engine* e, bool alpha) {
+cudaError_t issue_any_wave(pt_engine* e, bool alpha, uint32_t rounds) {
     const bool wide = (e->cfg.precision & PT_PRECISION_WIDE_BVH) != 0;
-    if (alpha) return issue_wave<true, false>(e);
-    return wide ? issue_wave<false, true>(e) : issue_wave<false, false>(e);
+    if (alpha) return issue_wave<true, false>(e, rounds);
+    return wide ? issue_wave<false, true>(e, rounds) : issue_wave<false, false>(e, rounds);
 }
 
-int launch_wave(pt_engine* e, bool alpha) {
+// one wave of `rounds` bounce rounds (the deepest job of the wave needs
+// max_bounces + 1; a path never takes more, so shallower waves skip the
+// launches of rounds that would find empty queues)
+int launch_wave(pt_engine* e, bool alpha, uint32_t rounds) {
     const int gi = alpha ? 1 : 0;
-    if (e->cfg.use_graphs && !e->graph[gi]) {
+    if (rounds < 1 || rounds > kRounds) rounds = kRounds;
+    cudaGraphExec_t& exec = e->graph[gi][rounds - 1];
+    if (e->cfg.use_graphs && !exec) {
         cudaGraph_t g = nullptr;
         int rc = e->cuda(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
         if (rc) return rc;
-        const cudaError_t le = issue_any_wave(e, alpha);
+        const cudaError_t le = issue_any_wave(e, alpha, rounds);
         const cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
         if ((rc = e->cuda(le, "wave capture"))) return rc;
         if ((rc = e->cuda(ce, "graph capture"))) return rc;
-        rc = e->cuda(cudaGraphInstantiate(&e->graph[gi], g, 0), "graph instantiate");
+        rc = e->cuda(cudaGraphInstantiate(&exec, g, 0), "graph instantiate");
         cudaGraphDestroy(g);
         if (rc) return rc;
     }
@@ -752,22 +764,13 @@ int launch_wave(pt_engine* e, bool alpha) {
     cudaEventRecord(f.start, e->stream);
     int rc;
     if (e->cfg.use_graphs)
-        rc = e->cuda(cudaGraphLaunch(e->graph[gi], e->stream), "graph launch");
+        rc = e->cuda(cudaGraphLaunch(exec, e->stream), "graph launch");
     else
-        rc = e->cuda(issue_any_wave(e, alpha), "wave launch");
+        rc = e->cuda(issue_any_wave(e, alpha, rounds), "wave launch");
     if (rc) return rc;
     cudaEventRecord(f.stop, e->stream);
     e->flights.push_back(f);
     return PT_OK;
-}
-
-bool any_alpha_active(pt_engine* e) {
-    for (auto& [id, j] : e->jobs)
-        if (j.status != PT_JOB_DONE) {
-            auto it = e->scenes.find(j.acc->scene);
-            if (it != e->scenes.end() && it->second->any_alpha) return true;
-        }
-    return false;
 }
 
 // queue the work items of a job whose accumulation is free
@@ -789,8 +792,9 @@ int start_job(pt_engine* e, Job& j) {
     int rc = e->cuda(cudaMemcpyAsync(e->d_jobs.as<JobDev>() + a.slot, &jd, sizeof jd, cudaMemcpyHostToDevice, e->stream),
                      "job record");
     if (rc) return rc;
-    std::vector<ItemDev> items;
+    // the job's work items wait on the host until feed_wave hands them to a wave
     const uint32_t T = e->cfg.tile_size;
+    size_t count = 0;
     for (uint32_t y = 0; y < a.height; y += T)
         for (uint32_t x = 0; x < a.width; x += T) {
             ItemDev it;
@@ -802,28 +806,77 @@ int start_job(pt_engine* e, Job& j) {
             it.first_sample = a.samples_done + 1u;
             it.samples = j.samples;
             it.pad = 0;
-            items.push_back(it);
+            j.pending.push_back(it);
+            j.pending_paths += (uint64_t)it.w * it.h * it.samples;
+            ++count;
         }
-    if (e->tail + items.size() - e->head_seen > e->ring_cap)
-        return e->fail(PT_ERR_OUT_OF_LIMITS, "work ring full");
-    // copy into the ring (two pieces across the wrap)
+    j.rounds = a.max_bounces + 1u;
+    j.alpha = sc->any_alpha;
+    e->slot_items[a.slot] += count;
+    j.items_target = e->slot_items[a.slot];
+    e->stats.items += count;
+    return PT_OK;
+}
+
+// Scheduling weight of a job's pending work: its remaining paths, shrunk as
+// it waits (halved after kAgeMs), so short jobs go first (shortest remaining
+// work first) and a long job's wait stays bounded.
+constexpr double kAgeMs = 50.0;
+double feed_key(const Job& j, std::chrono::steady_clock::time_point now) {
+    const double age_ms = std::chrono::duration<double, std::milli>(now - j.submitted).count();
+    return (double)j.pending_paths / (1.0 + age_ms / kAgeMs);
+}
+
+// Hands the next wave its work items: jobs in feed_key order, each giving
+// its pending items in tile order while they fit the wave's path budget and
+// item limit.  Writes them to the ring and the ring's tail, so the wave's
+// planner (which takes every item up to the budget) consumes exactly these.
+// Returns the number of items fed; *alpha and *rounds describe the wave.
+int feed_wave(pt_engine* e, size_t* fed, bool* alpha, uint32_t* rounds) {
+    *fed = 0;
+    *alpha = false;
+    *rounds = 1;
+    const auto now = std::chrono::steady_clock::now();
+    std::vector<std::pair<double, Job*>> order;
+    for (auto& [id, j] : e->jobs)
+        if (!j.pending.empty()) order.emplace_back(feed_key(j, now), &j);
+    if (order.empty()) return PT_OK;
+    std::stable_sort(order.begin(), order.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+    std::vector<ItemDev> wave;
+    uint64_t paths = 0;
+    const uint64_t budget = e->cfg.wave_paths;
+    for (auto& [key, j] : order) {
+        while (!j->pending.empty() && wave.size() < e->max_items) {
+            const ItemDev& it = j->pending.front();
+            const uint64_t np = (uint64_t)it.w * it.h * it.samples;
+            if (!wave.empty() && paths + np > budget) break;
+            wave.push_back(it);
+            paths += np;
+            j->pending_paths -= np;
+            j->pending.pop_front();
+            *alpha |= j->alpha;
+            *rounds = std::max(*rounds, j->rounds);
+        }
+        if (paths >= budget || wave.size() >= e->max_items) break;
+    }
+    if (e->tail + wave.size() - e->head_seen > e->ring_cap) return e->fail(PT_ERR_OUT_OF_LIMITS, "work ring full");
+    // copy into the ring (two pieces across the wrap); the copies read
+    // pageable host memory, so they have taken it before they return
     size_t done = 0;
-    while (done < items.size()) {
+    while (done < wave.size()) {
         const uint64_t pos = (e->tail + done) % e->ring_cap;
-        const size_t n = std::min<size_t>(items.size() - done, e->ring_cap - pos);
-        rc = e->cuda(cudaMemcpyAsync(e->d_ring.as<ItemDev>() + pos, items.data() + done, n * sizeof(ItemDev),
-                                     cudaMemcpyHostToDevice, e->stream), "ring write");
+        const size_t n = std::min<size_t>(wave.size() - done, e->ring_cap - pos);
+        int rc = e->cuda(cudaMemcpyAsync(e->d_ring.as<ItemDev>() + pos, wave.data() + done, n * sizeof(ItemDev),
+                                         cudaMemcpyHostToDevice, e->stream), "ring write");
         if (rc) return rc;
         done += n;
     }
-    e->tail += items.size();
+    e->tail += wave.size();
     const unsigned long long t = e->tail;
-    rc = e->cuda(cudaMemcpyAsync(&e->d_ctrl.as<Ctrl>()->tail, &t, sizeof t, cudaMemcpyHostToDevice, e->stream), "ring tail");
+    int rc = e->cuda(cudaMemcpyAsync(&e->d_ctrl.as<Ctrl>()->tail, &t, sizeof t, cudaMemcpyHostToDevice, e->stream),
+                     "ring tail");
     if (rc) return rc;
-    // the copies above read pageable host memory, so they complete before returning
-    e->slot_items[a.slot] += items.size();
-    j.items_target = e->slot_items[a.slot];
-    e->stats.items += items.size();
+    *fed = wave.size();
     return PT_OK;
 }
 
@@ -880,15 +933,18 @@ int harvest(pt_engine* e, bool block) {
     return PT_OK;
 }
 
-bool work_pending(pt_engine* e) { return e->tail > e->head_seen; }
-
+// keeps two waves queued on the stream while jobs have pending items; each
+// wave's items are chosen when it is queued, so a newly submitted job waits
+// at most for the two waves already queued
 int pump(pt_engine* e) {
-    while (e->flights.size() < 2 && work_pending(e)) {
-        // waves already in flight may consume the remaining items; one extra
-        // empty wave costs only its launches
-        if (e->flights.size() >= 1 && e->tail <= e->head_seen) break;
-        const int rc = launch_wave(e, any_alpha_active(e));
+    while (e->flights.size() < 2) {
+        size_t fed = 0;
+        bool alpha = false;
+        uint32_t rounds = 1;
+        int rc = feed_wave(e, &fed, &alpha, &rounds);
         if (rc) return rc;
+        if (fed == 0) break;
+        if ((rc = launch_wave(e, alpha, rounds))) return rc;
     }
     return PT_OK;
 }
@@ -1283,6 +1339,7 @@ int pte_submit(pt_engine* e, const pt_job_desc* d, uint64_t* job_id) {
     Job j;
     j.camera = d->camera;
     j.samples = d->samples;
+    j.submitted = std::chrono::steady_clock::now();
     if (d->continue_job) {
         auto it = e->jobs.find(d->continue_job);
         if (it == e->jobs.end() || !it->second.acc) return e->fail(PT_ERR_INVALID_ARG, "unknown job to continue");

@@ -594,6 +594,29 @@ PTD float bound_v(uint32_t w0, uint32_t w1) {
     return __uint_as_float(__byte_perm(i < 4 ? w0 : w1, 0x3F800000u, 0x7604u | ((unsigned)(i & 3) << 4)));
 }
 
+// 1: the 8-wide child test evaluates a child's near and far slab distance
+// on one axis with one packed FP32 fma (fma.rn.f32x2, sm_100 and later: each
+// half rounds as one fma.rn, so the distances are the same bits); 0: one fma
+// per distance
+#ifndef PT_WIDE_FMA2
+#define PT_WIDE_FMA2 1
+#endif
+PTD unsigned long long pack2(float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+PTD float2 unpack2(unsigned long long v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+PTD unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
 template <bool kShadow, bool kTri36 = false>
 struct WideTraverser {
     f3 o, d, rcp, nod;
@@ -655,6 +678,38 @@ struct WideTraverser {
         const AxisFrame Z = axis_frame(h0.z, (meta >> 16) & 0xffu, rcp.z, nod.z, __float_as_uint(h2.x),
                                        __float_as_uint(h2.y), __float_as_uint(h3.z), __float_as_uint(h3.w));
         uint32_t mask = 0u;
+#if PT_WIDE_FMA2
+        // the accept test of one child from its six slab distances
+        const auto accept = [&](int i, float nx, float ny, float nz, float fx, float fy, float fz) {
+#if PT_WIDE_MINMAX3
+            const float t_near = max3f(nx, ny, fmaxf(nz, 0.0f));
+            const float t_far = min3f(fx, fy, fminf(fz, hit_t));
+#else
+            const float t_near = fmaxf(fmaxf(nx, ny), fmaxf(nz, 0.0f));
+            const float t_far = fminf(fminf(fx, fy), fminf(fz, hit_t));
+#endif
+            if (t_near <= t_far) mask |= 1u << i;
+        };
+        // per axis (a15, a15) and (c_near, c_far): one packed fma gives a child's near and far distance
+        const unsigned long long xa = pack2(X.a15, X.a15), xc = pack2(X.c_near, X.c_far);
+        const unsigned long long ya = pack2(Y.a15, Y.a15), yc = pack2(Y.c_near, Y.c_far);
+        const unsigned long long za = pack2(Z.a15, Z.a15), zc = pack2(Z.c_near, Z.c_far);
+        const auto child = [&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            const float2 x = unpack2(fma2(pack2(bound_v<i>(X.near0, X.near1), bound_v<i>(X.far0, X.far1)), xa, xc));
+            const float2 y = unpack2(fma2(pack2(bound_v<i>(Y.near0, Y.near1), bound_v<i>(Y.far0, Y.far1)), ya, yc));
+            const float2 z = unpack2(fma2(pack2(bound_v<i>(Z.near0, Z.near1), bound_v<i>(Z.far0, Z.far1)), za, zc));
+            accept(i, x.x, y.x, z.x, x.y, y.y, z.y);
+        };
+        child(std::integral_constant<int, 0>());
+        child(std::integral_constant<int, 1>());
+        child(std::integral_constant<int, 2>());
+        child(std::integral_constant<int, 3>());
+        child(std::integral_constant<int, 4>());
+        child(std::integral_constant<int, 5>());
+        child(std::integral_constant<int, 6>());
+        child(std::integral_constant<int, 7>());
+#else
         const auto child = [&](auto ic) {
             constexpr int i = decltype(ic)::value;
             const float nx = fmaf(bound_v<i>(X.near0, X.near1), X.a15, X.c_near);
@@ -684,7 +739,8 @@ struct WideTraverser {
         child(std::integral_constant<int, 5>());
         child(std::integral_constant<int, 6>());
         child(std::integral_constant<int, 7>());
-#if PT_WIDE_MASK_PERMUTE
+#endif
+#if PT_WIDE_MASK_PERMUTE || PT_WIDE_FMA2
         // slot order -> octant order: bit i moves to bit i ^ oct
         mask &= (1u << count) - 1u;
         if (oct & 1u) mask = ((mask & 0x55u) << 1) | ((mask >> 1) & 0x55u);

@@ -2,6 +2,8 @@
 from __future__ import annotations
 
 import ctypes as C
+import json
+from pathlib import Path
 
 import numpy as np
 
@@ -9,8 +11,26 @@ from . import PathTracerError, abi
 from .abi import load
 
 
+TUNED = Path(__file__).resolve().parent / "engine_tuned.json"
+
+
 class Engine:
     """Many render jobs of uneven size, samples, depth and scene traced together on one GPU."""
+
+    @staticmethod
+    def tuned_config() -> dict:
+        """The engine settings pte_autotune chose for the compressed form on the batching mix
+        (engine_tuned.json, written by `python -m pathtracer.serving --compare 256 --scenes
+        10k,100k,1M,4M --precision compressed --autotune --save-tuned`)."""
+        return json.loads(TUNED.read_text())["config"]
+
+    @classmethod
+    def tuned(cls, device: int = 0, hbm_budget_bytes: int = 0) -> "Engine":
+        cfg = cls.tuned_config()
+        return cls(device=device, hbm_budget_bytes=hbm_budget_bytes, wave_paths=cfg["wave_paths"],
+                   tile_size=cfg["tile_size"], steps_per_refill=cfg["steps_per_refill"], use_graphs=True,
+                   precision=cfg["precision"], sort_min_hits=cfg["sort_min_hits"],
+                   traversal_threads=cfg["traversal_threads"], shade_threads=cfg["shade_threads"])
 
     def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, wave_paths: int = 0, tile_size: int = 0,
                  steps_per_refill: int = 0, use_graphs: bool = True, precision: int = 0, sort_min_hits: int = 0,

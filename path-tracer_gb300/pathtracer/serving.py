@@ -66,24 +66,27 @@ class ServeResult:
 
 
 def request_stream(rate: float, duration: float, scenes: list[str], seed: int = 1,
-                   progressive_fraction: float = 0.1, fixed: tuple | None = None) -> list[Request]:
+                   progressive_fraction: float = 0.1, fixed: tuple | None = None,
+                   fixed_share: float = 1.0) -> list[Request]:
+    """Poisson arrivals of the request mix; with `fixed` = (W, H, SPP, DEPTH), that share of the requests
+    (all by default) takes this shape instead and is never a progressive refinement."""
     rng = np.random.default_rng(seed)
     t, out = 0.0, []
     while True:
         t += rng.exponential(1.0 / rate)
         if t >= duration:
             return out
-        if fixed is not None:
+        side = math.exp(rng.uniform(math.log(64), math.log(1024)))
+        aspect = rng.uniform(1.0, 16.0 / 9.0)
+        w, h = max(8, int(side * math.sqrt(aspect))), max(8, int(side / math.sqrt(aspect)))
+        spp = int(rng.choice([1, 4, 16, 64]))
+        depth = int(rng.integers(4, 13))
+        progressive = bool(rng.random() < progressive_fraction)
+        if fixed is not None and (fixed_share >= 1.0 or rng.random() < fixed_share):
             w, h, spp, depth = fixed
-        else:
-            side = math.exp(rng.uniform(math.log(64), math.log(1024)))
-            aspect = rng.uniform(1.0, 16.0 / 9.0)
-            w, h = max(8, int(side * math.sqrt(aspect))), max(8, int(side / math.sqrt(aspect)))
-            spp = int(rng.choice([1, 4, 16, 64]))
-            depth = int(rng.integers(4, 13))
+            progressive = False
         out.append(Request(t, scenes[int(rng.integers(len(scenes)))], w, h, spp, depth,
-                           float(rng.uniform(-0.6, 0.6)), float(rng.uniform(-0.5, -0.2)),
-                           progressive=bool(rng.random() < progressive_fraction)))
+                           float(rng.uniform(-0.6, 0.6)), float(rng.uniform(-0.5, -0.2)), progressive=progressive))
 
 
 class Server:
@@ -146,6 +149,8 @@ class Server:
                 paths_of[jid] = paths
                 outstanding += paths
             for jid in eng.poll(timeout_ms=1):
+                if jid not in arrival_of:  # a job submitted outside this stream (e.g. a warm-up)
+                    continue
                 done_at = time.perf_counter() - t0
                 arrival, key, cont, req = arrival_of.pop(jid)
                 if on_done is not None:
@@ -202,8 +207,10 @@ def closed_loop(server: Server, requests: list[Request], mode: str) -> dict:
     for name, full in server.full.items():
         tracers[name] = pt.PathTracer(full, (64, 64))
         tracers[name].set_kernel(kernel)
+    service = []
     t0 = time.perf_counter()
     for r in requests:
+        s0 = time.perf_counter()
         tr = tracers[r.scene]
         cam = server.camera(r.scene, r)
         u = abi.WorldUpdates()
@@ -216,10 +223,22 @@ def closed_loop(server: Server, requests: list[Request], mode: str) -> dict:
         while left > 0:
             left -= tr.trace(left)
             tr.synchronize()
+        service.append(time.perf_counter() - s0)
     dt = time.perf_counter() - t0
     for tr in tracers.values():
         tr.close()
-    return {"mode": mode, "samples": total, "seconds": dt, "samples_per_s": total / dt}
+    return {"mode": mode, "samples": total, "seconds": dt, "samples_per_s": total / dt, "service_s": service}
+
+
+def replay_latencies(requests: list[Request], service_s: list[float]) -> list[float]:
+    """Arrival-to-completion latency (ms) of each request on a server that handles one request at a time,
+    in arrival order, each taking its measured service time."""
+    free_at, out = 0.0, []
+    for r, s in zip(requests, service_s):
+        start = max(r.arrival, free_at)
+        free_at = start + s
+        out.append((free_at - r.arrival) * 1e3)
+    return out
 
 
 def percentiles(xs: list) -> dict:
@@ -245,6 +264,8 @@ def main(argv=None) -> None:
     p.add_argument("--autotune", action="store_true",
                    help="with --compare: let the engine's autotuner pick wave size, tile size, refill steps, the "
                         "hit-sort threshold and the kernels' block shapes on 16 of the requests first")
+    p.add_argument("--save-tuned", action="store_true",
+                   help="with --compare --autotune: store the chosen settings in pathtracer/engine_tuned.json")
     p.add_argument("--compare", type=int, default=0,
                    help="instead of serving: render this many requests of the mix back to back with the plain "
                         "kernel, the wavefront kernel (one job per call) and the batched engine")
@@ -268,8 +289,14 @@ def main(argv=None) -> None:
             t = time.perf_counter()
             out["autotuned"] = eng.autotune(sample)
             out["autotune_s"] = time.perf_counter() - t
+            if args.save_tuned:
+                from pathlib import Path
+                cmd = ("python -m pathtracer.serving --compare " + str(args.compare) + " --scenes " + args.scenes +
+                       " --precision " + args.precision + " --autotune --save-tuned")
+                (Path(__file__).resolve().parent / "engine_tuned.json").write_text(json.dumps(
+                    {"config": out["autotuned"], "command": cmd, "seed": args.seed}, indent=1) + "\n")
         for mode in ("engine", "wavefront", "plain"):
-            out[mode] = closed_loop(server, reqs, mode)
+            out[mode] = {k: v for k, v in closed_loop(server, reqs, mode).items() if k != "service_s"}
         out["engine_over_plain"] = out["engine"]["samples_per_s"] / out["plain"]["samples_per_s"]
         out["wavefront_over_plain"] = out["wavefront"]["samples_per_s"] / out["plain"]["samples_per_s"]
         print(json.dumps(out))

@@ -22,6 +22,7 @@ import pytest
 
 import pathtracer as pt
 from pathtracer import abi
+from worlds import non_opaque_world
 
 pytestmark = pytest.mark.gpu
 
@@ -70,19 +71,27 @@ def noalloc(lib, dw, image, origin, tile, max_bounces, done, samples, accum, out
     return rc, err.value.decode()
 
 
-@pytest.mark.parametrize("scene", ["cornell", "procedural"])
+@pytest.mark.parametrize("scene", ["cornell", "procedural", "non_opaque"])
 def test_noalloc_matches_pt_trace_on_two_calls_in_a_row(scene):
+    """Opaque worlds run the wavefront kernels with a separate shadow stage; the non-opaque one (BLEND
+    and MASK materials, whose any-hit tests draw random numbers in the caller's triangle and material
+    buffers) traces its shadow rays inline."""
     torch = pytest.importorskip("torch")
     lib = pt.load()
     if scene == "cornell":
         world = pt.World.cornell_box()
         image, origin, tile, bounces, spp = (256, 256), (64, 32), (128, 128), 8, 4
-    else:
+    elif scene == "procedural":
         world = pt.World.procedural(grid_x=128, grid_z=64, boxes=100, spheres=10, sphere_subdivision=3,
                                     emissive_triangles=16, skybox_width=256, skybox_height=128)
         image, origin, tile, bounces, spp = (640, 360), (290, 150), (100, 80), 8, 3
+    else:
+        world = non_opaque_world()
+        image, origin, tile, bounces, spp = (200, 200), (40, 60), (96, 96), 6, 4
     world.set_aspect_ratio(image[0] / image[1])
     updates = world.take_updates()
+    mats = [updates.scene.contents.materials[i] for i in range(updates.scene.contents.material_count)]
+    assert any(m.alpha_mode != abi.PT_ALPHA_MODE_OPAQUE for m in mats) == (scene == "non_opaque")
 
     # the existing entry point
     tracer = pt.PathTracer(updates, tile)
@@ -126,6 +135,11 @@ def test_noalloc_rejects_requests_beyond_its_scratch():
     rc, msg = noalloc(lib, dw, (512, 512), (0, 0), tile, 2, 0, 1, accum, out)
     assert rc == abi.PT_OK, msg
     rc, msg = noalloc(lib, dw, (512, 512), (0, 0), tile, 2, 1, 2, accum, out)
+    assert rc == abi.PT_ERR_OUT_OF_LIMITS and "262144" in msg
+    # a request whose paths would wrap a 64-bit product (2^40 pixels x 2^24 samples) is refused on the host
+    # before anything is launched (the small buffers are never touched)
+    side = 1 << 20
+    rc, msg = noalloc(lib, dw, (side, side), (0, 0), (side, side), 2, 0, 1 << 24, accum, out)
     assert rc == abi.PT_ERR_OUT_OF_LIMITS and "262144" in msg
     torch.cuda.synchronize()
 
