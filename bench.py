@@ -57,6 +57,12 @@ PRECISIONS = {"fp32": 0, "wide": 1, "compressed": 7}
 # (dram__bytes_read.sum + dram__bytes_write.sum) of the first 16-spp group's
 # 9 extend launches
 TRAFFIC_PER_LAUNCH: dict = {("wavefront", "extend", "fp32"): 549.0e6}
+# warp instructions per path per launch of each kernel class (smsp__inst_executed.sum of the 9 launches
+# of each class of one 960x540 16-spp image of this scene, over 9 launches x 8,294,400 paths; the
+# per-path work of a launch does not depend on the image size); with the launch's paths and its
+# CUDA-event time they give the fraction of the SMs' issue slots the kernel fills
+WARP_INST_PER_PATH: dict = {("wavefront", "fp32"): {"extend": 92.58, "shade": 46.08, "shadow": 32.16}}
+SMS, SCHEDULERS_PER_SM = 152, 4
 
 
 def parse_args():
@@ -82,6 +88,7 @@ def parse_args():
     p.add_argument("--no-fp64", action="store_true",
                    help="skip the image error against the FP64 reference render")
     p.add_argument("--mix-seconds", type=float, default=10.0, help="seconds of arrivals of the serving stream")
+    p.add_argument("--dump-world", default=None, help=argparse.SUPPRESS)  # child process of --impl reference
     p.add_argument("--image", type=int, nargs=2, metavar=("W", "H"), default=None,
                    help="image size (default 1920 1080); smaller sizes are for ncu captures, not bench lines")
     args = p.parse_args()
@@ -371,11 +378,12 @@ def pinned_updates(updates):
     return u, keep, h2d
 
 
-def oracle_sample(updates, seconds: float, threads: int = 0):
+def oracle_sample(world, seconds: float, threads: int = 0):
     """Time the oracle's FP32 restatement on a strided pixel subset of the same workload,
-    sized to take about `seconds`; returns (Mrays/s, threads, description)."""
+    sized to take about `seconds`; returns (Mrays/s, threads, description).  `world` is a full
+    WorldUpdates or an oracle.OracleWorld."""
     import oracle
-    ow = oracle.world_from_updates(updates)
+    ow = world if isinstance(world, oracle.OracleWorld) else oracle.world_from_updates(world)
     threads = threads or oracle.max_threads()
 
     def run(stride_px: int, spp: int):
@@ -398,17 +406,102 @@ def oracle_sample(updates, seconds: float, threads: int = 0):
     return rays / dt / 1e6, threads, desc, dt
 
 
+# the buffers of a full world upload, in the order dump_world writes them
+UPLOAD_PARTS = ("geometries", "attributes", "materials", "bvh_nodes", "srgb", "linear", "sky", "sky_alias",
+                "scene_alias", "camera", "scene_uniforms", "skybox_uniforms")
+
+
+def dump_world(path: str) -> None:
+    """Build the workload's world with the library and write its full upload to `path` (.npz).
+    Runs in a child process of the reference arm, so that process never maps the library."""
+    world, u = build_world()
+    s, k = u.scene.contents, u.skybox.contents
+
+    def raw(ptr, n):
+        return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_uint8)), shape=(n,)).copy() if n else np.zeros(0, np.uint8)
+
+    layer = 8192 * 8192 * 4
+    parts = {
+        "geometries": raw(s.geometries, 36 * s.triangle_count),
+        "attributes": raw(s.attributes, 112 * s.triangle_count),
+        "materials": raw(s.materials, 224 * s.material_count),
+        "bvh_nodes": raw(s.bvh_nodes, 32 * s.node_count),
+        "srgb": raw(s.srgb_texture_atlases, layer * s.srgb_atlas_count),
+        "linear": raw(s.linear_texture_atlases, layer * s.linear_atlas_count),
+        "sky": raw(k.rgba, 16 * k.uniforms.width * k.uniforms.height),
+        "sky_alias": raw(k.alias_table, 12 * k.alias_count),
+        "scene_alias": raw(u.scene_alias_table, 16 * u.scene_alias_count),
+        "camera": np.frombuffer(bytes(u.camera.contents), np.uint8).copy(),
+        "scene_uniforms": np.frombuffer(bytes(u.scene_uniforms.contents), np.uint8).copy(),
+        "skybox_uniforms": np.frombuffer(bytes(u.skybox_uniforms.contents), np.uint8).copy(),
+        "counts": np.array([s.triangle_count, s.material_count, s.node_count, s.srgb_atlas_count,
+                            s.linear_atlas_count, k.alias_count, u.scene_alias_count], np.uint64),
+    }
+    np.savez(path, **parts)
+
+
+def oracle_world_from_dump(path: str):
+    """(OracleWorld, arrays it points into, counts) from a dump_world file; no library involved."""
+    import oracle
+    from pathtracer import abi
+    d = np.load(path)
+    keep = {name: np.ascontiguousarray(d[name]) for name in UPLOAD_PARTS}
+    tri, mats, nodes, srgb, linear, sky_alias, scene_alias = (int(x) for x in d["counts"])
+    w = oracle.OracleWorld()
+    w.geometries, w.attributes, w.triangle_count = keep["geometries"].ctypes.data, keep["attributes"].ctypes.data, tri
+    w.materials, w.material_count = keep["materials"].ctypes.data, mats
+    w.bvh_nodes, w.node_count = keep["bvh_nodes"].ctypes.data, nodes
+    w.srgb_atlases, w.srgb_atlas_count = (keep["srgb"].ctypes.data if srgb else None), srgb
+    w.linear_atlases, w.linear_atlas_count = (keep["linear"].ctypes.data if linear else None), linear
+    w.camera = abi.Camera.from_buffer_copy(keep["camera"].tobytes())
+    w.skybox_rgba = keep["sky"].ctypes.data
+    w.skybox = abi.SkyboxUniforms.from_buffer_copy(keep["skybox_uniforms"].tobytes())
+    w.skybox_aliases, w.skybox_alias_count = (keep["sky_alias"].ctypes.data if sky_alias else None), sky_alias
+    w.scene = abi.SceneUniforms.from_buffer_copy(keep["scene_uniforms"].tobytes())
+    w.scene_aliases, w.scene_alias_count = (keep["scene_alias"].ctypes.data if scene_alias else None), scene_alias
+    return w, keep, {"triangles": tri, "bvh_nodes": nodes}
+
+
+def gpu_library_mapped() -> bool:
+    """Whether this process has the GPU library (libpt.so) mapped."""
+    try:
+        return "libpt.so" in Path("/proc/self/maps").read_text()
+    except OSError:
+        return False
+
+
+class _Counts:
+    """triangle_count() / node_count() of a dumped world, for workload_config."""
+
+    def __init__(self, counts):
+        self.c = counts
+
+    def triangle_count(self):
+        return self.c["triangles"]
+
+    def node_count(self):
+        return self.c["bvh_nodes"]
+
+
 def run_reference(args):
     rank, _, world_size = dist_env()
     if rank != 0:
         return
-    world, updates = build_world()
+    # the scene is built in a child process and handed over as its upload bytes: this process loads
+    # only the oracle (the reference's CPU restatement), never the GPU library
+    with tempfile.TemporaryDirectory() as tmp:
+        path = str(Path(tmp) / "world.npz")
+        cmd = [sys.executable, str(Path(__file__).resolve()), "--dump-world", path, "--workload", WORKLOAD,
+               "--image", str(WIDTH), str(HEIGHT)]
+        subprocess.run(cmd, check=True)
+        ow, keep, counts = oracle_world_from_dump(path)
+    world = _Counts(counts)
     import oracle
     threads = oracle.max_threads()
     per_step = max(2.0, min(args.cpu_seconds, 20.0))
     values = []
     for i in range(args.warmup + args.steps):
-        v, threads, desc, dt = oracle_sample(updates, per_step if i >= args.warmup else 1.0)
+        v, threads, desc, dt = oracle_sample(ow, per_step if i >= args.warmup else 1.0)
         if i >= args.warmup:
             values.append((v, dt))
     value = float(np.mean([v for v, _ in values]))
@@ -420,7 +513,9 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": desc},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's own trace pass (Rust + WGSL via wgpu) cannot run on this box; this is the "
-                "oracle's C++ restatement of src/render/trace.slang, OpenMP over paths",
+                "oracle's C++ restatement of src/render/trace.slang, OpenMP over paths; the scene is built in a "
+                "child process and passed as its upload bytes",
+        "maps_gpu_library": gpu_library_mapped(),
     }
     print(json.dumps(line), flush=True)
 
@@ -528,6 +623,21 @@ def run_ours(args):
                 "image": [WIDTH, HEIGHT], "spp": spp, "precision": args.precision,
                 "fp64_render_s": time.perf_counter() - t64}
 
+    # issue-slot bound of the traversal and shading kernels: warp instructions per launch over the
+    # issue slots of its duration at the sampled SM clock
+    issue = None
+    inst = WARP_INST_PER_PATH.get((args.kernel, args.precision))
+    clock_summary = clocks.summary()
+    if inst and WIDTH * HEIGHT == 1920 * 1080 and clock_summary.get("sm_mhz"):
+        paths_per_launch = WIDTH * HEIGHT * min(spp, abi.PT_MAX_SAMPLES_PER_TRACE)
+        hz = clock_summary["sm_mhz"] * 1e6
+        issue = {"unit": "fraction of issue slots", "sm_mhz": clock_summary["sm_mhz"], "kernels": {}}
+        for k, per_path in inst.items():
+            n = max(1, times.launches[k])
+            avg_s = times.milliseconds[k] / n / 1e3
+            issue["kernels"][k] = {"warp_inst_per_launch": per_path * paths_per_launch, "avg_launch_ms": avg_s * 1e3,
+                                   "frac": per_path * paths_per_launch / (SMS * SCHEDULERS_PER_SM * hz * avg_s)}
+
     # end to end through the C ABI: world upload from pinned host memory, the
     # render, and the RGBA8 result read back, every step
     pinned, keep, h2d = pinned_updates(updates)
@@ -574,7 +684,8 @@ def run_ours(args):
             "roofline": roofline, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": WIDTH * HEIGHT * 4},
-            "gpu_launches": launches, "clocks": clocks.summary(), "latency": latency,
+            "issue_bound": issue,
+            "gpu_launches": launches, "clocks": clock_summary, "latency": latency,
             "rmse_vs_fp64": rmse, "mixed_stream": mix,
             "kernel_ms": {k: v for k, v in times.milliseconds.items() if times.launches[k]},
         }
@@ -587,6 +698,9 @@ def run_ours(args):
 
 def main():
     args = parse_args()
+    if args.dump_world:
+        dump_world(args.dump_world)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

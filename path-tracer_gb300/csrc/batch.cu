@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(kThreads, blocks_for(kWide ? PT_WIDE_MIN_BLOCK
             }
             return true;
         },
-        NoRound(), step_kind<PT_MAJORITY_SHADOW && !kWide>(tr));
+        NoRound(), step_kind<PT_MAJORITY_SHADOW && !kWide>(tr, [&]() -> const Fast& { return sc->f; }));
 }
 
 // accumulate, trace.slang:1299-1308: one block per item, samples in order;
@@ -933,11 +933,15 @@ int harvest(pt_engine* e, bool block) {
     return PT_OK;
 }
 
-// keeps two waves queued on the stream while jobs have pending items; each
-// wave's items are chosen when it is queued, so a newly submitted job waits
-// at most for the two waves already queued
+// waves queued on the stream at once: each wave's items are chosen when it
+// is queued, so a newly submitted job waits at most for the waves already
+// queued; one keeps that wait to the wave on the GPU, and the background
+// thread queues the next wave within ~0.1 ms of its end
+#ifndef PT_ENGINE_FLIGHTS
+#define PT_ENGINE_FLIGHTS 1
+#endif
 int pump(pt_engine* e) {
-    while (e->flights.size() < 2) {
+    while (e->flights.size() < PT_ENGINE_FLIGHTS) {
         size_t fed = 0;
         bool alpha = false;
         uint32_t rounds = 1;
@@ -1073,9 +1077,9 @@ bool evict_one(pt_engine* e) {
 
 }  // namespace
 
-// The background pump: every 100 us, finished waves are harvested and new
-// ones queued, so the stream never runs dry while the caller is busy between
-// calls (two waves in flight at most).
+// The background pump: while a wave runs, every ~20 us finished waves are
+// harvested and the next one queued, so the stream stays busy while the
+// caller is busy between calls (PT_ENGINE_FLIGHTS waves in flight at most).
 static void pump_loop(pt_engine* e) {
     cudaSetDevice(e->cfg.device);
     while (!e->stop.load(std::memory_order_relaxed)) {
@@ -1090,7 +1094,7 @@ static void pump_loop(pt_engine* e) {
             idle = e->flights.empty();  // nothing on the GPU and nothing queued by pump()
         }
         // while idle, a submit queues its own first wave, so a slower poll costs no latency
-        std::this_thread::sleep_for(std::chrono::microseconds(idle ? 1000 : 100));
+        std::this_thread::sleep_for(std::chrono::microseconds(idle ? 1000 : 20));
     }
 }
 

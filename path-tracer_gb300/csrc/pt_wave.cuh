@@ -266,6 +266,19 @@ PTD Tri load_tri4(const Fast& f, uint32_t tri) {
     return t;
 }
 
+// 1: after a closest-hit traversal step that did not finish, the lane
+// prefetches into L1 what its next step loads (the next child pair or
+// triangle), and a shadow lane that waits a majority step prefetches its
+// next step's data: the load is issued while the warp runs the other branch
+// for its other lanes.  The address is the one the next step reads, so it
+// is always inside the arrays.  Measured slower on the 2.1M-triangle scene
+// (1920x1080x64: 1648 against 1691 Mrays/s, extend +2.7 %, shadow +7 %; the
+// L1 is already busy with the loads themselves), so off by default
+#ifndef PT_PREFETCH
+#define PT_PREFETCH 0
+#endif
+PTD void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
 PTD float box_test(float4 lo, float4 hi, f3 nod, f3 rcp, float hit_t) {
     const float bmin[3] = {lo.x, lo.y, lo.z}, bmax[3] = {hi.x, hi.y, hi.z};
     return intersect_aabb(bmin, bmax, nod, rcp, hit_t);
@@ -361,12 +374,29 @@ struct Traverser {
 
     // kTriStep: one interior visit or one triangle of a leaf per step, else
     // one interior visit or a whole leaf
+    // prefetch what the next step loads: a leaf under way or about to start:
+    // its next triangle; else the next child pair (only while the traversal
+    // has not finished, so lf indexes a node pair or a triangle of a leaf)
+    PTD void prefetch_next(const Fast& f) const {
+#if PT_PREFETCH
+        if constexpr (!kTri36) {
+            if (tri_left > 0u || tc > 0u)
+                prefetch_l1(f.tri4 + kTriStride * (size_t)lf);
+            else
+                prefetch_l1(f.pairs + 2 * (size_t)lf);
+        }
+#endif
+    }
+
     template <class S>
     PTD bool step(const World& w, const Fast& f, S& stack, uint32_t* istack) {
-        if constexpr (kTriStep)
-            return step_tri(w, f, stack, istack);
-        else
+        if constexpr (kTriStep) {
+            const bool done = step_tri(w, f, stack, istack);
+            if (!done) prefetch_next(f);
+            return done;
+        } else {
             return step_leaf(w, f, stack, istack);
+        }
     }
 
 
@@ -597,9 +627,12 @@ PTD float bound_v(uint32_t w0, uint32_t w1) {
 // 1: the 8-wide child test evaluates a child's near and far slab distance
 // on one axis with one packed FP32 fma (fma.rn.f32x2, sm_100 and later: each
 // half rounds as one fma.rn, so the distances are the same bits); 0: one fma
-// per distance
+// per distance.  Measured slower on the 2.1M-triangle scene (compressed form,
+// 1920x1080x64: 1514 against 1535 Mrays/s, wide extend 442 against 429 ms
+// over three images; the packed operands cost registers and 40 B of spills),
+// so off by default
 #ifndef PT_WIDE_FMA2
-#define PT_WIDE_FMA2 1
+#define PT_WIDE_FMA2 0
 #endif
 PTD unsigned long long pack2(float lo, float hi) {
     unsigned long long r;
@@ -1195,15 +1228,18 @@ struct NoKind {};
 #ifndef PT_MAJORITY_SHADOW
 #define PT_MAJORITY_SHADOW 1
 #endif
-template <class T>
+template <class T, class G>
 struct StepKind {
     const T* t;
+    G fast;  // the lane's current scene layouts: () -> const Fast&
     PTD bool operator()() const { return t->next_is_interior(); }
+    // a lane that waits this step fetches its next step's data meanwhile (PT_PREFETCH)
+    PTD void wait() const { t->prefetch_next(fast()); }
 };
-template <bool kUse, class T>
-PTD auto step_kind(const T& t) {
+template <bool kUse, class T, class G>
+PTD auto step_kind(const T& t, G fast) {
     if constexpr (kUse)
-        return StepKind<T>{&t};
+        return StepKind<T, G>{&t, fast};
     else
         return NoKind{};
 }
@@ -1245,7 +1281,13 @@ PTD void lane_refill_loop(uint32_t* fetch, uint32_t count, uint32_t steps, unsig
                 if (alive == 0u) break;
                 const unsigned want = __ballot_sync(0xffffffffu, interior);
                 const bool run_interior = 2 * __popc(want) >= __popc(alive);
-                if (active && interior == run_interior && advance()) active = false;
+                if (active) {
+                    if (interior == run_interior) {
+                        if (advance()) active = false;
+                    } else {
+                        kind.wait();
+                    }
+                }
             }
         } else {
             if (active) {

@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
             filer.file(slot, tr.hit != -1);
             return true;
         },
-        [&]() { filer.flush(q, lane_id()); }, step_kind<PT_MAJORITY_EXTEND && !kWide>(tr));
+        [&]() { filer.flush(q, lane_id()); }, step_kind<PT_MAJORITY_EXTEND && !kWide>(tr, [&]() -> const Fast& { return f; }));
 }
 
 template <bool kRec, bool kAlpha>
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
             if constexpr (kRec) q.rec[path] = tr.c;
             return true;
         },
-        NoRound(), step_kind<PT_MAJORITY_SHADOW && !kWide>(tr));
+        NoRound(), step_kind<PT_MAJORITY_SHADOW && !kWide>(tr, [&]() -> const Fast& { return f; }));
 }
 
 // accumulate, trace.slang:1299-1308, samples of the group in order

@@ -69,3 +69,5 @@ def test_reference_arm_under_torchrun_prints_once():
     line = lines[0]
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+    # the arm runs the oracle only: the scene comes from a child process as upload bytes
+    assert line["maps_gpu_library"] is False
