@@ -40,6 +40,10 @@ WORKLOADS = {
                    "text": "procedural scene (1024x512-quad heightfield + 2000 boxes + 200 icospheres s4 + 64 "
                            "emissive triangles, 1024x512 sky)",
                    "l2": "inputs larger than L2 (scene buffers ~440 MB vs 129 MB L2), no flush"},
+    "procedural_4m": {"image": (1920, 1080), "spp": 64,
+                      "text": "procedural scene of the serving mix (1024x1024-quad heightfield + 4000 boxes + 360 "
+                              "icospheres s4 + 64 emissive triangles, 512x256 sky)",
+                      "l2": "inputs larger than L2 (scene buffers ~1.1 GB vs 129 MB L2), no flush"},
     "cornell": {"image": (256, 256), "spp": 16,
                 "text": "Cornell room (36 triangles: 5 wall quads, two rotated boxes, 0.25x0.25 emissive ceiling quad; "
                         "black sky)",
@@ -61,7 +65,8 @@ TRAFFIC_PER_LAUNCH: dict = {("wavefront", "extend", "fp32"): 549.0e6}
 # of each class of one 960x540 16-spp image of this scene, over 9 launches x 8,294,400 paths; the
 # per-path work of a launch does not depend on the image size); with the launch's paths and its
 # CUDA-event time they give the fraction of the SMs' issue slots the kernel fills
-WARP_INST_PER_PATH: dict = {("wavefront", "fp32"): {"extend": 92.58, "shade": 46.08, "shadow": 32.16}}
+WARP_INST_PER_PATH: dict = {("wavefront", "fp32"): {"extend": 92.57, "shade": 46.09, "shadow": 32.17},
+                             ("wavefront", "compressed"): {"extend": 122.08, "shade": 46.10, "shadow": 43.96}}
 SMS, SCHEDULERS_PER_SM = 152, 4
 
 
@@ -77,7 +82,8 @@ def parse_args():
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--workload", choices=list(WORKLOADS), default="procedural",
-                   help="procedural: the large scene of the bench line; cornell: the 36-triangle room")
+                   help="procedural: the large scene of the bench line; procedural_4m: the 4M-triangle scene of "
+                        "the serving mix; cornell: the 36-triangle room")
     p.add_argument("--spp", type=int, default=None, help="samples per pixel of one step (default: the workload's)")
     p.add_argument("--profile-run", action="store_true",
                    help="only the timed steps (no counting pass, e2e or CPU baseline): for ncu captures")
@@ -129,13 +135,19 @@ def workload_config(world, kernel: str) -> dict:
         "max_bounces": MAX_BOUNCES,
         "kernel": kernel,
         "l2": WORKLOADS[WORKLOAD]["l2"],
-        "seed": 1 if WORKLOAD == "procedural" else 0,
+        "seed": {"procedural": 1, "procedural_4m": 7}.get(WORKLOAD, 0),
     }
 
 
 def build_world():
     import pathtracer as pt
-    world = pt.World.procedural() if WORKLOAD == "procedural" else pt.World.cornell_box()
+    if WORKLOAD == "procedural":
+        world = pt.World.procedural()
+    elif WORKLOAD == "procedural_4m":
+        from pathtracer.serving import build_scene
+        world = build_scene("4M")
+    else:
+        world = pt.World.cornell_box()
     world.set_aspect_ratio(WIDTH / HEIGHT)
     return world, world.take_updates()
 
@@ -606,8 +618,8 @@ def run_ours(args):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = bytes_per_launch / avg_launch_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": TRAFFIC_PER_LAUNCH.get((args.kernel, cls, args.precision)) if WIDTH * HEIGHT * spp ==
-                1920 * 1080 * 64 else None, "kernel": cls,
+                "traffic": TRAFFIC_PER_LAUNCH.get((args.kernel, cls, args.precision))
+                if WORKLOAD == "procedural" and WIDTH * HEIGHT * spp == 1920 * 1080 * 64 else None, "kernel": cls,
                 "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs), of measured" if peaks else "fallback 6.8 TB/s"}
 
@@ -628,7 +640,7 @@ def run_ours(args):
     issue = None
     inst = WARP_INST_PER_PATH.get((args.kernel, args.precision))
     clock_summary = clocks.summary()
-    if inst and WIDTH * HEIGHT == 1920 * 1080 and clock_summary.get("sm_mhz"):
+    if inst and WORKLOAD == "procedural" and WIDTH * HEIGHT == 1920 * 1080 and clock_summary.get("sm_mhz"):
         paths_per_launch = WIDTH * HEIGHT * min(spp, abi.PT_MAX_SAMPLES_PER_TRACE)
         hz = clock_summary["sm_mhz"] * 1e6
         issue = {"unit": "fraction of issue slots", "sm_mhz": clock_summary["sm_mhz"], "kernels": {}}

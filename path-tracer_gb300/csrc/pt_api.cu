@@ -133,18 +133,27 @@ struct pt_ctx {
         cudaEventCreate(&e);
         return e;
     }
-    // bracket one kernel launch with events when profiling
+    // bracket one kernel launch (queued on stream s) with events when profiling
     template <class F>
-    cudaError_t timed(int cls, F&& launch) {
+    cudaError_t timed(int cls, cudaStream_t s, F&& launch) {
         launch_count += 1;
         if (!profiling) return launch();
         Timing t{cls, take_event(), take_event()};
-        cudaEventRecord(t.start, stream);
+        cudaEventRecord(t.start, s);
         cudaError_t e = launch();
-        cudaEventRecord(t.stop, stream);
+        cudaEventRecord(t.stop, s);
         pending.push_back(t);
         return e;
     }
+    template <class F>
+    cudaError_t timed(int cls, F&& launch) {
+        return timed(cls, stream, launch);
+    }
+    // Work queued on the context stream other than wavefront groups: the next
+    // pt_trace's groups then wait for the stream instead of starting beside the
+    // previous call's groups (ctx_ops counts such work).
+    uint64_t ctx_ops = 0, ops_at_trace = ~0ull;
+    void touched() { ctx_ops += 1; }
     void harvest() {
         for (Timing& t : pending) {
             cudaEventSynchronize(t.stop);
@@ -271,6 +280,7 @@ int validate_lights(pt_ctx* c, const pt_scene_uniforms& s, uint64_t scene_alias_
 namespace {
 
 int apply(pt_ctx* c, const pt_world_updates* u, bool initial) {
+    c->touched();
     if (!u) return c->fail(PT_ERR_INVALID_ARG, "updates is NULL");
     if (initial) {
         if (!u->scene) return c->fail(PT_ERR_INVALID_ARG, "initial scene upload missing");
@@ -414,6 +424,7 @@ int apply(pt_ctx* c, const pt_world_updates* u, bool initial) {
 }
 
 int alloc_tile(pt_ctx* c, uint32_t w, uint32_t h) {
+    c->touched();
     if (w == 0 || h == 0 || w > kMaxTileDim || h > kMaxTileDim) {
         char msg[160];
         snprintf(msg, sizeof msg, "tile size %ux%u must be positive and at most %u pixels in each dimension", w, h, kMaxTileDim);
@@ -459,6 +470,7 @@ int trace_impl(pt_ctx* c, uint32_t samples, uint32_t* traced, pt_path_record* ho
     const size_t tile_px = (size_t)c->tile_w * c->tile_h;
     pt_path_record* rec = nullptr;
     int rc = PT_OK;
+    if (host_records || host_totals || c->kernel == PT_KERNEL_PLAIN) c->touched();  // work on the context stream
     if (host_records) {
         if ((rc = c->cuda(c->records.reserve(tile_px * n * sizeof(pt_path_record)), "records"))) return rc;
         if ((rc = c->cuda(cudaMemsetAsync(c->records.p, 0, tile_px * n * sizeof(pt_path_record), c->stream), "records"))) return rc;
@@ -480,16 +492,26 @@ int trace_impl(pt_ctx* c, uint32_t samples, uint32_t* traced, pt_path_record* ho
             if (rc) return rc;
         }
     } else {
-        if (!c->wavefront) ptw::create(&c->wavefront);
+        if (!c->wavefront) {
+            const int ce = ptw::create(&c->wavefront);
+            if (ce) return c->cuda((cudaError_t)ce, "wavefront streams");
+        }
         const bool record = rec != nullptr || tot != nullptr;
         const uint32_t form = ptw::effective_precision(w, c->precision, record);
-        if ((rc = c->cuda(ptw::prepare(c->wavefront, w, c->node_count, c->tri_count, form, c->stream), "wavefront layouts")))
+        bool queued = false;
+        if ((rc = c->cuda(ptw::prepare(c->wavefront, w, c->node_count, c->tri_count, form, c->stream, &queued),
+                          "wavefront layouts")))
             return rc;
-        const ptw::Timer timer = [c](int cls, const std::function<cudaError_t()>& f) { return c->timed(cls, f); };
-        rc = c->cuda(ptw::trace(c->wavefront, w, t, first, n, ptk::Sinks{rec, tot}, c->stream, timer, form),
+        if (queued) c->touched();
+        const bool overlap = !record && c->ctx_ops == c->ops_at_trace;
+        const ptw::Timer timer = [c](int cls, cudaStream_t s, const std::function<cudaError_t()>& f) {
+            return c->timed(cls, s, f);
+        };
+        rc = c->cuda(ptw::trace(c->wavefront, w, t, first, n, ptk::Sinks{rec, tot}, c->stream, timer, form, overlap),
                      "wavefront trace");
         if (rc) return rc;
         c->precision_active = form;
+        if (!record) c->ops_at_trace = c->ctx_ops;
     }
     c->params.sample_count += n;
     if (traced) *traced = n;
@@ -617,6 +639,7 @@ int pt_trace_recorded(pt_ctx* c, uint32_t samples, uint32_t* traced, pt_path_rec
 int pt_read_tile(pt_ctx* c, int which, float* host_rgba) {
     if (!c || !host_rgba || (which != PT_TILE_IMAGE && which != PT_TILE_ACCUMULATION && which != PT_TILE_COMPENSATION))
         return PT_ERR_INVALID_ARG;
+    c->touched();
     cudaSetDevice(c->device);
     if (which == PT_TILE_COMPENSATION && !(c->precision & PT_PRECISION_KAHAN)) {
         std::memset(host_rgba, 0, (size_t)c->tile_w * c->tile_h * 16);
@@ -631,6 +654,7 @@ int pt_read_tile(pt_ctx* c, int which, float* host_rgba) {
 
 int pt_display_tile(pt_ctx* c, uint8_t* host_rgba8) {
     if (!c || !host_rgba8) return PT_ERR_INVALID_ARG;
+    c->touched();
     cudaSetDevice(c->device);
     const size_t px = (size_t)c->tile_w * c->tile_h;
     int rc = c->cuda(c->display.reserve(px * 4), "display buffer");
@@ -669,6 +693,7 @@ int pt_set_kernel(pt_ctx* c, int kernel) {
 
 int pt_set_precision(pt_ctx* c, uint32_t flags) {
     if (!c) return PT_ERR_INVALID_ARG;
+    c->touched();
     if (flags & ~PT_PRECISION_COMPRESSED) return c->fail(PT_ERR_INVALID_ARG, "unknown precision bits");
     if (flags != PT_PRECISION_FP32 && c->kernel != PT_KERNEL_WAVEFRONT)
         return c->fail(PT_ERR_STATE, "the precision form runs on the wavefront kernels");
@@ -689,6 +714,7 @@ uint32_t pt_precision_active(const pt_ctx* c) { return c ? c->precision_active :
 
 int pt_get_stream(pt_ctx* c, void** stream) {
     if (!c || !stream) return PT_ERR_INVALID_ARG;
+    c->touched();
     *stream = (void*)c->stream;
     return PT_OK;
 }
@@ -725,6 +751,7 @@ uint64_t pt_launch_count(const pt_ctx* c) { return c ? c->launch_count : 0; }
 
 int pt_render_fp64(pt_ctx* c, uint32_t sample_first, uint32_t sample_count, double* host_rgb_sums) {
     if (!c || !host_rgb_sums) return PT_ERR_INVALID_ARG;
+    c->touched();
     if (sample_first == 0 || sample_count == 0 || sample_count - 1u > 0xffffffffu - sample_first)
         return c->fail(PT_ERR_INVALID_ARG, "FP64 render needs a non-empty range of 1-based sample indices");
     if (!c->world_ready) return c->fail(PT_ERR_STATE, "no world uploaded");
@@ -744,6 +771,7 @@ int pt_render_fp64(pt_ctx* c, uint32_t sample_first, uint32_t sample_count, doub
 int pt_debug_intersect(pt_ctx* c, uint64_t n, const float* origins, const float* directions, const float* t_max,
                        int32_t* hit, float* hit_t, pt_path_record* records) {
     if (!c || !origins || !directions || !t_max || !hit || !hit_t) return PT_ERR_INVALID_ARG;
+    c->touched();
     if (!c->world_ready) return c->fail(PT_ERR_STATE, "no world uploaded");
     if (n == 0) return PT_OK;
     cudaSetDevice(c->device);
@@ -757,8 +785,8 @@ int pt_debug_intersect(pt_ctx* c, uint64_t n, const float* origins, const float*
     const ptd::World w = c->view();
     const bool wide = (ptw::effective_precision(w, c->precision, records != nullptr) & PT_PRECISION_WIDE_BVH) != 0;
     if (!rc && wide) {
-        if (!c->wavefront) ptw::create(&c->wavefront);
-        rc = c->cuda(ptw::prepare(c->wavefront, w, c->node_count, c->tri_count, PT_PRECISION_WIDE_BVH, c->stream),
+        if (!c->wavefront) rc = c->cuda((cudaError_t)ptw::create(&c->wavefront), "wavefront streams");
+        if (!rc) rc = c->cuda(ptw::prepare(c->wavefront, w, c->node_count, c->tri_count, PT_PRECISION_WIDE_BVH, c->stream),
                      "wide BVH");
     }
     if (!rc)

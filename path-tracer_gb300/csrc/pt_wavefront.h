@@ -26,8 +26,9 @@ void destroy(Wavefront* wf);
 // the world buffers changed: derived layouts are rebuilt on the next trace
 void world_changed(Wavefront* wf);
 
-// wraps each kernel launch (class id from PT_KC_*) so the caller can time it
-using Timer = std::function<cudaError_t(int cls, const std::function<cudaError_t()>& launch)>;
+// wraps each kernel launch (class id from PT_KC_*, the stream it is queued
+// on) so the caller can time it
+using Timer = std::function<cudaError_t(int cls, cudaStream_t stream, const std::function<cudaError_t()>& launch)>;
 
 // the skybox texels changed (its BF16 copy is rebuilt on the next trace)
 void sky_changed(Wavefront* wf);
@@ -36,16 +37,25 @@ void sky_changed(Wavefront* wf);
 // padded triangles always; for the precision form (PT_PRECISION_* bits of
 // include/pt_precision.h) the 8-wide BVH (collapsed on the host from the
 // device's binary nodes) and the FP16 attributes / BF16 skybox.
+// *queued (if given): whether work was queued on `stream`.
 cudaError_t prepare(Wavefront* wf, const ptd::World& w, uint64_t nodes, uint64_t tris, uint32_t precision,
-                    cudaStream_t stream);
+                    cudaStream_t stream, bool* queued = nullptr);
 
 // the precision bits a trace with these arguments runs: the wide BVH only for
 // opaque worlds and not for the recording variants (their records describe
 // the binary traversal)
 uint32_t effective_precision(const ptd::World& w, uint32_t precision, bool record);
 
+// Traces samples first_sample.. of the tile in groups of at most 2^25 paths.
+// Each group runs on one of two internal streams with its own queues, so
+// consecutive groups overlap (the next group's first bounces beside the last
+// bounces of the previous one); its accumulation is queued on `stream`, so
+// any later work there sees the finished samples in order.  `overlap`: no
+// work was queued on `stream` since the previous call's groups began, so this
+// call's groups may start where those did (otherwise they wait for `stream`).
 cudaError_t trace(Wavefront* wf, const ptd::World& w, const ptk::Tile& tile, uint32_t first_sample,
-                  uint32_t samples, ptk::Sinks sinks, cudaStream_t stream, const Timer& timer, uint32_t precision);
+                  uint32_t samples, ptk::Sinks sinks, cudaStream_t stream, const Timer& timer, uint32_t precision,
+                  bool overlap);
 
 // the narrow copies of the precision form, on `stream`: FP32 attributes ->
 // pt_half_attribute records (8 uint2 each), RGBA32F texels -> BF16 RGBA

@@ -411,9 +411,24 @@ constexpr uint64_t kMaxPaths = 1ull << 25;  // paths in flight per group
 
 }  // namespace
 
-struct Wavefront {
-    Buf o[2], d[2], T[2], hit, color, so, sd, sc, cnt, rec, rec_hits;
+// The queues of one group of paths and the stream it runs on.  Two lanes let
+// consecutive groups overlap: one group's last bounces (few, long rays that
+// leave most SMs idle) run beside the next group's first ones.
+struct Lane {
+    Buf o[2], d[2], T[2], hit, color, so, sd, sc, cnt;
     Buf lists;  // hit list, miss list, sorted hit list (capacity entries each), sort counts and offsets
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;   // the lane's group finished (recorded on the lane)
+    cudaEvent_t freed = nullptr;  // its accumulation consumed the colours (recorded on the caller's stream)
+    bool pending = false;         // `freed` was recorded and not yet waited for
+};
+
+struct Wavefront {
+    Lane lane[2];
+    Buf rec, rec_hits;
+    int next_lane = 0;
+    cudaEvent_t start = nullptr;  // the caller's stream before the last group began
+    bool have_start = false;
     Buf pairs, tri4;
     Buf wide, links, attr_h, sky_h;  // precision form copies (links: parent per node, leaf per triangle)
     bool stale = true;
@@ -430,18 +445,33 @@ struct Wavefront {
 };
 
 int create(Wavefront** out) {
-    *out = new Wavefront();
+    Wavefront* wf = new Wavefront();
     int dev = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&(*out)->sms, cudaDevAttrMultiProcessorCount, dev);
-    return 0;
+    cudaDeviceGetAttribute(&wf->sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaEventCreateWithFlags(&wf->start, cudaEventDisableTiming);
+    for (Lane& l : wf->lane) {
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.freed, cudaEventDisableTiming);
+    }
+    *out = wf;
+    return e == cudaSuccess ? 0 : (int)e;
 }
 
 void destroy(Wavefront* wf) {
     if (!wf) return;
-    for (Buf* b : {&wf->o[0], &wf->o[1], &wf->d[0], &wf->d[1], &wf->T[0], &wf->T[1], &wf->hit, &wf->color, &wf->so,
-                   &wf->sd, &wf->sc, &wf->cnt, &wf->rec, &wf->rec_hits, &wf->lists, &wf->pairs, &wf->tri4,
-                   &wf->wide, &wf->links, &wf->attr_h, &wf->sky_h})
+    for (Lane& l : wf->lane) {
+        if (l.stream) cudaStreamSynchronize(l.stream);
+        for (Buf* b : {&l.o[0], &l.o[1], &l.d[0], &l.d[1], &l.T[0], &l.T[1], &l.hit, &l.color, &l.so, &l.sd, &l.sc,
+                       &l.cnt, &l.lists})
+            b->release();
+        if (l.done) cudaEventDestroy(l.done);
+        if (l.freed) cudaEventDestroy(l.freed);
+        if (l.stream) cudaStreamDestroy(l.stream);
+    }
+    if (wf->start) cudaEventDestroy(wf->start);
+    for (Buf* b : {&wf->rec, &wf->rec_hits, &wf->pairs, &wf->tri4, &wf->wide, &wf->links, &wf->attr_h, &wf->sky_h})
         b->release();
     delete wf;
 }
@@ -499,12 +529,16 @@ cudaError_t build_wide(Wavefront* wf, const ptd::World& w, uint64_t nodes, uint6
 
 cudaError_t reserve_paths(Wavefront* wf, uint64_t paths, bool record) {
     const size_t b = paths * 16;
-    for (Buf* x : {&wf->o[0], &wf->o[1], &wf->d[0], &wf->d[1], &wf->T[0], &wf->T[1], &wf->hit, &wf->color, &wf->so,
-                   &wf->sd, &wf->sc})
-        PTW_TRY(x->reserve(b));
-    PTW_TRY(wf->cnt.reserve(64));
-    PTW_TRY(wf->lists.reserve(paths * 12 + 2 * ptd::kSortBuckets * 4));
-    PTW_TRY(cudaMemset(static_cast<uint32_t*>(wf->lists.p) + 3 * paths, 0, ptd::kSortBuckets * 4));  // sort counts
+    // earlier groups (on the lanes) and their accumulations (on the callers'
+    // streams) may still use the buffers a larger reservation frees
+    PTW_TRY(cudaDeviceSynchronize());
+    for (Lane& l : wf->lane) {
+        for (Buf* x : {&l.o[0], &l.o[1], &l.d[0], &l.d[1], &l.T[0], &l.T[1], &l.hit, &l.color, &l.so, &l.sd, &l.sc})
+            PTW_TRY(x->reserve(b));
+        PTW_TRY(l.cnt.reserve(64));
+        PTW_TRY(l.lists.reserve(paths * 12 + 2 * ptd::kSortBuckets * 4));
+        PTW_TRY(cudaMemset(static_cast<uint32_t*>(l.lists.p) + 3 * paths, 0, ptd::kSortBuckets * 4));  // sort counts
+    }
     if (record) {
         PTW_TRY(wf->rec.reserve(paths * sizeof(ptd::Counters)));
         PTW_TRY(wf->rec_hits.reserve(paths * PT_RECORD_MAX_BOUNCES * 4));
@@ -540,15 +574,18 @@ struct SortCfg {
 // one group of paths through raygen, max_bounces + 1 rounds of extend /
 // (hit sort) / shade / shadow, and accumulate; kTri36 reads the reference's
 // 36-byte triangles instead of the padded copy
+// One group of paths through every bounce on `stream`; the accumulation runs
+// on `acc_stream` (null: `stream`) after `done` marks the group's end there.
 template <bool kRec, bool kAlpha, bool kTri36, bool kWide = false, class TimerF>
 cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const ptd::Queues& q,
                       const ptk::Tile& tile, const ptd::Group& g, ptk::Sinks sinks, cudaStream_t stream,
-                      TimerF&& timer, const SortCfg& sort = SortCfg()) {
+                      TimerF&& timer, const SortCfg& sort = SortCfg(), cudaStream_t acc_stream = nullptr,
+                      cudaEvent_t done = nullptr) {
     using namespace ptd;
     const int ext_blocks = sms * occupancy(extend_kernel<kRec, kAlpha, kTri36, kWide>, kExtendThreads);
     const int sha_blocks = sms * occupancy(shade_kernel<kRec, kAlpha>, kShadeThreads);
     const int shd_blocks = sms * occupancy(shadow_kernel<kRec, kTri36, kWide>, kExtendThreads);
-    PTW_TRY(timer(PT_KC_RAYGEN, [&] {
+    PTW_TRY(timer(PT_KC_RAYGEN, stream, [&] {
         raygen_kernel<kRec><<<(g.paths + 255u) / 256u, 256, 0, stream>>>(w, tile, g, q);
         return cudaGetLastError();
     }));
@@ -568,14 +605,14 @@ cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const pt
         PTW_TRY(cudaGetLastError());
         if (PT_RAY_ORDER && sorting && bounce > 0) {  // camera rays are coherent already (pixel-major)
             // timed with the sorts (shading class), as the hit sort
-            PTW_TRY(timer(PT_KC_SHADE, [&] { return order_rays(cur ? q.d[1] : q.d[0], q.cnt + cur, 8u); }));
+            PTW_TRY(timer(PT_KC_SHADE, stream, [&] { return order_rays(cur ? q.d[1] : q.d[0], q.cnt + cur, 8u); }));
         }
-        PTW_TRY(timer(PT_KC_EXTEND, [&] {
+        PTW_TRY(timer(PT_KC_EXTEND, stream, [&] {
             extend_kernel<kRec, kAlpha, kTri36, kWide><<<ext_blocks, kExtendThreads, 0, stream>>>(w, f, q, cur, bounce);
             return cudaGetLastError();
         }));
         if (sort.counts && sort.min_hits != 0xffffffffu) {
-            PTW_TRY(timer(PT_KC_SHADE, [&] {
+            PTW_TRY(timer(PT_KC_SHADE, stream, [&] {
                 sort_count_kernel<PT_SORT_KEY><<<sms * 4, kSortThreads, 0, stream>>>(w, q, sort.counts, sort.min_hits,
                                                                                     sort.tri_shift);
                 sort_scan_kernel<0><<<1, 1024, 0, stream>>>(q, sort.counts, sort.counts + kSortBuckets, sort.min_hits);
@@ -584,23 +621,28 @@ cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const pt
                 return cudaGetLastError();
             }));
         }
-        PTW_TRY(timer(PT_KC_SHADE, [&] {
+        PTW_TRY(timer(PT_KC_SHADE, stream, [&] {
             shade_kernel<kRec, kAlpha><<<sha_blocks, kShadeThreads, 0, stream>>>(w, f, q, cur, bounce, tile.max_bounces);
             return cudaGetLastError();
         }));
         if constexpr (!kAlpha) {
             if (PT_SHADOW_ORDER && sorting) {
-                PTW_TRY(timer(PT_KC_SHADE, [&] { return order_rays(q.sd, q.cnt + 2, 9u); }));
+                PTW_TRY(timer(PT_KC_SHADE, stream, [&] { return order_rays(q.sd, q.cnt + 2, 9u); }));
             }
-            PTW_TRY(timer(PT_KC_SHADOW, [&] {
+            PTW_TRY(timer(PT_KC_SHADOW, stream, [&] {
                 shadow_kernel<kRec, kTri36, kWide><<<shd_blocks, kExtendThreads, 0, stream>>>(w, f, q);
                 return cudaGetLastError();
             }));
         }
         cur ^= 1;
     }
-    PTW_TRY(timer(PT_KC_ACCUMULATE, [&] {
-        accumulate_kernel<<<(g.pixels + 255u) / 256u, 256, 0, stream>>>(tile, g, q.color);
+    const cudaStream_t as = acc_stream ? acc_stream : stream;
+    if (as != stream) {
+        PTW_TRY(cudaEventRecord(done, stream));
+        PTW_TRY(cudaStreamWaitEvent(as, done, 0));
+    }
+    PTW_TRY(timer(PT_KC_ACCUMULATE, as, [&] {
+        accumulate_kernel<<<(g.pixels + 255u) / 256u, 256, 0, as>>>(tile, g, q.color);
         return cudaGetLastError();
     }));
     if constexpr (kRec) {
@@ -613,7 +655,7 @@ cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const pt
 }  // namespace
 
 cudaError_t trace(Wavefront* wf, const ptd::World& w_in, const ptk::Tile& tile, uint32_t first, uint32_t samples,
-                  ptk::Sinks sinks, cudaStream_t stream, const Timer& timer, uint32_t precision) {
+                  ptk::Sinks sinks, cudaStream_t stream, const Timer& timer, uint32_t precision, bool overlap) {
     precision = effective_precision(w_in, precision, sinks.any());
     ptd::World w = w_in;
     if (precision & PT_PRECISION_HALF_ATTRIBUTES) {
@@ -633,36 +675,16 @@ cudaError_t trace(Wavefront* wf, const ptd::World& w_in, const ptk::Tile& tile, 
     if (group > samples) group = samples;
     const uint64_t paths = pixels * group;
     const bool record = sinks.any();
-    if (paths > wf->capacity || (record && wf->rec.bytes < paths * sizeof(ptd::Counters)))
+    if (paths > wf->capacity || (record && wf->rec.bytes < paths * sizeof(ptd::Counters))) {
         PTW_TRY(reserve_paths(wf, paths > wf->capacity ? paths : wf->capacity, record));
-    ptd::Queues q;
-    for (int k = 0; k < 2; ++k) {
-        q.o[k] = static_cast<float4*>(wf->o[k].p);
-        q.d[k] = static_cast<float4*>(wf->d[k].p);
-        q.T[k] = static_cast<float4*>(wf->T[k].p);
+        wf->have_start = false;
     }
-    q.hit = static_cast<float4*>(wf->hit.p);
-    q.color = static_cast<float4*>(wf->color.p);
-    q.so = static_cast<float4*>(wf->so.p);
-    q.sd = static_cast<float4*>(wf->sd.p);
-    q.sc = static_cast<float4*>(wf->sc.p);
-    q.cnt = static_cast<uint32_t*>(wf->cnt.p);
-    q.hit_list = static_cast<uint32_t*>(wf->lists.p);
-    q.miss_list = q.hit_list + wf->capacity;
-    q.hit_sorted = q.miss_list + wf->capacity;
-    uint32_t* sort_counts = q.hit_sorted + wf->capacity;  // kSortBuckets counts, then kSortBuckets offsets
-    q.rec = static_cast<ptd::Counters*>(wf->rec.p);
-    q.rec_hits = static_cast<int32_t*>(wf->rec_hits.p);
     ptd::Fast f;
     f.pairs = reinterpret_cast<const float4*>(static_cast<const char*>(wf->pairs.p) + 32);
     f.tri4 = static_cast<const float4*>(wf->tri4.p);
     f.wide = static_cast<const float4*>(wf->wide.p);
     f.parent = static_cast<const uint32_t*>(wf->links.p);
     f.leaf_of = f.parent ? f.parent + wf->links_nodes : nullptr;
-    SortCfg sort;
-    sort.counts = sort_counts;
-    sort.min_hits = PT_SORT_MIN_HITS;
-    while (((uint64_t)ptd::kSortBuckets << sort.tri_shift) < wf->tri_count && sort.tri_shift < 31u) sort.tri_shift += 1u;
     for (uint32_t s0 = 0; s0 < samples; s0 += group) {
         ptd::Group g;
         g.vis_w = vis_w;
@@ -672,22 +694,78 @@ cudaError_t trace(Wavefront* wf, const ptd::World& w_in, const ptk::Tile& tile, 
         g.paths = (uint32_t)(pixels * g.samples);
         g.first_sample = first + s0;
         g.record_sample = s0;
+        // The recording variants run in order on the caller's stream with lane
+        // 0's queues.  Otherwise the group runs on the next lane: it starts after
+        // the caller's stream reaches this call (or, when `overlap` says nothing
+        // was queued there since the previous group began, after that group's
+        // starting point) and after the lane's previous accumulation; its own
+        // accumulation runs on the caller's stream, so the samples of a pixel
+        // are still summed in order and any later work there sees the result.
+        Lane& l = record ? wf->lane[0] : wf->lane[wf->next_lane];
+        const cudaStream_t gs = record ? stream : l.stream;
+        if (!record) {
+            wf->next_lane ^= 1;
+            if (!(overlap && wf->have_start)) {
+                PTW_TRY(cudaEventRecord(wf->start, stream));
+                wf->have_start = true;
+            }
+            overlap = true;  // the call's later groups start from the same point
+            PTW_TRY(cudaStreamWaitEvent(gs, wf->start, 0));
+            if (l.pending) PTW_TRY(cudaStreamWaitEvent(gs, l.freed, 0));
+        }
+        ptd::Queues q;
+        for (int k = 0; k < 2; ++k) {
+            q.o[k] = static_cast<float4*>(l.o[k].p);
+            q.d[k] = static_cast<float4*>(l.d[k].p);
+            q.T[k] = static_cast<float4*>(l.T[k].p);
+        }
+        q.hit = static_cast<float4*>(l.hit.p);
+        q.color = static_cast<float4*>(l.color.p);
+        q.so = static_cast<float4*>(l.so.p);
+        q.sd = static_cast<float4*>(l.sd.p);
+        q.sc = static_cast<float4*>(l.sc.p);
+        q.cnt = static_cast<uint32_t*>(l.cnt.p);
+        q.hit_list = static_cast<uint32_t*>(l.lists.p);
+        q.miss_list = q.hit_list + wf->capacity;
+        q.hit_sorted = q.miss_list + wf->capacity;
+        q.rec = static_cast<ptd::Counters*>(wf->rec.p);
+        q.rec_hits = static_cast<int32_t*>(wf->rec_hits.p);
+        SortCfg sort;
+        sort.counts = q.hit_sorted + wf->capacity;  // kSortBuckets counts, then kSortBuckets offsets
+        sort.min_hits = PT_SORT_MIN_HITS;
+        while (((uint64_t)ptd::kSortBuckets << sort.tri_shift) < wf->tri_count && sort.tri_shift < 31u) sort.tri_shift += 1u;
+        const cudaStream_t as = record ? nullptr : stream;
         cudaError_t e;
         if (record)
-            e = w.any_alpha ? run_group<true, true, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer)
-                            : run_group<true, false, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer);
+            e = w.any_alpha ? run_group<true, true, false>(wf->sms, w, f, q, tile, g, sinks, gs, timer)
+                            : run_group<true, false, false>(wf->sms, w, f, q, tile, g, sinks, gs, timer);
         else if (wide)
-            e = run_group<false, false, false, true>(wf->sms, w, f, q, tile, g, sinks, stream, timer, sort);
+            e = run_group<false, false, false, true>(wf->sms, w, f, q, tile, g, sinks, gs, timer, sort, as, l.done);
         else
-            e = w.any_alpha ? run_group<false, true, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer, sort)
-                            : run_group<false, false, false>(wf->sms, w, f, q, tile, g, sinks, stream, timer, sort);
+            e = w.any_alpha ? run_group<false, true, false>(wf->sms, w, f, q, tile, g, sinks, gs, timer, sort, as, l.done)
+                            : run_group<false, false, false>(wf->sms, w, f, q, tile, g, sinks, gs, timer, sort, as, l.done);
         PTW_TRY(e);
+        if (!record) {
+            PTW_TRY(cudaEventRecord(l.freed, stream));
+            l.pending = true;
+        } else {
+            wf->have_start = false;  // a later group must start after this one, which used lane 0 on `stream`
+        }
     }
     return cudaSuccess;
 }
 
 cudaError_t prepare(Wavefront* wf, const ptd::World& w, uint64_t nodes, uint64_t tris, uint32_t precision,
-                    cudaStream_t stream) {
+                    cudaStream_t stream, bool* queued) {
+    const bool work = wf->stale || wf->layout_nodes != w.nodes || wf->layout_geo != w.geo ||
+                      ((precision & PT_PRECISION_WIDE_BVH) && !wf->wide_ready) ||
+                      ((precision & PT_PRECISION_HALF_ATTRIBUTES) && (!wf->attr_h_ready || !wf->sky_h_ready));
+    if (queued) *queued = work;
+    if (work) {
+        // groups still running on the lanes read the layouts about to be rebuilt
+        for (Lane& l : wf->lane) PTW_TRY(cudaStreamWaitEvent(stream, l.done, 0));
+        wf->have_start = false;
+    }
     if (wf->stale || wf->layout_nodes != w.nodes || wf->layout_geo != w.geo)
         PTW_TRY(build_layouts(wf, w, nodes, tris, stream));
     if ((precision & PT_PRECISION_WIDE_BVH) && !wf->wide_ready) PTW_TRY(build_wide(wf, w, nodes, tris, stream));
@@ -905,7 +983,7 @@ extern "C" int pt_trace_noalloc(const pt_device_world* world, const pt_trace_par
     g.record_sample = 0;
 
     const cudaStream_t s = static_cast<cudaStream_t>(stream);
-    auto untimed = [](int, auto&& launch) { return launch(); };
+    auto untimed = [](int, cudaStream_t, auto&& launch) { return launch(); };
     const cudaError_t e = w.any_alpha
                               ? ptw::run_group<false, true, true>(g_noalloc_devices[dev].sms, w, f, q, t, g, ptk::Sinks{nullptr, nullptr}, s, untimed)
                               : ptw::run_group<false, false, true>(g_noalloc_devices[dev].sms, w, f, q, t, g, ptk::Sinks{nullptr, nullptr}, s, untimed);
