@@ -166,7 +166,7 @@ def algorithmic_bytes(t: dict, emissive: int, paths: int) -> dict:
     shade = 372 * t["hits"] + alias * t["light_samples"] + 24 * t["sky_light_samples"] + 64 * t["sky_misses"]
     accumulate = 48 * paths
     total = extend + shadow + shade + accumulate
-    return {"extend": extend, "shadow": shadow, "shade": shade, "accumulate": accumulate, "raygen": 0,
+    return {"extend": extend, "shadow": shadow, "shade": shade, "accumulate": accumulate, "raygen": 0, "sort": 0,
             "plain": total, "total": total}
 
 
@@ -294,30 +294,35 @@ def mixed_stream_report(seconds: float = 10.0, rate: float = 50.0, jobs: int = 2
     * serving: Poisson arrivals at `rate` req/s for `seconds` s, 10 % progressive refinements, a
       fifth of the requests 512x512 x 16 spp x max_bounces 8; latency from arrival to result
       through the serving loop (continuous batching) on the same engine, overall and for the
-      512x512x16 requests inside the mix; the plain path's latencies for the same stream are
-      replayed from its measured per-request service times."""
+      512x512x16 requests inside the mix, on a second engine with the same settings but 4M-path
+      waves (Engine.SERVING_WAVE_PATHS: the latency setting); the plain path's latencies for the
+      same stream are replayed from its measured per-request service times."""
     from pathtracer.engine import Engine
     from pathtracer.serving import (Server, build_scene, closed_loop, percentiles, replay_latencies,
                                     request_stream)
     t0 = time.perf_counter()
     worlds = {n: build_scene(n) for n in MIX_SCENES}
     build_s = time.perf_counter() - t0
-    eng = Engine.tuned(hbm_budget_bytes=150 << 30)
+    eng = Engine.tuned(hbm_budget_bytes=100 << 30)
     server = Server(eng, worlds)
+    serve_eng = Engine.tuned(hbm_budget_bytes=100 << 30, wave_paths=Engine.SERVING_WAVE_PATHS)
+    serve_server = Server(serve_eng, worlds, full=server.full)
     reqs = request_stream(1000.0, jobs / 1000.0 * 2.0 + 1.0, MIX_SCENES, seed=4, progressive_fraction=0.0)[:jobs]
-    warm = [eng.submit(server.scene_ids[r.scene], server.camera(r.scene, r), r.width, r.height, r.samples,
-                       r.max_bounces) for r in reqs[:8]]  # graph capture, layouts
-    eng.wait_idle(timeout_ms=0)
-    eng.poll(timeout_ms=0)  # take the warm-up jobs' completion reports
-    for j in warm:
-        eng.release(j)
+    for e, s in ((eng, server), (serve_eng, serve_server)):
+        warm = [e.submit(s.scene_ids[r.scene], s.camera(r.scene, r), r.width, r.height, r.samples,
+                         r.max_bounces) for r in reqs[:8]]  # graph capture, layouts
+        e.wait_idle(timeout_ms=0)
+        e.poll(timeout_ms=0)  # take the warm-up jobs' completion reports
+        for j in warm:
+            e.release(j)
     batch = {mode: closed_loop(server, reqs, mode) for mode in ("engine", "wavefront", "plain")}
     samples = batch["plain"]["samples"]
     stream = request_stream(rate, seconds, MIX_SCENES, seed=5, progressive_fraction=0.1, fixed=(512, 512, 16, 8),
                             fixed_share=0.2)
-    g0 = eng.stats()["gpu_ms"]
-    res = server.run(stream)
-    busy = (eng.stats()["gpu_ms"] - g0) / 1e3 / res.wall_s
+    g0 = serve_eng.stats()["gpu_ms"]
+    res = serve_server.run(stream)
+    busy = (serve_eng.stats()["gpu_ms"] - g0) / 1e3 / res.wall_s
+    serve_eng.close()
     # the plain path on the same stream (refinements as fresh renders of their samples)
     plain_all = closed_loop(server, stream, "plain")
     plain_lat = replay_latencies(stream, plain_all["service_s"])
@@ -330,6 +335,7 @@ def mixed_stream_report(seconds: float = 10.0, rate: float = 50.0, jobs: int = 2
                     f"({samples} samples); serving: Poisson {rate:g} req/s for {seconds:g} s, 10% progressive, "
                     f"20% 512x512x16 spp depth 8",
         "engine": eng_config_of(Engine.tuned_config()),
+        "serving_engine": eng_config_of(dict(Engine.tuned_config(), wave_paths=Engine.SERVING_WAVE_PATHS)),
         "batching_samples_per_s": rate_of,
         "engine_over_plain": rate_of["engine"] / rate_of["plain"],
         "wavefront_over_plain": rate_of["wavefront"] / rate_of["plain"],
@@ -589,8 +595,6 @@ def run_ours(args):
         pg.barrier()
     torch.cuda.synchronize()
     tracer.synchronize()
-    tracer.reset_kernel_times()
-    tracer.set_profiling(True)
     launches0 = tracer.launch_count()
     with ClockSampler(local_rank) as clocks:
         start.record(stream)
@@ -601,8 +605,20 @@ def run_ours(args):
         torch.cuda.synchronize()
     elapsed_ms = start.elapsed_time(stop)
     launches = tracer.launch_count() - launches0
+    # per-kernel times from a separate instrumented pass: with profiling on, the
+    # library runs the stages one after another (no overlap of consecutive groups
+    # or of a bounce's shadow stage), so each launch's CUDA-event time is its own
+    prof_steps = min(args.steps, 3)
+    tracer.reset_kernel_times()
+    tracer.set_profiling(True)
+    for _ in range(prof_steps):
+        step()
+    tracer.synchronize()
     times = tracer.kernel_times()
     tracer.set_profiling(False)
+    for k in times.launches:  # per image
+        times.launches[k] = times.launches[k] * args.steps // prof_steps
+        times.milliseconds[k] = times.milliseconds[k] * args.steps / prof_steps
     elapsed_ms = max_over_ranks(elapsed_ms, pg, "cuda")
     if pg:
         pg.barrier()
@@ -621,7 +637,9 @@ def run_ours(args):
                 "traffic": TRAFFIC_PER_LAUNCH.get((args.kernel, cls, args.precision))
                 if WORKLOAD == "procedural" and WIDTH * HEIGHT * spp == 1920 * 1080 * 64 else None, "kernel": cls,
                 "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
-                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs), of measured" if peaks else "fallback 6.8 TB/s"}
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs), of measured" if peaks else "fallback 6.8 TB/s",
+                "launch_timing": f"CUDA events around each launch on its stream, {prof_steps} instrumented steps "
+                                 "after the timed ones, stages serialised (no overlap between groups)"}
 
     # image error of the step's image (its accumulation holds samples 1..spp)
     # against the FP64 reference render of the same paths on the GPU

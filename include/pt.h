@@ -264,19 +264,26 @@ const char* pt_last_error(const pt_ctx* ctx);
 /* select PT_KERNEL_WAVEFRONT or PT_KERNEL_PLAIN; both give identical bits */
 int pt_set_kernel(pt_ctx* ctx, int kernel);
 
-/* the cudaStream_t the context launches on (for CUDA-event timing by callers) */
+/* the cudaStream_t the context launches on (for CUDA-event timing by callers).
+ * The wavefront kernels of a pt_trace run on streams of the library that
+ * join this one: work queued here after a pt_trace call runs after that
+ * call's samples are accumulated. */
 int pt_get_stream(pt_ctx* ctx, void** stream);
 
 /* --------------------------------------------------------- instrumentation */
 
-/* per-kernel timing with CUDA events on the context stream (0 = off) */
-#define PT_KERNEL_CLASS_COUNT 6
+/* per-kernel timing with CUDA events (0 = off).  While it is on, the
+ * wavefront stages of pt_trace run one after another (consecutive groups and
+ * a bounce's shadow stage otherwise overlap), so each kernel's time is its
+ * own; the total time of a trace is then longer than with profiling off. */
+#define PT_KERNEL_CLASS_COUNT 7
 #define PT_KC_RAYGEN 0
 #define PT_KC_EXTEND 1
 #define PT_KC_SHADE 2
 #define PT_KC_SHADOW 3
 #define PT_KC_ACCUMULATE 4
 #define PT_KC_PLAIN 5
+#define PT_KC_SORT 6 /* ray and hit ordering of the wavefront method */
 int pt_set_profiling(pt_ctx* ctx, int enabled);
 /* per class: launches and summed milliseconds since the last reset */
 int pt_get_kernel_times(pt_ctx* ctx, uint64_t launches[PT_KERNEL_CLASS_COUNT],

@@ -507,7 +507,8 @@ int trace_impl(pt_ctx* c, uint32_t samples, uint32_t* traced, pt_path_record* ho
         const ptw::Timer timer = [c](int cls, cudaStream_t s, const std::function<cudaError_t()>& f) {
             return c->timed(cls, s, f);
         };
-        rc = c->cuda(ptw::trace(c->wavefront, w, t, first, n, ptk::Sinks{rec, tot}, c->stream, timer, form, overlap),
+        rc = c->cuda(ptw::trace(c->wavefront, w, t, first, n, ptk::Sinks{rec, tot}, c->stream, timer, form, overlap,
+                                c->profiling),
                      "wavefront trace");
         if (rc) return rc;
         c->precision_active = form;

@@ -53,9 +53,13 @@ uint32_t effective_precision(const ptd::World& w, uint32_t precision, bool recor
 // any later work there sees the finished samples in order.  `overlap`: no
 // work was queued on `stream` since the previous call's groups began, so this
 // call's groups may start where those did (otherwise they wait for `stream`).
+// Within a group, a bounce's shadow rays are traced on a second stream beside
+// the next bounce's extend stage.  `serial`: no overlap at all (each group
+// starts after the previous one's accumulation, each stage after the one
+// before), so that the timer sees every kernel alone.
 cudaError_t trace(Wavefront* wf, const ptd::World& w, const ptk::Tile& tile, uint32_t first_sample,
                   uint32_t samples, ptk::Sinks sinks, cudaStream_t stream, const Timer& timer, uint32_t precision,
-                  bool overlap);
+                  bool overlap, bool serial);
 
 // the narrow copies of the precision form, on `stream`: FP32 attributes ->
 // pt_half_attribute records (8 uint2 each), RGBA32F texels -> BF16 RGBA

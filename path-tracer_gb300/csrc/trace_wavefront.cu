@@ -91,15 +91,26 @@ __global__ void __launch_bounds__(256) raygen_kernel(World w, ptk::Tile t, Group
     }
 }
 
-__global__ void bounce_reset_kernel(uint32_t* cnt, int next) {
+// counters of one bounce: the next ray queue, the extend fetch, the hit and
+// miss lists, the sort and order flags (shadow: true also the shadow queue,
+// its fetch counter and order flag)
+__global__ void bounce_reset_kernel(uint32_t* cnt, int next, bool shadow) {
     cnt[next] = 0u;
-    cnt[2] = 0u;
     cnt[3] = 0u;
-    cnt[4] = 0u;
     cnt[5] = 0u;
     cnt[6] = 0u;
     cnt[7] = 0u;
     cnt[8] = 0u;
+    if (shadow) {
+        cnt[2] = 0u;
+        cnt[4] = 0u;
+        cnt[9] = 0u;
+    }
+}
+// the shadow queue's counters alone (before the shading kernel appends to it)
+__global__ void shadow_reset_kernel(uint32_t* cnt) {
+    cnt[2] = 0u;
+    cnt[4] = 0u;
     cnt[9] = 0u;
 }
 
@@ -403,6 +414,12 @@ struct Buf {
 
 constexpr uint64_t kMaxPaths = 1ull << 25;  // paths in flight per group
 
+// 1: a group's shadow stage runs on a second stream of its lane, beside the
+// next bounce's extend stage
+#ifndef PT_SHADOW_SIDE
+#define PT_SHADOW_SIDE 1
+#endif
+
 #define PTW_TRY(x)                          \
     do {                                    \
         const cudaError_t e_ = (x);         \
@@ -411,6 +428,13 @@ constexpr uint64_t kMaxPaths = 1ull << 25;  // paths in flight per group
 
 }  // namespace
 
+// the second stream of a lane for the shadow stage, with its two events
+struct ShadowSide {
+    cudaStream_t stream;
+    cudaEvent_t shaded;  // a bounce's shading finished (recorded on the group's stream)
+    cudaEvent_t traced;  // its shadow rays finished (recorded on `stream`)
+};
+
 // The queues of one group of paths and the stream it runs on.  Two lanes let
 // consecutive groups overlap: one group's last bounces (few, long rays that
 // leave most SMs idle) run beside the next group's first ones.
@@ -418,6 +442,7 @@ struct Lane {
     Buf o[2], d[2], T[2], hit, color, so, sd, sc, cnt;
     Buf lists;  // hit list, miss list, sorted hit list (capacity entries each), sort counts and offsets
     cudaStream_t stream = nullptr;
+    ShadowSide side{};            // the stream the lane's shadow stage runs on (PT_SHADOW_SIDE)
     cudaEvent_t done = nullptr;   // the lane's group finished (recorded on the lane)
     cudaEvent_t freed = nullptr;  // its accumulation consumed the colours (recorded on the caller's stream)
     bool pending = false;         // `freed` was recorded and not yet waited for
@@ -454,6 +479,9 @@ int create(Wavefront** out) {
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.freed, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&l.side.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.side.shaded, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.side.traced, cudaEventDisableTiming);
     }
     *out = wf;
     return e == cudaSuccess ? 0 : (int)e;
@@ -466,8 +494,12 @@ void destroy(Wavefront* wf) {
         for (Buf* b : {&l.o[0], &l.o[1], &l.d[0], &l.d[1], &l.T[0], &l.T[1], &l.hit, &l.color, &l.so, &l.sd, &l.sc,
                        &l.cnt, &l.lists})
             b->release();
+        if (l.side.stream) cudaStreamSynchronize(l.side.stream);
         if (l.done) cudaEventDestroy(l.done);
         if (l.freed) cudaEventDestroy(l.freed);
+        if (l.side.shaded) cudaEventDestroy(l.side.shaded);
+        if (l.side.traced) cudaEventDestroy(l.side.traced);
+        if (l.side.stream) cudaStreamDestroy(l.side.stream);
         if (l.stream) cudaStreamDestroy(l.stream);
     }
     if (wf->start) cudaEventDestroy(wf->start);
@@ -580,7 +612,7 @@ template <bool kRec, bool kAlpha, bool kTri36, bool kWide = false, class TimerF>
 cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const ptd::Queues& q,
                       const ptk::Tile& tile, const ptd::Group& g, ptk::Sinks sinks, cudaStream_t stream,
                       TimerF&& timer, const SortCfg& sort = SortCfg(), cudaStream_t acc_stream = nullptr,
-                      cudaEvent_t done = nullptr) {
+                      cudaEvent_t done = nullptr, const ShadowSide* side = nullptr) {
     using namespace ptd;
     const int ext_blocks = sms * occupancy(extend_kernel<kRec, kAlpha, kTri36, kWide>, kExtendThreads);
     const int sha_blocks = sms * occupancy(shade_kernel<kRec, kAlpha>, kShadeThreads);
@@ -600,19 +632,23 @@ cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const pt
                                                                   q.hit_sorted, sort.min_hits);
         return cudaGetLastError();
     };
+    // With `side`, bounce k's shadow rays are traced on side->stream while
+    // bounce k + 1's extend (and hit sort) run: neither touches what the other
+    // reads or writes.  Bounce k + 1's shading waits for them (it adds to the
+    // same path colours, in the reference's order, and refills the shadow queue).
+    const bool split = side != nullptr && !kAlpha;
     for (uint32_t bounce = 0; bounce <= tile.max_bounces; ++bounce) {
-        bounce_reset_kernel<<<1, 1, 0, stream>>>(q.cnt, cur ^ 1);
+        bounce_reset_kernel<<<1, 1, 0, stream>>>(q.cnt, cur ^ 1, !split);
         PTW_TRY(cudaGetLastError());
         if (PT_RAY_ORDER && sorting && bounce > 0) {  // camera rays are coherent already (pixel-major)
-            // timed with the sorts (shading class), as the hit sort
-            PTW_TRY(timer(PT_KC_SHADE, stream, [&] { return order_rays(cur ? q.d[1] : q.d[0], q.cnt + cur, 8u); }));
+            PTW_TRY(timer(PT_KC_SORT, stream, [&] { return order_rays(cur ? q.d[1] : q.d[0], q.cnt + cur, 8u); }));
         }
         PTW_TRY(timer(PT_KC_EXTEND, stream, [&] {
             extend_kernel<kRec, kAlpha, kTri36, kWide><<<ext_blocks, kExtendThreads, 0, stream>>>(w, f, q, cur, bounce);
             return cudaGetLastError();
         }));
         if (sort.counts && sort.min_hits != 0xffffffffu) {
-            PTW_TRY(timer(PT_KC_SHADE, stream, [&] {
+            PTW_TRY(timer(PT_KC_SORT, stream, [&] {
                 sort_count_kernel<PT_SORT_KEY><<<sms * 4, kSortThreads, 0, stream>>>(w, q, sort.counts, sort.min_hits,
                                                                                     sort.tri_shift);
                 sort_scan_kernel<0><<<1, 1024, 0, stream>>>(q, sort.counts, sort.counts + kSortBuckets, sort.min_hits);
@@ -621,21 +657,33 @@ cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const pt
                 return cudaGetLastError();
             }));
         }
+        if (split) {
+            if (bounce > 0) PTW_TRY(cudaStreamWaitEvent(stream, side->traced, 0));
+            shadow_reset_kernel<<<1, 1, 0, stream>>>(q.cnt);
+            PTW_TRY(cudaGetLastError());
+        }
         PTW_TRY(timer(PT_KC_SHADE, stream, [&] {
             shade_kernel<kRec, kAlpha><<<sha_blocks, kShadeThreads, 0, stream>>>(w, f, q, cur, bounce, tile.max_bounces);
             return cudaGetLastError();
         }));
         if constexpr (!kAlpha) {
             if (PT_SHADOW_ORDER && sorting) {
-                PTW_TRY(timer(PT_KC_SHADE, stream, [&] { return order_rays(q.sd, q.cnt + 2, 9u); }));
+                PTW_TRY(timer(PT_KC_SORT, stream, [&] { return order_rays(q.sd, q.cnt + 2, 9u); }));
             }
-            PTW_TRY(timer(PT_KC_SHADOW, stream, [&] {
-                shadow_kernel<kRec, kTri36, kWide><<<shd_blocks, kExtendThreads, 0, stream>>>(w, f, q);
+            const cudaStream_t ss = split ? side->stream : stream;
+            if (split) {
+                PTW_TRY(cudaEventRecord(side->shaded, stream));
+                PTW_TRY(cudaStreamWaitEvent(ss, side->shaded, 0));
+            }
+            PTW_TRY(timer(PT_KC_SHADOW, ss, [&] {
+                shadow_kernel<kRec, kTri36, kWide><<<shd_blocks, kExtendThreads, 0, ss>>>(w, f, q);
                 return cudaGetLastError();
             }));
+            if (split) PTW_TRY(cudaEventRecord(side->traced, ss));
         }
         cur ^= 1;
     }
+    if (split) PTW_TRY(cudaStreamWaitEvent(stream, side->traced, 0));  // the last bounce's shadow rays
     const cudaStream_t as = acc_stream ? acc_stream : stream;
     if (as != stream) {
         PTW_TRY(cudaEventRecord(done, stream));
@@ -655,7 +703,8 @@ cudaError_t run_group(int sms, const ptd::World& w, const ptd::Fast& f, const pt
 }  // namespace
 
 cudaError_t trace(Wavefront* wf, const ptd::World& w_in, const ptk::Tile& tile, uint32_t first, uint32_t samples,
-                  ptk::Sinks sinks, cudaStream_t stream, const Timer& timer, uint32_t precision, bool overlap) {
+                  ptk::Sinks sinks, cudaStream_t stream, const Timer& timer, uint32_t precision, bool overlap,
+                  bool serial) {
     precision = effective_precision(w_in, precision, sinks.any());
     ptd::World w = w_in;
     if (precision & PT_PRECISION_HALF_ATTRIBUTES) {
@@ -705,11 +754,11 @@ cudaError_t trace(Wavefront* wf, const ptd::World& w_in, const ptk::Tile& tile, 
         const cudaStream_t gs = record ? stream : l.stream;
         if (!record) {
             wf->next_lane ^= 1;
-            if (!(overlap && wf->have_start)) {
+            if (serial || !(overlap && wf->have_start)) {
                 PTW_TRY(cudaEventRecord(wf->start, stream));
                 wf->have_start = true;
             }
-            overlap = true;  // the call's later groups start from the same point
+            overlap = true;  // the call's later groups start from the same point (unless serial)
             PTW_TRY(cudaStreamWaitEvent(gs, wf->start, 0));
             if (l.pending) PTW_TRY(cudaStreamWaitEvent(gs, l.freed, 0));
         }
@@ -735,15 +784,17 @@ cudaError_t trace(Wavefront* wf, const ptd::World& w_in, const ptk::Tile& tile, 
         sort.min_hits = PT_SORT_MIN_HITS;
         while (((uint64_t)ptd::kSortBuckets << sort.tri_shift) < wf->tri_count && sort.tri_shift < 31u) sort.tri_shift += 1u;
         const cudaStream_t as = record ? nullptr : stream;
+        const ShadowSide* side = (!record && !serial && PT_SHADOW_SIDE) ? &l.side : nullptr;
         cudaError_t e;
         if (record)
             e = w.any_alpha ? run_group<true, true, false>(wf->sms, w, f, q, tile, g, sinks, gs, timer)
                             : run_group<true, false, false>(wf->sms, w, f, q, tile, g, sinks, gs, timer);
         else if (wide)
-            e = run_group<false, false, false, true>(wf->sms, w, f, q, tile, g, sinks, gs, timer, sort, as, l.done);
+            e = run_group<false, false, false, true>(wf->sms, w, f, q, tile, g, sinks, gs, timer, sort, as, l.done, side);
         else
             e = w.any_alpha ? run_group<false, true, false>(wf->sms, w, f, q, tile, g, sinks, gs, timer, sort, as, l.done)
-                            : run_group<false, false, false>(wf->sms, w, f, q, tile, g, sinks, gs, timer, sort, as, l.done);
+                            : run_group<false, false, false>(wf->sms, w, f, q, tile, g, sinks, gs, timer, sort, as, l.done,
+                                                             side);
         PTW_TRY(e);
         if (!record) {
             PTW_TRY(cudaEventRecord(l.freed, stream));

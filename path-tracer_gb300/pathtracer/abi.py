@@ -44,8 +44,8 @@ PT_PRECISION_WIDE_BVH = 1
 PT_PRECISION_HALF_ATTRIBUTES = 2
 PT_PRECISION_KAHAN = 4
 PT_PRECISION_COMPRESSED = 7
-PT_KERNEL_CLASS_COUNT = 6
-KERNEL_CLASSES = ["raygen", "extend", "shade", "shadow", "accumulate", "plain"]
+PT_KERNEL_CLASS_COUNT = 7
+KERNEL_CLASSES = ["raygen", "extend", "shade", "shadow", "accumulate", "plain", "sort"]
 PT_RECORD_MAX_BOUNCES = 17
 COUNT_FIELDS = ["extend_rays", "shadow_rays", "interior_visits", "leaf_visits", "triangle_tests",
                 "shadow_interior_visits", "shadow_leaf_visits", "shadow_triangle_tests", "rand_draws",

@@ -24,9 +24,20 @@ class Engine:
         10k,100k,1M,4M --precision compressed --autotune --save-tuned`)."""
         return json.loads(TUNED.read_text())["config"]
 
+    # Wave size for latency-bound serving.  A wave holds the paths the engine traces per launch
+    # sequence; a request arriving while one is in flight waits for it.  On the serving stream of
+    # the mixed workload (Poisson 50 req/s, a fifth of them 512x512 x 16 spp = 4.2M paths) the
+    # 512x512 requests' p99 latency was 54 / 45 ms with 8M-path waves (the batching optimum),
+    # 37 / 35 ms with 4M-path waves and 56 / 49 ms with 2M-path waves (two arrival seeds; more
+    # waves per request cost more than the shorter wait saves); the GPU is about 45 % busy there,
+    # so the smaller waves cost no throughput.
+    SERVING_WAVE_PATHS = 4 << 20
+
     @classmethod
-    def tuned(cls, device: int = 0, hbm_budget_bytes: int = 0) -> "Engine":
-        cfg = cls.tuned_config()
+    def tuned(cls, device: int = 0, hbm_budget_bytes: int = 0, **overrides) -> "Engine":
+        """An engine with the autotuned settings; keyword arguments replace single settings
+        (e.g. wave_paths=Engine.SERVING_WAVE_PATHS for a latency-bound server)."""
+        cfg = dict(cls.tuned_config(), **overrides)
         return cls(device=device, hbm_budget_bytes=hbm_budget_bytes, wave_paths=cfg["wave_paths"],
                    tile_size=cfg["tile_size"], steps_per_refill=cfg["steps_per_refill"], use_graphs=True,
                    precision=cfg["precision"], sort_min_hits=cfg["sort_min_hits"],

@@ -92,10 +92,12 @@ def request_stream(rate: float, duration: float, scenes: list[str], seed: int = 
 class Server:
     """Admission + continuous batching on one engine; scenes cached by content hash."""
 
-    def __init__(self, engine: Engine, worlds: dict[str, pt.World]):
+    def __init__(self, engine: Engine, worlds: dict[str, pt.World], full: dict | None = None):
+        """full: the worlds' full updates, when another server took them already (they stay valid
+        only until the next take_updates of a world, i.e. until the first camera() call)."""
         self.engine = engine
         self.worlds = worlds
-        self.full = {name: w.take_updates() for name, w in worlds.items()}
+        self.full = full if full is not None else {name: w.take_updates() for name, w in worlds.items()}
         self.scene_ids = {name: engine.add_scene(u) for name, u in self.full.items()}
         self._last = {name: abi.Camera.from_buffer_copy(u.camera.contents) for name, u in self.full.items()}
 
