@@ -257,6 +257,14 @@ def main(argv=None) -> None:
     p.add_argument("--duration", type=float, default=10.0, help="seconds of arrivals")
     p.add_argument("--scenes", default="10k,100k,1M")
     p.add_argument("--fixed", default="", help="W,H,SPP,DEPTH: every request this shape (e.g. 512,512,16,8)")
+    p.add_argument("--fixed-share", type=float, default=1.0,
+                   help="with --fixed: the share of the requests of that shape (the others follow the mix)")
+    p.add_argument("--tuned", action="store_true",
+                   help="the engine settings of pathtracer/engine_tuned.json (their precision form replaces "
+                        "--precision)")
+    p.add_argument("--wave-paths", type=int, default=0, help="paths per wave (0: the engine's or the tuned value)")
+    p.add_argument("--warmup", type=int, default=8,
+                   help="requests of another seed rendered before the stream (graph capture, buffer layouts)")
     p.add_argument("--progressive", type=float, default=0.1)
     p.add_argument("--budget-gb", type=float, default=150.0)
     p.add_argument("--seed", type=int, default=1)
@@ -278,7 +286,15 @@ def main(argv=None) -> None:
     build_s = time.perf_counter() - t
     precision = {"fp32": abi.PT_PRECISION_FP32, "wide": abi.PT_PRECISION_WIDE_BVH,
                  "compressed": abi.PT_PRECISION_COMPRESSED}[args.precision]
-    eng = Engine(hbm_budget_bytes=int(args.budget_gb * (1 << 30)), precision=precision)
+    budget = int(args.budget_gb * (1 << 30))
+    if args.tuned:
+        over = {"wave_paths": args.wave_paths} if args.wave_paths else {}
+        eng = Engine.tuned(hbm_budget_bytes=budget, **over)
+        args.precision = {abi.PT_PRECISION_FP32: "fp32", abi.PT_PRECISION_WIDE_BVH: "wide",
+                          abi.PT_PRECISION_COMPRESSED: "compressed"}.get(Engine.tuned_config()["precision"],
+                                                                         args.precision)
+    else:
+        eng = Engine(hbm_budget_bytes=budget, precision=precision, wave_paths=args.wave_paths)
     server = Server(eng, worlds)
     fixed = tuple(int(x) for x in args.fixed.split(",")) if args.fixed else None
     if args.compare:
@@ -304,7 +320,16 @@ def main(argv=None) -> None:
         print(json.dumps(out))
         eng.close()
         return
-    reqs = request_stream(args.rate, args.duration, names, args.seed, args.progressive, fixed)
+    if args.warmup > 0:
+        warm = request_stream(1000.0, args.warmup / 1000.0 * 2.0 + 1.0, names, args.seed + 1000, 0.0)[:args.warmup]
+        ids = [eng.submit(server.scene_ids[r.scene], server.camera(r.scene, r), r.width, r.height, r.samples,
+                          r.max_bounces) for r in warm]
+        eng.wait_idle(timeout_ms=0)
+        eng.poll(timeout_ms=0)
+        for j in ids:
+            eng.release(j)
+    reqs = request_stream(args.rate, args.duration, names, args.seed, args.progressive, fixed,
+                          fixed_share=args.fixed_share)
     res = server.run(reqs)
     st = eng.stats()
     print(json.dumps({
@@ -313,6 +338,7 @@ def main(argv=None) -> None:
         "latency_512x512x16_ms": percentiles(res.latencies_512_16_ms),
         "samples_per_s": res.paths / res.wall_s, "wall_s": res.wall_s, "gpu_ms": st["gpu_ms"],
         "waves": st["waves"], "scene_build_s": build_s, "engine_precision": args.precision,
+        "wave_paths": st["wave_paths"],
         "triangles": {n: worlds[n].triangle_count() for n in names},
     }))
     eng.close()
