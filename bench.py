@@ -53,9 +53,9 @@ WORKLOADS = {
 WORKLOAD = "procedural"
 METRIC = "Mrays/s"
 KERNEL_NAMES = {"wavefront": 0, "plain": 1}
-# include/pt_precision.h: FP32 (the reference's buffers), 8-wide quantised BVH only, or the full
-# compressed form (wide BVH + FP16 attributes / BF16 skybox + Kahan sums)
-PRECISIONS = {"fp32": 0, "wide": 1, "compressed": 7}
+# include/pt_precision.h: FP32 (the reference's buffers), 8-wide quantised BVH only, FP16 attributes /
+# BF16 skybox + Kahan sums on the binary BVH, or the full compressed form (all three)
+PRECISIONS = {"fp32": 0, "wide": 1, "half": 6, "compressed": 7}
 # DRAM bytes (read + write) per launch of the dominant kernel on this workload
 # (1920x1080, 64 spp, FP32 form), measured by a single-pass ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum) of the first 16-spp group's
@@ -289,14 +289,14 @@ def mixed_stream_report(seconds: float = 10.0, rate: float = 50.0, jobs: int = 2
       {1,4,16,64}, max_bounces 4-12, random camera poses) rendered back to back: samples/s through
       the plain kernel (one pt_trace of <= 16 samples per call, the host waiting on each call:
       the reference's dispatch shape, FP32), the wavefront kernels one job per call (FP32), and the
-      batched engine in the compressed form with the settings its autotuner chose
-      (pathtracer/engine_tuned.json).
+      batched engine in the form and with the settings its autotuner run chose
+      (pathtracer/engine_tuned.json: FP16 attributes / BF16 skybox + Kahan sums on the binary BVH).
     * serving: Poisson arrivals at `rate` req/s for `seconds` s, 10 % progressive refinements, a
       fifth of the requests 512x512 x 16 spp x max_bounces 8; latency from arrival to result
-      through the serving loop (continuous batching) on the same engine, overall and for the
-      512x512x16 requests inside the mix, on a second engine with the same settings but 4M-path
-      waves (Engine.SERVING_WAVE_PATHS: the latency setting); the plain path's latencies for the
-      same stream are replayed from its measured per-request service times."""
+      through the serving loop (continuous batching), overall and for the 512x512x16 requests
+      inside the mix, on a second engine with the same settings but 4M-path waves
+      (Engine.SERVING_WAVE_PATHS: the latency setting); the plain path's latencies for the same
+      stream are replayed from its measured per-request service times."""
     from pathtracer.engine import Engine
     from pathtracer.serving import (Server, build_scene, closed_loop, percentiles, replay_latencies,
                                     request_stream)

@@ -19,9 +19,11 @@ class Engine:
 
     @staticmethod
     def tuned_config() -> dict:
-        """The engine settings pte_autotune chose for the compressed form on the batching mix
-        (engine_tuned.json, written by `python -m pathtracer.serving --compare 256 --scenes
-        10k,100k,1M,4M --precision compressed --autotune --save-tuned`)."""
+        """The engine settings pte_autotune chose on the batching mix, in the FP16-attribute form
+        (FP16 attributes / BF16 skybox + Kahan sums on the binary BVH: 608 Msamples/s there against
+        570 for the full compressed form with the 8-wide BVH); engine_tuned.json, written by
+        `python -m pathtracer.serving --compare 256 --scenes 10k,100k,1M,4M --precision half
+        --autotune --save-tuned`."""
         return json.loads(TUNED.read_text())["config"]
 
     # Wave size for latency-bound serving.  A wave holds the paths the engine traces per launch
@@ -46,7 +48,8 @@ class Engine:
     def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, wave_paths: int = 0, tile_size: int = 0,
                  steps_per_refill: int = 0, use_graphs: bool = True, precision: int = 0, sort_min_hits: int = 0,
                  traversal_threads: int = 0, shade_threads: int = 0):
-        """precision: PT_PRECISION_* bits (0 = the reference's FP32 buffers, 7 = the compressed form);
+        """precision: PT_PRECISION_* bits (0 = the reference's FP32 buffers, 6 = FP16 attributes / BF16
+        skybox + Kahan sums, 7 = those and the 8-wide BVH: the compressed form);
         sort_min_hits: hits of a bounce are sorted by triangle bucket before shading from this many on
         (0 = the default 65536, 0xffffffff = never); traversal_threads / shade_threads: threads per block
         of the traversal kernels (64, 128 or 256; 0 = 128) and of the shading kernel (128, 256, 512 or 1024;

@@ -268,9 +268,9 @@ def main(argv=None) -> None:
     p.add_argument("--progressive", type=float, default=0.1)
     p.add_argument("--budget-gb", type=float, default=150.0)
     p.add_argument("--seed", type=int, default=1)
-    p.add_argument("--precision", choices=["fp32", "wide", "compressed"], default="fp32",
-                   help="engine form: the reference's FP32 buffers, the 8-wide BVH, or the compressed form "
-                        "(8-wide BVH + FP16 attributes / BF16 skybox + Kahan sums)")
+    p.add_argument("--precision", choices=["fp32", "wide", "half", "compressed"], default="fp32",
+                   help="engine form: the reference's FP32 buffers, the 8-wide BVH, FP16 attributes / BF16 skybox "
+                        "+ Kahan sums on the binary BVH, or the compressed form (all three)")
     p.add_argument("--autotune", action="store_true",
                    help="with --compare: let the engine's autotuner pick wave size, tile size, refill steps, the "
                         "hit-sort threshold and the kernels' block shapes on 16 of the requests first")
@@ -284,15 +284,15 @@ def main(argv=None) -> None:
     t = time.perf_counter()
     worlds = {n: build_scene(n) for n in names}
     build_s = time.perf_counter() - t
-    precision = {"fp32": abi.PT_PRECISION_FP32, "wide": abi.PT_PRECISION_WIDE_BVH,
-                 "compressed": abi.PT_PRECISION_COMPRESSED}[args.precision]
+    forms = {"fp32": abi.PT_PRECISION_FP32, "wide": abi.PT_PRECISION_WIDE_BVH,
+             "half": abi.PT_PRECISION_HALF_ATTRIBUTES | abi.PT_PRECISION_KAHAN,
+             "compressed": abi.PT_PRECISION_COMPRESSED}
+    precision = forms[args.precision]
     budget = int(args.budget_gb * (1 << 30))
     if args.tuned:
         over = {"wave_paths": args.wave_paths} if args.wave_paths else {}
         eng = Engine.tuned(hbm_budget_bytes=budget, **over)
-        args.precision = {abi.PT_PRECISION_FP32: "fp32", abi.PT_PRECISION_WIDE_BVH: "wide",
-                          abi.PT_PRECISION_COMPRESSED: "compressed"}.get(Engine.tuned_config()["precision"],
-                                                                         args.precision)
+        args.precision = {v: k for k, v in forms.items()}.get(Engine.tuned_config()["precision"], args.precision)
     else:
         eng = Engine(hbm_budget_bytes=budget, precision=precision, wave_paths=args.wave_paths)
     server = Server(eng, worlds)

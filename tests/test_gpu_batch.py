@@ -266,17 +266,19 @@ def test_autotune_picks_a_candidate(scenes):
     eng.close()
 
 
-def test_compressed_engine_equals_alone(scenes):
-    """The precision form in the engine (8-wide BVH, FP16 attributes, BF16 sky, Kahan) gives each job
-    the bits pt_trace gives it alone in the same form."""
-    eng = Engine(wave_paths=1 << 15, tile_size=16, precision=abi.PT_PRECISION_COMPRESSED)
+@pytest.mark.parametrize("form", [abi.PT_PRECISION_COMPRESSED,
+                                  abi.PT_PRECISION_HALF_ATTRIBUTES | abi.PT_PRECISION_KAHAN])
+def test_compressed_engine_equals_alone(scenes, form):
+    """The precision forms in the engine (8-wide BVH, FP16 attributes, BF16 sky, Kahan; or all but the
+    8-wide BVH) give each job the bits pt_trace gives it alone in the same form."""
+    eng = Engine(wave_paths=1 << 15, tile_size=16, precision=form)
     ids = {name: eng.add_scene(scenes.full[name]) for name in scenes.full}
     cams = [scenes.camera(n, w, h, yaw) for n, w, h, _, _, yaw in JOBS[:3]]
     jobs = [eng.submit(ids[n], cam, w, h, spp, b) for (n, w, h, spp, b, _), cam in zip(JOBS[:3], cams)]
     eng.wait_idle(timeout_ms=300000)
     for (n, w, h, spp, b, _), cam, jid in zip(JOBS[:3], cams, jobs):
         tr = pt.PathTracer(scenes.updates_with_camera(n, cam), (w, h))
-        tr.set_precision(abi.PT_PRECISION_COMPRESSED)
+        tr.set_precision(form)
         tr.set_max_bounces(b)
         tr.set_tile((w, h), (0, 0), (w, h))
         done = 0

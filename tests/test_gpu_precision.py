@@ -148,7 +148,8 @@ def test_compressed_rmse_vs_fp64():
     rad64, _ = oracle.trace_paths(ow, image, 8, px, 1, spp, precision=64)
     ref = rad64.mean(axis=0).reshape(size[1], size[0], 3)
     errs = {}
-    for prec in (abi.PT_PRECISION_FP32, abi.PT_PRECISION_COMPRESSED):
+    half = abi.PT_PRECISION_HALF_ATTRIBUTES | abi.PT_PRECISION_KAHAN
+    for prec in (abi.PT_PRECISION_FP32, half, abi.PT_PRECISION_COMPRESSED):
         tr = pt.PathTracer(u, size)
         tr.set_precision(prec)
         tr.set_max_bounces(8)
@@ -160,8 +161,10 @@ def test_compressed_rmse_vs_fp64():
         acc = tr.read_tile(abi.PT_TILE_ACCUMULATION)[..., :3].astype(np.float64) / spp
         errs[prec] = np.sqrt(np.mean((acc - ref) ** 2)) / np.sqrt(np.mean(ref ** 2))
         tr.close()
-    print(f"relative RMSE vs FP64 oracle at {spp} spp: FP32 {errs[0]:.3e}, compressed {errs[7]:.3e}")
+    print(f"relative RMSE vs FP64 oracle at {spp} spp: FP32 {errs[0]:.3e}, FP16 attributes {errs[half]:.3e}, "
+          f"compressed {errs[7]:.3e}")
     assert errs[abi.PT_PRECISION_FP32] < 1e-3
+    assert errs[half] < 1e-2
     assert errs[abi.PT_PRECISION_COMPRESSED] < 1e-2
 
 
