@@ -318,8 +318,15 @@ PTD bool shade_hit(const World& w, uint32_t bounce, uint32_t max_bounces, PathSt
     const LightSample light = sample_light(w, next_origin, rng, c);
     const f3 lwi = mk(dot(Tn, light.direction), dot(Bn, light.direction), dot(N, light.direction));
     if constexpr (!kInlineShadow) shadow->valid = false;
+#if PT_LOBE_TERMS
+    const LobeTerms lt = lobe_terms(wo, b);
+#endif
     if (light.pdf > 0.0f && lwi.z > 0.0f && any_positive(light.emission)) {
+#if PT_LOBE_TERMS
+        const Lobes lobes = evaluate_lobes_t(wo, lwi, b, lt);
+#else
         const Lobes lobes = evaluate_lobes(wo, lwi, b);
+#endif
         const float weight = bounce < max_bounces ? power_heuristic(light.pdf, lobes.pdf) : 1.0f;
         const f3 contribution = ps.throughput * lobes.f * lwi.z * light.emission * (weight / light.pdf);
         if constexpr (kInlineShadow) {
@@ -364,7 +371,11 @@ PTD bool shade_hit(const World& w, uint32_t bounce, uint32_t max_bounces, PathSt
         wi = normalize(wu.x * b.bx + wu.y * b.by + wu.z * mk(0.0f, 0.0f, 1.0f));
     }
     if (wi.z <= 0.0f) return false;
+#if PT_LOBE_TERMS
+    const Lobes lobes = evaluate_lobes_t(wo, wi, b, lt);
+#else
     const Lobes lobes = evaluate_lobes(wo, wi, b);
+#endif
     if (lobes.pdf <= 0.0f) return false;
     ps.throughput = ps.throughput * (lobes.f * wi.z / lobes.pdf);
     ps.prev_pdf = lobes.pdf;
