@@ -65,8 +65,8 @@ TRAFFIC_PER_LAUNCH: dict = {("wavefront", "extend", "fp32"): 549.0e6}
 # of each class of one 960x540 16-spp image of this scene, over 9 launches x 8,294,400 paths; the
 # per-path work of a launch does not depend on the image size); with the launch's paths and its
 # CUDA-event time they give the fraction of the SMs' issue slots the kernel fills
-WARP_INST_PER_PATH: dict = {("wavefront", "fp32"): {"extend": 92.57, "shade": 46.09, "shadow": 32.17},
-                             ("wavefront", "compressed"): {"extend": 122.08, "shade": 46.10, "shadow": 43.96}}
+WARP_INST_PER_PATH: dict = {("wavefront", "fp32"): {"extend": 92.57, "shade": 43.85, "shadow": 32.17},
+                             ("wavefront", "compressed"): {"extend": 122.08, "shade": 43.86, "shadow": 43.96}}
 SMS, SCHEDULERS_PER_SM = 152, 4
 
 

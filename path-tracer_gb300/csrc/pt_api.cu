@@ -179,21 +179,31 @@ int copy_to(pt_ctx* c, DevBuf& buf, const void* src, size_t bytes, const char* w
 }
 
 // the BVH must be a tree reachable from node 0 whose traversal never needs
-// more than 64 deferred entries (trace.slang:632,786)
-int validate_bvh(pt_ctx* c, const pt_bvh_node* nodes, uint64_t count, uint64_t tris) {
-    if (count == 0) return c->fail(PT_ERR_INVALID_ARG, "BVH has no nodes");
+// more than 64 deferred entries (trace.slang:632,786).  Returns PT_OK or an
+// error code with *msg set; touches no context, so it may run on a helper
+// thread.
+int check_bvh(const pt_bvh_node* nodes, uint64_t count, uint64_t tris, const char** msg) {
+    if (count == 0) {
+        *msg = "BVH has no nodes";
+        return PT_ERR_INVALID_ARG;
+    }
     // one forward pass when every child follows its parent (the reference
     // builder allocates children after their parent, world.rs:1578-1583): then
-    // the graph is acyclic, and at most one parent per node makes it a tree
+    // the graph is acyclic, and at most one parent per node makes it a tree.
+    // reached[i]: 0 = no parent seen, else 1 + the node's depth
     {
-        std::vector<uint8_t> depth(count, 0), parents(count, 0);
+        std::vector<uint8_t> reached(count, 0);
+        reached[0] = 1;
         bool ordered = true;
         for (uint64_t i = 0; i < count && ordered; ++i) {
+            const uint8_t r = reached[i];
+            if (r == 0) continue;  // unreachable from the root: ignored, as by the traversal
             const pt_bvh_node& n = nodes[i];
-            if (i > 0 && parents[i] == 0) continue;  // unreachable from the root: ignored, as by the traversal
             if (n.tri_count > 0) {
-                if ((uint64_t)n.left_first + n.tri_count > tris)
-                    return c->fail(PT_ERR_INVALID_ARG, "BVH leaf triangle range outside the triangle buffer");
+                if ((uint64_t)n.left_first + n.tri_count > tris) {
+                    *msg = "BVH leaf triangle range outside the triangle buffer";
+                    return PT_ERR_INVALID_ARG;
+                }
                 continue;
             }
             const uint64_t l = n.left_first;
@@ -201,10 +211,15 @@ int validate_bvh(pt_ctx* c, const pt_bvh_node* nodes, uint64_t count, uint64_t t
                 ordered = false;  // out of order or out of range: the general walk below decides
                 break;
             }
-            if (depth[i] >= 64) return c->fail(PT_ERR_OUT_OF_LIMITS, "BVH deeper than the 64-entry traversal stack");
-            if (parents[l] || parents[l + 1]) return c->fail(PT_ERR_INVALID_ARG, "BVH node reached twice (not a tree)");
-            parents[l] = parents[l + 1] = 1;
-            depth[l] = depth[l + 1] = (uint8_t)(depth[i] + 1);
+            if (r > 64) {
+                *msg = "BVH deeper than the 64-entry traversal stack";
+                return PT_ERR_OUT_OF_LIMITS;
+            }
+            if (reached[l] | reached[l + 1]) {
+                *msg = "BVH node reached twice (not a tree)";
+                return PT_ERR_INVALID_ARG;
+            }
+            reached[l] = reached[l + 1] = (uint8_t)(r + 1);
         }
         if (ordered) return PT_OK;
     }
@@ -213,21 +228,38 @@ int validate_bvh(pt_ctx* c, const pt_bvh_node* nodes, uint64_t count, uint64_t t
     while (!st.empty()) {
         auto [i, depth] = st.back();
         st.pop_back();
-        if (seen[i]) return c->fail(PT_ERR_INVALID_ARG, "BVH node reached twice (not a tree)");
+        if (seen[i]) {
+            *msg = "BVH node reached twice (not a tree)";
+            return PT_ERR_INVALID_ARG;
+        }
         seen[i] = 1;
         const pt_bvh_node& n = nodes[i];
         if (n.tri_count > 0) {
-            if ((uint64_t)n.left_first + n.tri_count > tris)
-                return c->fail(PT_ERR_INVALID_ARG, "BVH leaf triangle range outside the triangle buffer");
+            if ((uint64_t)n.left_first + n.tri_count > tris) {
+                *msg = "BVH leaf triangle range outside the triangle buffer";
+                return PT_ERR_INVALID_ARG;
+            }
         } else {
-            if (depth >= 64) return c->fail(PT_ERR_OUT_OF_LIMITS, "BVH deeper than the 64-entry traversal stack");
-            if ((uint64_t)n.left_first + 1 >= count || n.left_first == 0)
-                return c->fail(PT_ERR_INVALID_ARG, "BVH child index outside the node buffer");
+            if (depth >= 64) {
+                *msg = "BVH deeper than the 64-entry traversal stack";
+                return PT_ERR_OUT_OF_LIMITS;
+            }
+            if ((uint64_t)n.left_first + 1 >= count || n.left_first == 0) {
+                *msg = "BVH child index outside the node buffer";
+                return PT_ERR_INVALID_ARG;
+            }
             st.push_back({n.left_first, depth + 1});
             st.push_back({(uint64_t)n.left_first + 1, depth + 1});
         }
     }
     return PT_OK;
+}
+
+// every skybox alias entry points inside the table
+bool sky_aliases_in_range(const pt_skybox_alias_entry* a, uint64_t n) {
+    for (uint64_t i = 0; i < n; ++i)
+        if (a[i].alias_index >= n) return false;
+    return true;
 }
 
 // every triangle's material index below material_count; large scenes are
@@ -316,6 +348,7 @@ int apply(pt_ctx* c, const pt_world_updates* u, bool initial) {
     pt_skybox_uniforms sky = u->skybox_uniforms ? *u->skybox_uniforms : c->sky_u;
     uint64_t sky_alias_count = c->sky_alias_count;
     uint64_t live = u->scene ? 0 : c->scene_alias_live;
+    bool sky_checked = false, sky_aliases_ok = true;  // the skybox alias scan, when it ran beside the BVH walk
     const auto validate = [&]() -> int {
         if (const pt_scene_upload* s = u->scene) {
             if (!s->geometries || !s->attributes || !s->materials || !s->bvh_nodes)
@@ -325,10 +358,29 @@ int apply(pt_ctx* c, const pt_world_updates* u, bool initial) {
             if (s->material_count == 0) return c->fail(PT_ERR_INVALID_ARG, "scene has no materials");
             if ((s->srgb_atlas_count && !s->srgb_texture_atlases) || (s->linear_atlas_count && !s->linear_texture_atlases))
                 return c->fail(PT_ERR_INVALID_ARG, "atlas count without atlas data");
-            if (!materials_in_range(s->attributes, s->triangle_count, s->material_count))
-                return c->fail(PT_ERR_INVALID_ARG, "triangle material index outside the material buffer");
-            int rc = validate_bvh(c, s->bvh_nodes, s->node_count, s->triangle_count);
-            if (rc) return rc;
+            // the BVH walk (and the skybox alias scan) run on a helper thread
+            // while this one scans the triangles' material indices
+            const pt_skybox_upload* k = u->skybox;
+            const bool scan_sky = k && k->rgba && k->alias_count && k->alias_table;
+            const char* bvh_msg = nullptr;
+            int bvh_rc = PT_OK;
+            bool sky_ok = true;
+            const auto helper = [&] {
+                bvh_rc = check_bvh(s->bvh_nodes, s->node_count, s->triangle_count, &bvh_msg);
+                if (scan_sky) sky_ok = sky_aliases_in_range(k->alias_table, k->alias_count);
+            };
+            std::thread worker;
+            try {
+                worker = std::thread(helper);
+            } catch (const std::system_error&) {
+                helper();  // no thread to be had: the same work on this one
+            }
+            const bool mats_ok = materials_in_range(s->attributes, s->triangle_count, s->material_count);
+            if (worker.joinable()) worker.join();
+            sky_checked = scan_sky;
+            sky_aliases_ok = sky_ok;
+            if (!mats_ok) return c->fail(PT_ERR_INVALID_ARG, "triangle material index outside the material buffer");
+            if (bvh_rc) return c->fail(bvh_rc, bvh_msg);
             tri = s->triangle_count;
             mats = s->material_count;
         }
@@ -341,11 +393,11 @@ int apply(pt_ctx* c, const pt_world_updates* u, bool initial) {
                 return c->fail(PT_ERR_OUT_OF_LIMITS, "skybox dimensions out of range");
             if (k->alias_count && k->alias_count != (uint64_t)k->uniforms.width * k->uniforms.height)
                 return c->fail(PT_ERR_INVALID_ARG, "skybox alias table size does not match the skybox");
+            if (k->alias_count && !k->alias_table) return c->fail(PT_ERR_INVALID_ARG, "skybox alias table is NULL");
             if (!u->skybox_uniforms) sky = k->uniforms;
             sky_alias_count = k->alias_count;
-            for (uint64_t i = 0; i < k->alias_count; ++i)
-                if (k->alias_table[i].alias_index >= k->alias_count)
-                    return c->fail(PT_ERR_INVALID_ARG, "skybox alias index out of range");
+            if (!(sky_checked ? sky_aliases_ok : sky_aliases_in_range(k->alias_table, k->alias_count)))
+                return c->fail(PT_ERR_INVALID_ARG, "skybox alias index out of range");
         }
         if (u->skybox_uniforms && !u->skybox && (u->skybox_uniforms->width != c->sky_u.width || u->skybox_uniforms->height != c->sky_u.height))
             return c->fail(PT_ERR_INVALID_ARG, "skybox uniforms change the size of the uploaded skybox");

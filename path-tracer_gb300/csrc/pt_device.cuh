@@ -753,6 +753,13 @@ PTD Lobes evaluate_lobes_t(f3 wo, f3 wi, const Bsdf& b, const LobeTerms& t) {
 #ifndef PT_HOIST_INVARIANTS
 #define PT_HOIST_INVARIANTS 1
 #endif
+// unroll factor of that loop (1: a rolled loop; 2 and 4 measured slower on
+// the 2.1M-triangle scene, 1798 and 1789 against 1818 Mrays/s)
+#ifndef PT_EDIEL_UNROLL
+#define PT_EDIEL_UNROLL 1
+#endif
+#define PT_STRINGIFY(x) #x
+#define PT_PRAGMA(x) _Pragma(PT_STRINGIFY(x))
 template <bool kRec>
 PTD f3 estimate_e_dielectric(f3 wo, float opl, f2 alpha, float ior_m, f3 spec_color, Rng<kRec>& rng) {
     float sum = 0.0f;
@@ -761,7 +768,7 @@ PTD f3 estimate_e_dielectric(f3 wo, float opl, f2 alpha, float ior_m, f3 spec_co
     const float ww1 = 1.0f + ww.z;
     const float ior2 = ior_m * ior_m;
     const float ax2 = alpha.x * alpha.x, ay2 = alpha.y * alpha.y;
-#pragma unroll 1
+    PT_PRAGMA(unroll PT_EDIEL_UNROLL)
     for (int i = 0; i < 16; ++i) {
         const float r1 = rng();
         const float tpr = kTwoPi * rng();

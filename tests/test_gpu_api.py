@@ -111,6 +111,93 @@ def test_malformed_bvh_rejected_on_host(cornell, field, value):
     tr.close()
 
 
+def _scene_with_nodes(updates, nodes):
+    s = updates.scene.contents
+    scene = abi.SceneUpload.from_buffer_copy(s)
+    scene.bvh_nodes = C.cast(nodes, C.POINTER(abi.BvhNode))
+    scene.node_count = len(nodes)
+    u = abi.WorldUpdates.from_buffer_copy(updates)
+    u.scene = C.pointer(scene)
+    return u, (nodes, scene)
+
+
+def _chain_nodes(levels):
+    """A degenerate tree: node 2k + 1 interior, node 2k + 2 a one-triangle leaf, `levels` deep."""
+    nodes = (abi.BvhNode * (2 * levels + 1))()
+    for i in range(len(nodes)):
+        n = nodes[i]
+        n.aabb_min[:] = (-1.0, -1.0, -1.0)
+        n.aabb_max[:] = (1.0, 1.0, 1.0)
+    for k in range(levels):
+        i = 0 if k == 0 else 2 * k - 1
+        nodes[i].left_first, nodes[i].tri_count = 2 * k + 1, 0
+        nodes[2 * k + 2].left_first, nodes[2 * k + 2].tri_count = 0, 1
+    last = 2 * levels - 1
+    nodes[last].left_first, nodes[last].tri_count = 0, 1
+    return nodes
+
+
+def test_bvh_validation_messages(cornell):
+    """Each malformed BVH is rejected with its own code and message, by the same checks whether the
+    tree is in the builder's order (the forward pass) or not (the general walk)."""
+    _, updates, _ = cornell
+    s = updates.scene.contents
+    tr = pt.PathTracer(updates, (8, 8))
+    base = (abi.BvhNode * s.node_count)()
+    C.memmove(base, s.bvh_nodes, C.sizeof(base))
+    assert base[1].tri_count == 0 and base[2].tri_count == 0
+
+    def expect(nodes, code, text):
+        bad, keep = _scene_with_nodes(updates, nodes)
+        with pytest.raises(pt.PathTracerError) as e:
+            tr.apply_updates(bad)
+        assert e.value.code == code and text in e.value.message, (e.value.code, e.value.message)
+
+    twice = (abi.BvhNode * s.node_count)()
+    C.memmove(twice, base, C.sizeof(base))
+    twice[2].left_first = twice[1].left_first  # two parents for one child pair
+    expect(twice, abi.PT_ERR_INVALID_ARG, "reached twice")
+    leaf = (abi.BvhNode * s.node_count)()
+    C.memmove(leaf, base, C.sizeof(base))
+    leaf[1].tri_count, leaf[1].left_first = 5, s.triangle_count - 2
+    expect(leaf, abi.PT_ERR_INVALID_ARG, "leaf triangle range")
+    expect(_chain_nodes(70), abi.PT_ERR_OUT_OF_LIMITS, "deeper than the 64-entry")
+    # 64 interior levels are accepted (a traversal defers at most one entry per level)
+    tr.apply_updates(_scene_with_nodes(updates, _chain_nodes(64))[0])
+    tr.apply_updates(updates)
+    tr.close()
+
+
+def test_skybox_alias_validation(cornell):
+    w = pt.World.procedural(grid_x=16, grid_z=8, boxes=4, spheres=1, sphere_subdivision=1, emissive_triangles=2,
+                            skybox_width=32, skybox_height=16)
+    w.set_aspect_ratio(1.0)
+    u = w.take_updates()
+    tr = pt.PathTracer(u, (8, 8))
+    k = u.skybox.contents
+    assert k.alias_count == 32 * 16
+    table = (abi.SkyboxAliasEntry * k.alias_count)()
+    C.memmove(table, k.alias_table, C.sizeof(table))
+    table[7].alias_index = k.alias_count
+    sky = abi.SkyboxUpload.from_buffer_copy(k)
+    sky.alias_table = C.cast(table, C.POINTER(abi.SkyboxAliasEntry))
+    bad = abi.WorldUpdates.from_buffer_copy(u)
+    bad.skybox = C.pointer(sky)
+    with pytest.raises(pt.PathTracerError) as e:
+        tr.apply_updates(bad)  # with the scene: the scan runs beside the BVH walk
+    assert e.value.code == abi.PT_ERR_INVALID_ARG and "skybox alias index" in e.value.message
+    bad.scene = None
+    with pytest.raises(pt.PathTracerError) as e:
+        tr.apply_updates(bad)  # skybox alone
+    assert "skybox alias index" in e.value.message
+    sky.alias_table = None
+    with pytest.raises(pt.PathTracerError) as e:
+        tr.apply_updates(bad)
+    assert "alias table is NULL" in e.value.message
+    tr.apply_updates(u)
+    tr.close()
+
+
 def test_inconsistent_lights_rejected(cornell):
     _, updates, _ = cornell
     u = abi.WorldUpdates.from_buffer_copy(updates)
