@@ -125,7 +125,9 @@ def job_rate(units_per_step: float, steps: int, world_size: int, seconds: float)
     return units_per_step * steps * world_size / seconds
 
 
-def workload_config(world, kernel: str) -> dict:
+def workload_config(world, precision: str, replicas: int) -> dict:
+    """The workload of a bench line; both arms print the same dict (the implementation that ran is the
+    line's top-level "kernel")."""
     return {
         "workload": f"{WORKLOADS[WORKLOAD]['text']}, {WIDTH}x{HEIGHT}, {SPP} spp, max_bounces 8, one image per step",
         "triangles": int(world.triangle_count()),
@@ -133,9 +135,10 @@ def workload_config(world, kernel: str) -> dict:
         "image": [WIDTH, HEIGHT],
         "spp": SPP,
         "max_bounces": MAX_BOUNCES,
-        "kernel": kernel,
         "l2": WORKLOADS[WORKLOAD]["l2"],
         "seed": {"procedural": 1, "procedural_4m": 7}.get(WORKLOAD, 0),
+        "precision": precision,
+        "parallelism": f"replicas x{replicas}",
     }
 
 
@@ -526,8 +529,9 @@ def run_reference(args):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean([d for _, d in values]) * 1e3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(world, "cpu"),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (scene built from a seed)",
+        "config": workload_config(world, "fp32", args.gpus), "kernel": "cpu",
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": desc},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's own trace pass (Rust + WGSL via wgpu) cannot run on this box; this is the "
@@ -703,9 +707,8 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world_size, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": dict(workload_config(world, args.kernel), precision=args.precision,
-                           parallelism=f"replicas x{world_size}"),
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (scene built from a seed)",
+            "config": workload_config(world, args.precision, world_size), "kernel": args.kernel,
             "rays_per_step": rays_per_step, "samples_per_s": job_rate(paths_per_step, args.steps, world_size,
                                                                      elapsed_ms / 1e3),
             # whole-pass algorithmic bytes per ray and the Mrays/s they would allow at the HBM peak

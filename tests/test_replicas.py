@@ -71,3 +71,8 @@ def test_reference_arm_under_torchrun_prints_once():
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
     # the arm runs the oracle only: the scene comes from a child process as upload bytes
     assert line["maps_gpu_library"] is False
+    # the same workload dict as the GPU arm's line at this replica count (which implementation ran is
+    # the top-level "kernel", not part of the config)
+    assert line["kernel"] == "cpu" and "kernel" not in line["config"]
+    assert line["config"]["precision"] == "fp32" and line["config"]["parallelism"] == "replicas x2"
+    assert line["config"]["image"] == [256, 256] and line["config"]["spp"] == 16
