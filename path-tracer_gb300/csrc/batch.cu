@@ -220,12 +220,16 @@ __global__ void __launch_bounds__(kThreads, blocks_for(PT_SHADE_MIN_BLOCKS, kSha
             const uint32_t tag = b.tag[p];
             const World& w = scenes[tag & 0xffu].w;
             const uint32_t max_bounces = jobs[tag >> 8].max_bounces;
-            const float4 c4 = b.q.color[p];
             ps.o = mk(o4.x, o4.y, o4.z);
             ps.d = mk(d4.x, d4.y, d4.z);
             ps.throughput = mk(t4.x, t4.y, t4.z);
             ps.prev_pdf = t4.w;
-            ps.color = mk(c4.x, c4.y, c4.z);
+            if constexpr (kColorDelta<kAlpha>) {
+                ps.color = mk(0.0f, 0.0f, 0.0f);
+            } else {
+                const float4 c4 = b.q.color[p];
+                ps.color = mk(c4.x, c4.y, c4.z);
+            }
             Rng<false> rng;
             rng.s = __float_as_uint(d4.w);
             const int32_t hit = __float_as_int(h4.y);
@@ -237,7 +241,7 @@ __global__ void __launch_bounds__(kThreads, blocks_for(PT_SHADE_MIN_BLOCKS, kSha
                                                     nullptr, &sr);
                 }
             }
-            b.q.color[p] = make_float4(ps.color.x, ps.color.y, ps.color.z, 0.0f);
+            store_color<kAlpha>(b.q.color, p, ps.color);
             rs = rng.s;
         }
         const uint32_t slot = warp_append(cont, st.next_count, 0xffffffffu);
@@ -353,6 +357,7 @@ __global__ void pad_triangles_kernel(const pt_triangle_geometry* geo, uint64_t n
     tri4[kTriStride * i + 0] = make_float4(v[0], v[1], v[2], 0.0f);
     tri4[kTriStride * i + 1] = make_float4(v[3], v[4], v[5], 0.0f);
     tri4[kTriStride * i + 2] = make_float4(v[6], v[7], v[8], 0.0f);
+    if (kTriStride == 4) tri4[kTriStride * i + 3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // read, never used
 }
 
 // ---------------------------------------------------------------- host

@@ -12,7 +12,7 @@ namespace ptd {
 
 struct Fast {
     const float4* pairs;  // node i at pairs[2i], pairs[2i+1]
-    const float4* tri4;   // triangle i at tri4[3i .. 3i+2]
+    const float4* tri4;   // triangle i at tri4[kTriStride i .. kTriStride i + 2] (padded to 48 or 64 bytes)
     const float4* wide = nullptr;  // pt_wide_node i at wide[8i .. 8i+7] (precision form)
     const uint32_t* parent = nullptr;   // binary node -> its parent (root: 0xffffffff)
     const uint32_t* leaf_of = nullptr;  // triangle -> the binary leaf holding it
@@ -238,11 +238,24 @@ PTD void load_node(const float4* p, float4& lo, float4& hi) {
 #ifndef PT_V8_TRIS
 #define PT_V8_TRIS 0
 #endif
+// 1: a traversal step that tests one triangle (PT_TRI_PER_STEP) reads its
+// data - a child pair, or a triangle padded to 64 bytes - with the same two
+// 256-bit loads whichever kind of step the lane runs, so a warp whose lanes
+// run both kinds waits for one load, not for two in turn
+#ifndef PT_UNIFIED_STEP
+#define PT_UNIFIED_STEP 1
+#endif
 // float4s per padded triangle: 3 (48 bytes), or 4 (64 bytes: one 256-bit and
-// one 128-bit load, both aligned)
+// one 128-bit load, both aligned; the shape of a child pair, which the
+// unified step needs)
 #ifndef PT_TRI_STRIDE
+#if PT_UNIFIED_STEP
+#define PT_TRI_STRIDE 4
+#else
 #define PT_TRI_STRIDE 3
 #endif
+#endif
+static_assert(!PT_UNIFIED_STEP || PT_TRI_STRIDE == 4, "the unified traversal step reads triangles padded to 64 bytes");
 constexpr uint32_t kTriStride = PT_TRI_STRIDE;
 PTD Tri load_tri4(const Fast& f, uint32_t tri) {
     const float4* p = f.tri4 + kTriStride * (size_t)tri;
@@ -343,13 +356,17 @@ struct Traverser {
     // the watertight test of one triangle against the ray; for kShadow true
     // when the triangle occludes
     PTD bool test_triangle(const World& w, const Fast& f, uint32_t tri) {
-        rec.tri();
-        float t, v, wb;
         Tri tv;
         if constexpr (kTri36)
             tv = load_tri(w, tri);  // the caller's 36-byte triangles
         else
             tv = load_tri4(f, tri);
+        return test_loaded(w, tri, tv);
+    }
+    // the same with the triangle's vertices already loaded
+    PTD bool test_loaded(const World& w, uint32_t tri, const Tri& tv) {
+        rec.tri();
+        float t, v, wb;
         if (!triangle_test(tv, o, s, &t, &v, &wb)) return false;
         if (t > 0.0f && t < hit_t) {
             if constexpr (kAlpha) {
@@ -390,7 +407,9 @@ struct Traverser {
 
     template <class S>
     PTD bool step(const World& w, const Fast& f, S& stack, uint32_t* istack) {
-        if constexpr (kTriStep) {
+        if constexpr (kTriStep && PT_UNIFIED_STEP && !kTri36) {
+            return step_unified(w, f, stack, istack);
+        } else if constexpr (kTriStep) {
             const bool done = step_tri(w, f, stack, istack);
             if (!done) prefetch_next(f);
             return done;
@@ -445,6 +464,61 @@ struct Traverser {
         if (tri_left > 0u) return false;
         return pop(stack, istack);
     }
+    // step_tri with one load for both kinds of step: the lane's next child
+    // pair (interior) or next triangle (64-byte padded layout) is read by the
+    // same two 256-bit loads before the branch, so the warp's interior lanes
+    // and triangle lanes wait for memory together.  The same visits, tests
+    // and stack operations as step_tri, in the same order.
+    template <class S>
+    PTD bool step_unified(const World& w, const Fast& f, S& stack, uint32_t* istack) {
+        if (tri_left == 0u) {
+            rec.visit(idx);
+            if (tc != 0u) {
+                rec.leaf();
+                tri_left = tc;  // lf walks the leaf's triangles
+            } else {
+                rec.interior();
+            }
+        }
+        const bool interior = tri_left == 0u;
+        const float4* p = interior ? f.pairs + 2 * (size_t)lf : f.tri4 + kTriStride * (size_t)lf;
+        float4 a0, a1, b0, b1;
+        load_node(p, a0, a1);
+        load_node(p + 2, b0, b1);
+        if (interior) {
+            const float dl = box_test(a0, a1, nod, rcp, hit_t);
+            const float dr = box_test(b0, b1, nod, rcp, hit_t);
+            const bool hl = dl >= 0.0f, hr = dr >= 0.0f;
+            if (hl || hr) {
+                const bool go_left = hl && (!hr || dl < dr);
+                if (hl && hr) {
+                    const float4 f0 = go_left ? b0 : a0, f1 = go_left ? b1 : a1;
+                    stack.put(sp, make_uint2(__float_as_uint(f0.w), __float_as_uint(f1.w)));
+                    if constexpr (kRec) istack[sp & 63u] = go_left ? lf + 1u : lf;
+                    sp += 1u;
+                }
+                const float4 n0 = go_left ? a0 : b0, n1 = go_left ? a1 : b1;
+                if constexpr (kRec) idx = go_left ? lf : lf + 1u;
+                lf = __float_as_uint(n0.w);
+                tc = __float_as_uint(n1.w);
+                return false;
+            }
+            return pop(stack, istack);
+        }
+        const uint32_t tri = lf;
+        lf += 1u;
+        tri_left -= 1u;
+        bool skip = false;
+        if constexpr (kShadow) skip = (int32_t)tri == light_tri;
+        Tri tv;
+        tv.v0 = mk(a0.x, a0.y, a0.z);
+        tv.v1 = mk(a1.x, a1.y, a1.z);
+        tv.v2 = mk(b0.x, b0.y, b0.z);
+        if (!skip && test_loaded(w, tri, tv)) return true;
+        if (tri_left > 0u) return false;
+        return pop(stack, istack);
+    }
+
     // one node visit; true when the traversal has finished (for kShadow,
     // hit == 1 marks an occluder)
     template <class S>
@@ -1006,6 +1080,35 @@ struct FilerSlots {
 struct NoRound {
     PTD void operator()() const {}
 };
+
+// 1: in opaque scenes a shading step adds exactly one radiance term to its
+// path's colour (the sky at a miss, trace.slang:925; emission at a hit,
+// :991; the next-event light of :1204 arrives later through the shadow
+// kernel), so
+// the shading kernel starts from zero, and reads and rewrites the path's
+// colour only when that term is not zero.  Same bits: the colour starts at
+// +0 and is only ever a sum, so it is never -0, and colour + (+-0) = colour.
+// Non-opaque scenes add the unoccluded light in the same step (two terms),
+// so they keep the read-modify-write of the running colour.
+#ifndef PT_COLOR_DELTA
+#define PT_COLOR_DELTA 1
+#endif
+template <bool kAlpha>
+constexpr bool kColorDelta = PT_COLOR_DELTA && !kAlpha;
+
+// the path's colour after a shading step: `c` is the new colour, or with
+// kColorDelta the term the step added (0 + term)
+template <bool kAlpha>
+PTD void store_color(float4* color, uint32_t p, f3 c) {
+    if constexpr (kColorDelta<kAlpha>) {
+        if (c.x != 0.0f || c.y != 0.0f || c.z != 0.0f) {
+            const float4 old = color[p];
+            color[p] = make_float4(old.x + c.x, old.y + c.y, old.z + c.z, 0.0f);
+        }
+    } else {
+        color[p] = make_float4(c.x, c.y, c.z, 0.0f);
+    }
+}
 
 // The shading kernels' view of the filed results: misses first, padded to
 // whole warps, then hits.  Entry j of that range maps to a queue slot.

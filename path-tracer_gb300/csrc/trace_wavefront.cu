@@ -178,12 +178,16 @@ __global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kern
         if (i != 0xffffffffu) {
             const float4 o4 = st.o[i], d4 = st.d[i], t4 = st.T[i], h4 = q.hit[i];
             p = __float_as_uint(o4.w);
-            const float4 c4 = q.color[p];
             ps.o = mk(o4.x, o4.y, o4.z);
             ps.d = mk(d4.x, d4.y, d4.z);
             ps.throughput = mk(t4.x, t4.y, t4.z);
             ps.prev_pdf = t4.w;
-            ps.color = mk(c4.x, c4.y, c4.z);
+            if constexpr (kColorDelta<kAlpha>) {
+                ps.color = mk(0.0f, 0.0f, 0.0f);
+            } else {
+                const float4 c4 = q.color[p];
+                ps.color = mk(c4.x, c4.y, c4.z);
+            }
             Counters c;
             Rng<kRec> rng;
             rng.s = __float_as_uint(d4.w);
@@ -199,7 +203,7 @@ __global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kern
                 if constexpr (kRec) c.hits += 1;
                 cont = shade_hit<kRec, kAlpha>(w, bounce, max_bounces, ps, h4.x, (uint32_t)hit, h4.z, h4.w, rng, &c, &sr);
             }
-            q.color[p] = make_float4(ps.color.x, ps.color.y, ps.color.z, 0.0f);
+            store_color<kAlpha>(q.color, p, ps.color);
             rs = rng.s;
             if constexpr (kRec) q.rec[p] = c;
         }
@@ -339,6 +343,7 @@ __global__ void pad_triangles_kernel(const pt_triangle_geometry* geo, uint64_t n
     tri4[kTriStride * i + 0] = make_float4(v[0], v[1], v[2], 0.0f);
     tri4[kTriStride * i + 1] = make_float4(v[3], v[4], v[5], 0.0f);
     tri4[kTriStride * i + 2] = make_float4(v[6], v[7], v[8], 0.0f);
+    if (kTriStride == 4) tri4[kTriStride * i + 3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // read, never used
 }
 
 // FP32 attributes -> pt_half_attribute records (round to nearest even)
