@@ -215,7 +215,10 @@ __global__ void __launch_bounds__(kThreads, blocks_for(PT_SHADE_MIN_BLOCKS, kSha
         PathState ps;
         uint32_t p = 0, rs = 0;
         if (i != 0xffffffffu) {
-            const float4 o4 = st.o[i], d4 = st.d[i], t4 = st.T[i], h4 = b.q.hit[i];
+            // the entries before miss_span are misses (the extend kernel filed them so): no hit record to read
+            const bool miss = base + lane < range.miss_span;
+            const float4 o4 = st.o[i], d4 = st.d[i], t4 = st.T[i];
+            const float4 h4 = miss ? make_float4(0.0f, __int_as_float(-1), 0.0f, 0.0f) : b.q.hit[i];
             p = __float_as_uint(o4.w);
             const uint32_t tag = b.tag[p];
             const World& w = scenes[tag & 0xffu].w;
@@ -1050,6 +1053,8 @@ int upload_scene(pt_engine* e, Scene& s, const pt_world_updates* u) {
     w.scene = *u->scene_uniforms;
     w.srgb_lut = s.lut.as<float>();
     w.any_alpha = s.any_alpha ? 1 : 0;
+    w.attr16 = 1;  // a device allocation
+    if (ptd::kTriStride == 4) w.tri64 = s.tri4.as<float4>();  // the shading frame's vertices
     d.f.pairs = reinterpret_cast<const float4*>(static_cast<const char*>(s.pairs.p) + 32);
     d.f.tri4 = s.tri4.as<float4>();
     d.f.wide = s.wide.p ? s.wide.as<float4>() : nullptr;

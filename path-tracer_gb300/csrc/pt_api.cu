@@ -117,6 +117,7 @@ struct pt_ctx {
         w.scene = scene;
         w.camera = camera;
         w.srgb_lut = srgb_lut.as<const float>();
+        w.attr16 = 1;  // a device allocation
         int any = 0;
         for (uint32_t m : alpha_modes) any |= (m != PT_ALPHA_MODE_OPAQUE);
         w.any_alpha = any;

@@ -105,6 +105,10 @@ struct World {
     // compressed copies (precision form); null: read attr / sky
     const uint2* attr_h = nullptr;  // pt_half_attribute records, 8 x uint2 each
     const uint2* sky_h = nullptr;   // skybox texels as BF16 RGBA
+    // the triangles padded to 64 bytes (the wavefront traversal's copy), read
+    // by the shading code with two vector loads; null: geo
+    const float4* tri64 = nullptr;
+    int attr16 = 0;  // attr is 16-byte aligned: records are read in 16-byte pieces
 };
 
 // per-path instrumentation (pt_path_record) kept in registers while tracing
@@ -185,6 +189,22 @@ PTD Tri load_tri(const World& w, uint32_t tri) {
     t.v0 = mk(__ldg(p + 0), __ldg(p + 1), __ldg(p + 2));
     t.v1 = mk(__ldg(p + 3), __ldg(p + 4), __ldg(p + 5));
     t.v2 = mk(__ldg(p + 6), __ldg(p + 7), __ldg(p + 8));
+    return t;
+}
+// The hit triangle for the shading frame: with the 64-byte padded copy one
+// 256-bit and one 128-bit load instead of nine 32-bit loads (same values)
+PTD Tri load_hit_tri(const World& w, uint32_t tri) {
+    if (!w.tri64) return load_tri(w, tri);
+    const float4* p = w.tri64 + 4 * (size_t)tri;
+    float4 a, b;
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+    const float4 c = __ldg(p + 2);
+    Tri t;
+    t.v0 = mk(a.x, a.y, a.z);
+    t.v1 = mk(b.x, b.y, b.z);
+    t.v2 = mk(c.x, c.y, c.z);
     return t;
 }
 
@@ -358,8 +378,57 @@ PTD f2 attr_uv(const World& w, uint32_t tri, int k) {
     return {__ldg(uv), __ldg(uv + 1)};
 }
 
+// The FP32 attribute record (112 bytes) in 16-byte pieces, when the buffer is
+// 16-byte aligned: [0] material, n0 | [1] n1, n2.x | [2] n2.yz, uv0 |
+// [3] uv1, uv2 | [4] t0 | [5] t1 | [6] t2.  Three normals, three tangents or
+// three UVs then take two or three 128-bit loads instead of six to ten
+// 32-bit loads (same values).
+#ifndef PT_VEC_ATTR
+#define PT_VEC_ATTR 1
+#endif
+PTD bool attr_pieces(const World& w) { return PT_VEC_ATTR && w.attr16 && !w.attr_h; }
+PTD float4 attr_piece(const World& w, uint32_t tri, int k) {
+    return __ldg(reinterpret_cast<const float4*>(w.attr + tri) + k);
+}
+PTD void attr_normals(const World& w, uint32_t tri, f3& n0, f3& n1, f3& n2) {
+    if (attr_pieces(w)) {
+        const float4 a = attr_piece(w, tri, 0), b = attr_piece(w, tri, 1), c = attr_piece(w, tri, 2);
+        n0 = mk(a.y, a.z, a.w);
+        n1 = mk(b.x, b.y, b.z);
+        n2 = mk(b.w, c.x, c.y);
+        return;
+    }
+    n0 = attr_normal(w, tri, 0);
+    n1 = attr_normal(w, tri, 1);
+    n2 = attr_normal(w, tri, 2);
+}
+PTD void attr_tangents(const World& w, uint32_t tri, f3& t0, f3& t1, f3& t2, float& t0w) {
+    if (attr_pieces(w)) {
+        const float4 a = attr_piece(w, tri, 4), b = attr_piece(w, tri, 5), c = attr_piece(w, tri, 6);
+        t0 = mk(a.x, a.y, a.z);
+        t0w = a.w;
+        t1 = mk(b.x, b.y, b.z);
+        t2 = mk(c.x, c.y, c.z);
+        return;
+    }
+    t0 = attr_tangent(w, tri, 0);
+    t1 = attr_tangent(w, tri, 1);
+    t2 = attr_tangent(w, tri, 2);
+    t0w = attr_tangent0_w(w, tri);
+}
+
 PTD f2 interp_uv(const World& w, uint32_t tri, float u, float v, float w2) {
-    const f2 a = attr_uv(w, tri, 0), b = attr_uv(w, tri, 1), c = attr_uv(w, tri, 2);
+    f2 a, b, c;
+    if (attr_pieces(w)) {
+        const float4 p = attr_piece(w, tri, 2), q = attr_piece(w, tri, 3);
+        a = {p.z, p.w};
+        b = {q.x, q.y};
+        c = {q.z, q.w};
+    } else {
+        a = attr_uv(w, tri, 0);
+        b = attr_uv(w, tri, 1);
+        c = attr_uv(w, tri, 2);
+    }
     return {fract(u * a.x + v * b.x + w2 * c.x), fract(u * a.y + v * b.y + w2 * c.y)};
 }
 

@@ -241,18 +241,16 @@ PTD bool shade_hit(const World& w, uint32_t bounce, uint32_t max_bounces, PathSt
     // shading frame, trace.slang:993-1091
     const f3 hit_point = ps.d * hit_t + ps.o;
     const f3 V = -ps.d;
-    const Tri tri = load_tri(w, h);
+    const Tri tri = load_hit_tri(w, h);
     const f3 flat_raw = normalize(cross(tri.v1 - tri.v0, tri.v2 - tri.v0));
     const float bfm = dot(V, flat_raw) > 0.0f ? 1.0f : -1.0f;
     const f3 flat_n = flat_raw * bfm;
-    const f3 n0 = attr_normal(w, h, 0);
-    const f3 n1 = attr_normal(w, h, 1);
-    const f3 n2 = attr_normal(w, h, 2);
+    f3 n0, n1, n2;
+    attr_normals(w, h, n0, n1, n2);
     f3 N = normalize(hu * n0 + hv * n1 + hw * n2) * bfm;
-    const f3 t0 = attr_tangent(w, h, 0);
-    const f3 t1 = attr_tangent(w, h, 1);
-    const f3 t2 = attr_tangent(w, h, 2);
-    const float t0w = attr_tangent0_w(w, h);
+    f3 t0, t1, t2;
+    float t0w;
+    attr_tangents(w, h, t0, t1, t2, t0w);
     f3 Tn = orthonormal_tangent(hu * t0 + hv * t1 + hw * t2, N) * bfm;
     f3 Bn = cross(N, Tn) * t0w * bfm;
     bool n_changed = false;

@@ -176,7 +176,10 @@ __global__ void __launch_bounds__(kShadeThreads, PT_SHADE_MIN_BLOCKS) shade_kern
         PathState ps;
         uint32_t p = 0, rs = 0;
         if (i != 0xffffffffu) {
-            const float4 o4 = st.o[i], d4 = st.d[i], t4 = st.T[i], h4 = q.hit[i];
+            // the entries before miss_span are misses (the extend kernel filed them so): no hit record to read
+            const bool miss = base + lane < range.miss_span;
+            const float4 o4 = st.o[i], d4 = st.d[i], t4 = st.T[i];
+            const float4 h4 = miss ? make_float4(0.0f, __int_as_float(-1), 0.0f, 0.0f) : q.hit[i];
             p = __float_as_uint(o4.w);
             ps.o = mk(o4.x, o4.y, o4.z);
             ps.d = mk(d4.x, d4.y, d4.z);
@@ -731,6 +734,7 @@ cudaError_t trace(Wavefront* wf, const ptd::World& w_in, const ptk::Tile& tile, 
     const uint64_t pixels = (uint64_t)vis_w * vis_h;
     if (pixels == 0 || samples == 0) return cudaSuccess;
     if (wf->stale || wf->layout_nodes != w.nodes || wf->layout_geo != w.geo) return cudaErrorNotReady;  // prepare() first
+    if (ptd::kTriStride == 4) w.tri64 = static_cast<const float4*>(wf->tri4.p);  // the shading frame's vertices
     uint32_t group = (uint32_t)(kMaxPaths / pixels);
     if (group == 0) group = 1;
     if (group > samples) group = samples;
@@ -999,6 +1003,7 @@ extern "C" int pt_trace_noalloc(const pt_device_world* world, const pt_trace_par
     w.camera = world->camera;
     w.srgb_lut = reinterpret_cast<const float*>(base + kNoAllocLutOffset);
     w.any_alpha = world->any_non_opaque ? 1 : 0;
+    w.attr16 = ((uintptr_t)world->attributes & 15u) == 0u ? 1 : 0;  // the caller's buffer: any alignment
 
     ptd::Queues q;
     float4* slots = reinterpret_cast<float4*>(base);
