@@ -163,3 +163,36 @@ def test_noalloc_rejects_unaligned_nodes_on_the_host():
     rc, msg = noalloc(lib, dw, (8, 8), (0, 0), (8, 8), 2, 0, 1, accum, out)
     assert rc == abi.PT_ERR_INVALID_ARG and "32-byte aligned" in msg
     torch.cuda.synchronize()
+
+
+def test_noalloc_reads_attributes_at_any_alignment():
+    # the caller's attribute records may start at any 4-byte boundary: 16-byte pieces are read only from
+    # a 16-byte aligned array, others are read by fields, with the same bits as pt_trace
+    torch = pytest.importorskip("torch")
+    lib = pt.load()
+    world = pt.World.cornell_box()
+    image, origin, tile, bounces, spp = (128, 128), (16, 24), (64, 64), 8, 2
+    world.set_aspect_ratio(1.0)
+    updates = world.take_updates()
+    tracer = pt.PathTracer(updates, tile)
+    tracer.set_kernel(abi.PT_KERNEL_WAVEFRONT)
+    tracer.set_max_bounces(bounces)
+    tracer.set_tile(image, origin, tile)
+    assert tracer.trace(spp) == spp
+    want = tracer.read_tile(abi.PT_TILE_ACCUMULATION)
+    tracer.close()
+    keep = []
+    dw = device_world(torch, updates, keep)
+    s = updates.scene.contents
+    host = np.ctypeslib.as_array(C.cast(s.attributes, C.POINTER(C.c_uint8)), shape=(112 * s.triangle_count,)).copy()
+    shifted = torch.zeros(112 * s.triangle_count + 16, dtype=torch.uint8, device="cuda")
+    shifted[4:4 + host.size] = torch.from_numpy(host).to("cuda")
+    keep.append(shifted)
+    dw.attributes = shifted.data_ptr() + 4
+    accum = torch.zeros((tile[1], tile[0], 4), dtype=torch.float32, device="cuda")
+    out = torch.zeros_like(accum)
+    rc, msg = noalloc(lib, dw, image, origin, tile, bounces, 0, spp, accum, out)
+    assert rc == abi.PT_OK, msg
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(accum.cpu().numpy().view(np.uint32), want.view(np.uint32))
+    assert float(out.max()) > 0.0
