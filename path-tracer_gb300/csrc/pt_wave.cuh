@@ -1084,12 +1084,12 @@ struct NoRound {
 // 1: in opaque scenes a shading step adds exactly one radiance term to its
 // path's colour (the sky at a miss, trace.slang:925; emission at a hit,
 // :991; the next-event light of :1204 arrives later through the shadow
-// kernel), so
-// the shading kernel starts from zero, and reads and rewrites the path's
-// colour only when that term is not zero.  Same bits: the colour starts at
-// +0 and is only ever a sum, so it is never -0, and colour + (+-0) = colour.
-// Non-opaque scenes add the unoccluded light in the same step (two terms),
-// so they keep the read-modify-write of the running colour.
+// kernel), so the shading kernel starts from zero, and reads and rewrites
+// the path's colour only when that term is not zero.  Same bits: the colour
+// starts at +0 and is only ever a sum, so it is never -0, and
+// colour + (+-0) = colour.  Non-opaque scenes add the unoccluded light in
+// the same step (two terms), so they keep the read-modify-write of the
+// running colour.
 #ifndef PT_COLOR_DELTA
 #define PT_COLOR_DELTA 1
 #endif
