@@ -3,7 +3,8 @@
 Per path: node-visit order (FNV-1a hash), closest-hit triangle per bounce,
 every counter and the radiance bits must be identical; the accumulation
 buffer and storage texture must match the oracle's FP32 running sums bit for
-bit; RMSE against the FP64 oracle render is reported and bounded.
+bit, both from the recording kernels and from the kernels the library runs
+otherwise; RMSE against the FP64 oracle render is reported and bounded.
 """
 import numpy as np
 import pytest
@@ -32,6 +33,19 @@ def assert_records_equal(gpu, ref):
         bad = np.nonzero(np.any((gpu[field] != ref[field]).reshape(gpu.shape[0], -1), axis=1))[0]
         assert bad.size == 0, f"{field} differs in {bad.size} paths, first {bad[:5]}"
     np.testing.assert_array_equal(gpu["radiance"].view(np.uint32), ref["radiance"].view(np.uint32))
+
+
+def assert_fast_accumulation(tr, image, origin, size, spp, ref):
+    """The kernels that run outside the tests (no per-path records) give the oracle's accumulation
+    bits for the same paths: the tile is traced again from its first sample with pt_trace."""
+    tr.set_tile(image, origin, size)
+    done = 0
+    while done < spp:
+        done += tr.trace(spp - done)
+    vis = (min(size[0], image[0] - origin[0]), min(size[1], image[1] - origin[1]))
+    acc = tr.read_tile(abi.PT_TILE_ACCUMULATION)[:vis[1], :vis[0], :3].reshape(-1, 3)
+    want = oracle.accumulate(ref["radiance"].reshape(spp, -1, 3))[-1]
+    np.testing.assert_array_equal(acc.view(np.uint32), want.view(np.uint32))
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
@@ -168,6 +182,7 @@ def test_large_scene_tile_bit_exact(large_world, kernel):
         px = pixels_of(origin, (64, 64), (1920, 1080))
         _, ref = oracle.trace_paths(ow, (1920, 1080), 8, px, 1, 4, records=True)
         assert_records_equal(gpu, ref)
+        assert_fast_accumulation(tr, (1920, 1080), origin, (64, 64), 4, ref)
         light += int(ref["light_samples"].sum())
         sky += int(ref["sky_light_samples"].sum())
     assert light > 0 and sky > 0  # both light categories exercised
@@ -202,6 +217,7 @@ def test_textured_cornell_tile_bit_exact(kernel):
     px = pixels_of((96, 128), (64, 64), (256, 256))
     _, ref = oracle.trace_paths(ow, (256, 256), 8, px, 1, 4, records=True)
     assert_records_equal(gpu, ref)
+    assert_fast_accumulation(tr, (256, 256), (96, 128), (64, 64), 4, ref)
     tr.close()
 
 
@@ -237,6 +253,7 @@ def test_gltf_textured_bit_exact(tmp_path, kernel):
     gpu = tr.trace_recorded(2)
     _, ref = oracle.trace_paths(ow, (128, 128), 4, pixels_of((32, 32), (64, 64), (128, 128)), 1, 2, records=True)
     assert_records_equal(gpu, ref)
+    assert_fast_accumulation(tr, (128, 128), (32, 32), (64, 64), 2, ref)
     assert (gpu["hits"] > 0).mean() > 0.5  # the camera sees the textured quads
     tr.close()
     w.close()
@@ -283,6 +300,7 @@ def test_non_opaque_tile_bit_exact(kernel):
         px = pixels_of(origin, (48, 48), (128, 128))
         _, ref = oracle.trace_paths(ow, (128, 128), 8, px, 1, 4, records=True)
         assert_records_equal(gpu, ref)
+        assert_fast_accumulation(tr, (128, 128), origin, (48, 48), 4, ref)
         draws += int(ref["rand_draws"].sum())
     assert draws > 0
     # the paths' hits include surfaces of both non-opaque kinds
@@ -315,6 +333,7 @@ def test_material_zoo_bit_exact(kernel):
     mat_of_tri = np.frombuffer(w.attributes_raw().tobytes(), np.uint32).reshape(w.triangle_count(), -1)[:, 0]
     first = ref["hit"][:, 0]
     assert set(range(5)) <= set(mat_of_tri[first[first >= 0]].tolist())  # every zoo sphere is seen
+    assert_fast_accumulation(tr, image, origin, size, 4, ref)
     if kernel == abi.PT_KERNEL_WAVEFRONT:
         want = oracle.accumulate(ref["radiance"].reshape(4, -1, 3))[-1]
         tr.set_precision(abi.PT_PRECISION_WIDE_BVH)
