@@ -6,8 +6,9 @@ procedural scene (1024x512-quad heightfield, 2000 boxes, 200 icospheres,
 64 emissive triangles, 1024x512 sky), 64 samples per pixel, max_bounces 8,
 traced through pt_trace in calls of at most 16 samples exactly as the
 reference's headless loop does (one tile covering the image).  A ray is every
-extend or shadow traversal.  The scene (BVH 134 MB + triangles 75 MB +
-attributes 235 MB) is larger than the 129 MB L2, so no L2 flush is needed
+extend or shadow traversal.  The scene as the kernels read it (BVH child
+pairs 75 MB + triangles padded to 64 bytes 134 MB + attributes 235 MB) is
+larger than the 129 MB L2, so no L2 flush is needed
 between steps.
 
 Contract: python bench.py [--gpus N --steps K --warmup W] prints one JSON line.
