@@ -294,13 +294,16 @@ def mixed_stream_report(seconds: float = 10.0, rate: float = 50.0, jobs: int = 2
       the plain kernel (one pt_trace of <= 16 samples per call, the host waiting on each call:
       the reference's dispatch shape, FP32), the wavefront kernels one job per call (FP32), and the
       batched engine in the form and with the settings its autotuner run chose
-      (pathtracer/engine_tuned.json: FP16 attributes / BF16 skybox + Kahan sums on the binary BVH).
+      (pathtracer/engine_tuned.json: FP16 attributes / BF16 skybox + Kahan sums on the binary BVH),
+      and the batched engine in the full compressed-node form (the same settings with the 8-wide
+      BVH of 8-bit outward-rounded child boxes as well).
     * serving: Poisson arrivals at `rate` req/s for `seconds` s, 10 % progressive refinements, a
       fifth of the requests 512x512 x 16 spp x max_bounces 8; latency from arrival to result
       through the serving loop (continuous batching), overall and for the 512x512x16 requests
       inside the mix, on a second engine with the same settings but 4M-path waves
       (Engine.SERVING_WAVE_PATHS: the latency setting); the plain path's latencies for the same
       stream are replayed from its measured per-request service times."""
+    from pathtracer import abi
     from pathtracer.engine import Engine
     from pathtracer.serving import (Server, build_scene, closed_loop, percentiles, replay_latencies,
                                     request_stream)
@@ -311,8 +314,10 @@ def mixed_stream_report(seconds: float = 10.0, rate: float = 50.0, jobs: int = 2
     server = Server(eng, worlds)
     serve_eng = Engine.tuned(hbm_budget_bytes=100 << 30, wave_paths=Engine.SERVING_WAVE_PATHS)
     serve_server = Server(serve_eng, worlds, full=server.full)
+    comp_eng = Engine.tuned(hbm_budget_bytes=100 << 30, precision=abi.PT_PRECISION_COMPRESSED)
+    comp_server = Server(comp_eng, worlds, full=server.full)
     reqs = request_stream(1000.0, jobs / 1000.0 * 2.0 + 1.0, MIX_SCENES, seed=4, progressive_fraction=0.0)[:jobs]
-    for e, s in ((eng, server), (serve_eng, serve_server)):
+    for e, s in ((eng, server), (serve_eng, serve_server), (comp_eng, comp_server)):
         warm = [e.submit(s.scene_ids[r.scene], s.camera(r.scene, r), r.width, r.height, r.samples,
                          r.max_bounces) for r in reqs[:8]]  # graph capture, layouts
         e.wait_idle(timeout_ms=0)
@@ -320,6 +325,8 @@ def mixed_stream_report(seconds: float = 10.0, rate: float = 50.0, jobs: int = 2
         for j in warm:
             e.release(j)
     batch = {mode: closed_loop(server, reqs, mode) for mode in ("engine", "wavefront", "plain")}
+    batch["engine_compressed"] = closed_loop(comp_server, reqs, "engine")
+    comp_eng.close()
     samples = batch["plain"]["samples"]
     stream = request_stream(rate, seconds, MIX_SCENES, seed=5, progressive_fraction=0.1, fixed=(512, 512, 16, 8),
                             fixed_share=0.2)
@@ -340,8 +347,10 @@ def mixed_stream_report(seconds: float = 10.0, rate: float = 50.0, jobs: int = 2
                     f"20% 512x512x16 spp depth 8",
         "engine": eng_config_of(Engine.tuned_config()),
         "serving_engine": eng_config_of(dict(Engine.tuned_config(), wave_paths=Engine.SERVING_WAVE_PATHS)),
+        "compressed_engine": eng_config_of(dict(Engine.tuned_config(), precision=abi.PT_PRECISION_COMPRESSED)),
         "batching_samples_per_s": rate_of,
         "engine_over_plain": rate_of["engine"] / rate_of["plain"],
+        "engine_compressed_over_plain": rate_of["engine_compressed"] / rate_of["plain"],
         "wavefront_over_plain": rate_of["wavefront"] / rate_of["plain"],
         "serving": {"requests": len(stream), "completed": res.completed, "rejected": res.rejected,
                     "latency_ms": percentiles(res.latencies_ms),

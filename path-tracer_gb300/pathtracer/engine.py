@@ -20,8 +20,8 @@ class Engine:
     @staticmethod
     def tuned_config() -> dict:
         """The engine settings pte_autotune chose on the batching mix, in the FP16-attribute form
-        (FP16 attributes / BF16 skybox + Kahan sums on the binary BVH: 608 Msamples/s there against
-        570 for the full compressed form with the 8-wide BVH); engine_tuned.json, written by
+        (FP16 attributes / BF16 skybox + Kahan sums on the binary BVH: 640 Msamples/s there against
+        575 for the full compressed form with the 8-wide BVH); engine_tuned.json, written by
         `python -m pathtracer.serving --compare 256 --scenes 10k,100k,1M,4M --precision half
         --autotune --save-tuned`."""
         return json.loads(TUNED.read_text())["config"]
