@@ -6,9 +6,9 @@ wgpu.  WGSL defines its vector built-ins by formula but lets division,
 inverseSqrt and the transcendentals be inexact within ULP bounds, lets an
 implementation assume no NaN or infinity occurs, and lets drivers contract
 a*b+c into one fused operation.  So no single bit pattern is "the
-reference's"; the oracle and the CUDA kernels fix one reading, listed here
-and in the design doc, and each test below fails if the oracle's choice flips to
-a named alternative (every input set contains cases where the alternative
+reference's"; the oracle and the CUDA kernels fix one reading, listed here,
+and each test below fails if the oracle's choice flips to a named
+alternative (every input set contains cases where the alternative
 gives a different float32 result).  The kernels reproduce the oracle's bits
 (tests/test_gpu_parity.py), so these pins hold for them too.
 """
