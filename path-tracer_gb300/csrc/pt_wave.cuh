@@ -31,6 +31,12 @@ struct Queues {
     uint32_t* hit_list;   // slots of the current queue whose ray hit a triangle
     uint32_t* miss_list;  // slots whose ray left the scene
     uint32_t* hit_sorted = nullptr;  // the hit list sorted by key (when cnt[7] != 0)
+    // beside the hit list, each filed hit's triangle-bucket sort key (triangle
+    // >> key_shift, at most the last bucket), written by the extend kernel so
+    // that the sort reads its keys in order instead of gathering the hit
+    // records; null: the sort computes the keys itself
+    uint32_t* hit_keys = nullptr;
+    uint32_t key_shift = 0;
     uint32_t* cnt;  // [0], [1] ray queue lengths, [2] shadow length, [3] extend fetch, [4] shadow fetch,
                     // [5] hit list length, [6] miss list length, [7] 1 if hit_sorted holds this bounce's hits,
                     // [8] 1 if hit_sorted holds the order of the current ray queue, [9] of the shadow queue
@@ -1038,12 +1044,13 @@ PTD uint32_t warp_append(bool want, uint32_t* counter, unsigned mask) {
 // once per refill round (one global atomic per list and round).  A lane
 // finishes at most one ray per round, so 32 entries per list suffice.
 struct ResultFiler {
-    uint32_t* buf;   // this warp's [2][32] in shared memory: hits, misses
+    uint32_t* buf;   // this warp's [3][32] in shared memory: hits, misses, the hits' sort keys
     uint32_t* fill;  // this warp's [2] entry counts
-    PTD void file(uint32_t slot, bool is_hit) {
+    PTD void file(uint32_t slot, bool is_hit, uint32_t key = 0u) {
         const uint32_t b = is_hit ? 0u : 1u;
         const uint32_t j = atomicAdd(&fill[b], 1u);
         buf[b * 32u + j] = slot;
+        if (is_hit) buf[64u + j] = key;
     }
     // all 32 lanes, converged
     PTD void flush(const Queues& q, unsigned lane) {
@@ -1056,7 +1063,10 @@ struct ResultFiler {
         }
         bh = __shfl_sync(0xffffffffu, bh, 0);
         bm = __shfl_sync(0xffffffffu, bm, 0);
-        if (lane < nh) q.hit_list[bh + lane] = buf[lane];
+        if (lane < nh) {
+            q.hit_list[bh + lane] = buf[lane];
+            if (q.hit_keys) q.hit_keys[bh + lane] = buf[64u + lane];
+        }
         if (lane < nm) q.miss_list[bm + lane] = buf[32u + lane];
         __syncwarp();
         if (lane == 0u) fill[0] = fill[1] = 0u;
@@ -1067,7 +1077,7 @@ struct ResultFiler {
 // shared-memory buffers of the ResultFilers of one extend block
 template <int kThreads>
 struct FilerSlots {
-    uint32_t buf[kThreads / 32][64];
+    uint32_t buf[kThreads / 32][96];
     uint32_t fill[kThreads / 32][2];
     PTD ResultFiler of_warp(unsigned lane) {
         const unsigned wi = threadIdx.x >> 5;
@@ -1161,7 +1171,8 @@ __global__ void __launch_bounds__(kSortThreads) sort_count_kernel(World w, Queue
     for (uint32_t i = threadIdx.x; i < kSortBuckets; i += blockDim.x) hist[i] = 0u;
     __syncthreads();
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-        atomicAdd(&hist[hit_key<kMode>(w, q, q.hit_list[j], tri_shift)], 1u);
+        atomicAdd(&hist[kMode == 1 && q.hit_keys ? q.hit_keys[j] : hit_key<kMode>(w, q, q.hit_list[j], tri_shift)],
+                  1u);
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < kSortBuckets; i += blockDim.x)
         if (hist[i]) atomicAdd(&counts[i], hist[i]);
@@ -1288,7 +1299,7 @@ __global__ void __launch_bounds__(kSortThreads) sort_scatter_kernel(World w, Que
             keys[k] = 0xffffffffu;
             if (j < n) {
                 slots[k] = q.hit_list[j];
-                keys[k] = hit_key<kMode>(w, q, slots[k], tri_shift);
+                keys[k] = kMode == 1 && q.hit_keys ? q.hit_keys[j] : hit_key<kMode>(w, q, slots[k], tri_shift);
                 atomicAdd(&hist[keys[k]], 1u);
             }
         }

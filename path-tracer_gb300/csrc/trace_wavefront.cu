@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kExtendThreads, kWide ? PT_WIDE_MIN_BLOCKS : P
                 q.rec[path] = tr.c;
                 if (bounce < PT_RECORD_MAX_BOUNCES) q.rec_hits[(size_t)path * PT_RECORD_MAX_BOUNCES + bounce] = tr.hit;
             }
-            filer.file(slot, tr.hit != -1);
+            filer.file(slot, tr.hit != -1, min((uint32_t)tr.hit >> q.key_shift, kSortBuckets - 1u));
             return true;
         },
         [&]() { filer.flush(q, lane_id()); }, step_kind<PT_MAJORITY_EXTEND && !kWide>(tr, [&]() -> const Fast& { return f; }));
@@ -583,7 +583,8 @@ cudaError_t reserve_paths(Wavefront* wf, uint64_t paths, bool record) {
         for (Buf* x : {&l.o[0], &l.o[1], &l.d[0], &l.d[1], &l.T[0], &l.T[1], &l.hit, &l.color, &l.so, &l.sd, &l.sc})
             PTW_TRY(x->reserve(b));
         PTW_TRY(l.cnt.reserve(64));
-        PTW_TRY(l.lists.reserve(paths * 12 + 2 * ptd::kSortBuckets * 4));
+        // hit list, miss list, sorted hit list, sort counts and offsets, hit sort keys
+        PTW_TRY(l.lists.reserve(paths * 16 + 2 * ptd::kSortBuckets * 4));
         PTW_TRY(cudaMemset(static_cast<uint32_t*>(l.lists.p) + 3 * paths, 0, ptd::kSortBuckets * 4));  // sort counts
     }
     if (record) {
@@ -799,6 +800,10 @@ cudaError_t trace(Wavefront* wf, const ptd::World& w_in, const ptk::Tile& tile, 
         sort.counts = q.hit_sorted + wf->capacity;  // kSortBuckets counts, then kSortBuckets offsets
         sort.min_hits = PT_SORT_MIN_HITS;
         while (((uint64_t)ptd::kSortBuckets << sort.tri_shift) < wf->tri_count && sort.tri_shift < 31u) sort.tri_shift += 1u;
+        if (PT_SORT_KEY == 1) {  // the extend kernel files each hit's bucket beside the hit list
+            q.hit_keys = sort.counts + 2 * ptd::kSortBuckets;
+            q.key_shift = sort.tri_shift;
+        }
         const cudaStream_t as = record ? nullptr : stream;
         const ShadowSide* side = (!record && !serial && PT_SHADOW_SIDE) ? &l.side : nullptr;
         cudaError_t e;
