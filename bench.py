@@ -61,12 +61,12 @@ PRECISIONS = {"fp32": 0, "wide": 1, "half": 6, "compressed": 7}
 # (1920x1080, 64 spp, FP32 form), measured by a single-pass ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum) of the first 16-spp group's
 # 9 extend launches
-TRAFFIC_PER_LAUNCH: dict = {("wavefront", "extend", "fp32"): 561.2e6}
+TRAFFIC_PER_LAUNCH: dict = {("wavefront", "extend", "fp32"): 583.1e6}
 # warp instructions per path per launch of each kernel class (smsp__inst_executed.sum of the 9 launches
 # of each class of one 960x540 16-spp image of this scene, over 9 launches x 8,294,400 paths; the
 # per-path work of a launch does not depend on the image size); with the launch's paths and its
 # CUDA-event time they give the fraction of the SMs' issue slots the kernel fills
-WARP_INST_PER_PATH: dict = {("wavefront", "fp32"): {"extend": 94.40, "shade": 43.44, "shadow": 32.13},
+WARP_INST_PER_PATH: dict = {("wavefront", "fp32"): {"extend": 95.04, "shade": 43.44, "shadow": 32.12},
                              ("wavefront", "compressed"): {"extend": 121.68, "shade": 44.08, "shadow": 43.92}}
 SMS, SCHEDULERS_PER_SM = 152, 4
 
