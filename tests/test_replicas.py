@@ -76,3 +76,22 @@ def test_reference_arm_under_torchrun_prints_once():
     assert line["kernel"] == "cpu" and "kernel" not in line["config"]
     assert line["config"]["precision"] == "fp32" and line["config"]["parallelism"] == "replicas x2"
     assert line["config"]["image"] == [256, 256] and line["config"]["spp"] == 16
+
+
+def test_both_arms_print_one_workload_config():
+    # the GPU arm describes its world object, the reference arm the counts of the world it received as
+    # upload bytes: the same workload gives the same config dict, whichever implementation ran
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    class World:
+        def triangle_count(self):
+            return 2096640
+
+        def node_count(self):
+            return 2358439
+
+    ours = bench.workload_config(World(), "fp32", 1)
+    ref = bench.workload_config(bench._Counts({"triangles": 2096640, "bvh_nodes": 2358439}), "fp32", 1)
+    assert ours == ref and "kernel" not in ours
+    assert ours["precision"] == "fp32" and ours["parallelism"] == "replicas x1"
