@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <atomic>
 #include <climits>
+#include <exception>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -58,9 +59,15 @@ struct Json {
         const Json* j = get(key);
         return j && j->kind == Number ? j->num : dflt;
     }
+    // a number member as an integer (truncated); NaN and values outside the
+    // range of long become LONG_MIN, which every caller rejects as an index,
+    // count, offset or length
     long integer(const char* key, long dflt) const {
         const Json* j = get(key);
-        return j && j->kind == Number ? (long)j->num : dflt;
+        if (!j || j->kind != Number) return dflt;
+        const double v = j->num;
+        if (!(v > -9.2e18 && v < 9.2e18)) return LONG_MIN;
+        return (long)v;
     }
     std::string string(const char* key, const char* dflt) const {
         const Json* j = get(key);
@@ -339,6 +346,22 @@ struct AtlasSlot {
     float uv[4] = {0, 0, 0, 0};  // offset x, y, scale x, y
 };
 
+// largest accessor count accepted (elements): far beyond any scene this
+// renderer holds, small enough that count x stride cannot overflow
+constexpr long kMaxAccessorCount = 1L << 28;
+
+// an array element used as a node index: -1 (rejected as out of range) unless
+// it is a number within the range of long
+inline long index_of(const Json& j) {
+    if (j.kind != Json::Number || !(j.num > -9.2e18 && j.num < 9.2e18)) return -1;
+    return (long)j.num;
+}
+
+// [offset, offset + length) lies within a buffer of `size` bytes (no overflow)
+inline bool in_range(long offset, long length, size_t size) {
+    return offset >= 0 && length >= 0 && (unsigned long)offset <= size && (unsigned long)length <= size - (unsigned long)offset;
+}
+
 struct Loader {
     ptw_world* world;
     std::string dir;
@@ -546,9 +569,10 @@ struct Loader {
         if (comps != want_comps) return fail("accessor has type " + type);
         const long ctype = a.integer("componentType", 0);
         const bool norm = a.get("normalized") && a.get("normalized")->b;
-        const size_t n = (size_t)a.integer("count", 0);
+        const long cnt = a.integer("count", 0);
+        if (cnt < 0 || cnt > kMaxAccessorCount) return fail("accessor count out of range");
+        const size_t n = (size_t)cnt;
         const int csize = ctype == 5126 || ctype == 5125 ? 4 : ctype == 5123 || ctype == 5122 ? 2 : 1;
-        out.assign(n * comps, 0.0f);
         *count = n;
         const size_t elem = (size_t)csize * comps;
         if (a.get("bufferView")) {  // else all zeros before the sparse substitution
@@ -557,10 +581,13 @@ struct Loader {
             if (!view(a.integer("bufferView", -1), a.integer("byteOffset", 0), elem, &base, &stride, &avail))
                 return false;
             if (n && (n - 1) * stride + elem > avail) return fail("accessor runs past its buffer view");
+            out.assign(n * comps, 0.0f);
             for (size_t i = 0; i < n; ++i)
                 for (int c = 0; c < comps; ++c)
                     if (!component(base + i * stride + (size_t)c * csize, ctype, norm, &out[i * comps + c]))
                         return fail("unsupported accessor component type");
+        } else {
+            out.assign(n * comps, 0.0f);
         }
         return sparse(a, n, elem, [&](uint32_t i, const uint8_t* e) {
             for (int c = 0; c < comps; ++c)
@@ -576,8 +603,9 @@ struct Loader {
         const long ctype = a.integer("componentType", 0);
         const int csize = ctype == 5125 ? 4 : ctype == 5123 ? 2 : ctype == 5121 ? 1 : 0;
         if (!csize || a.string("type", "") != "SCALAR") return fail("index accessor must be unsigned SCALAR");
-        const size_t n = (size_t)a.integer("count", 0);
-        out.assign(n, 0u);
+        const long cnt = a.integer("count", 0);
+        if (cnt < 0 || cnt > kMaxAccessorCount) return fail("index accessor count out of range");
+        const size_t n = (size_t)cnt;
         const auto get = [&](const uint8_t* e) -> uint32_t {
             if (csize == 4) {
                 uint32_t u;
@@ -597,7 +625,10 @@ struct Loader {
             if (!view(a.integer("bufferView", -1), a.integer("byteOffset", 0), (size_t)csize, &base, &stride, &avail))
                 return false;
             if (n && (n - 1) * stride + (size_t)csize > avail) return fail("index accessor runs past its buffer view");
+            out.assign(n, 0u);
             for (size_t i = 0; i < n; ++i) out[i] = get(base + i * stride);
+        } else {
+            out.assign(n, 0u);
         }
         return sparse(a, n, (size_t)csize, [&](uint32_t i, const uint8_t* e) {
             out[i] = get(e);
@@ -612,10 +643,12 @@ struct Loader {
         const long b = v.integer("buffer", -1);
         if (b < 0 || (size_t)b >= buffers.size()) return fail("buffer out of range");
         const long voff = v.integer("byteOffset", 0), vlen = v.integer("byteLength", 0);
-        if (voff < 0 || vlen < 0 || offset < 0 || (size_t)(voff + vlen) > buffers[(size_t)b].size() || offset > vlen)
+        if (!in_range(voff, vlen, buffers[(size_t)b].size()) || offset < 0 || offset > vlen)
             return fail("buffer view out of range");
         *base = buffers[(size_t)b].data() + voff + offset;
         const long st = v.integer("byteStride", 0);
+        // glTF 2.0 3.6.2.4: a stride is a multiple of 4 in [4, 252]
+        if (v.get("byteStride") && (st < 4 || st > 252 || st % 4 != 0)) return fail("invalid buffer view byteStride");
         *stride = st > 0 ? (size_t)st : elem;
         *avail = (size_t)(vlen - offset);
         return true;
@@ -651,7 +684,7 @@ struct Loader {
         if (!views || vi < 0 || (size_t)vi >= views->arr.size()) return fail("image without uri or buffer view");
         const Json& v = views->arr[(size_t)vi];
         const long b = v.integer("buffer", -1), off = v.integer("byteOffset", 0), len = v.integer("byteLength", 0);
-        if (b < 0 || (size_t)b >= buffers.size() || off < 0 || len < 0 || (size_t)(off + len) > buffers[(size_t)b].size())
+        if (b < 0 || (size_t)b >= buffers.size() || !in_range(off, len, buffers[(size_t)b].size()))
             return fail("image buffer view out of range");
         out.assign(buffers[(size_t)b].begin() + off, buffers[(size_t)b].begin() + off + len);
         return true;
@@ -912,7 +945,7 @@ struct Loader {
         const long scene = doc.integer("scene", scenes && !scenes->arr.empty() ? 0 : -1);
         if (scene >= 0 && scenes && (size_t)scene < scenes->arr.size()) {
             if (const Json* sn = scenes->arr[(size_t)scene].get("nodes"))
-                for (const Json& n : sn->arr) roots.push_back((long)n.num);
+                for (const Json& n : sn->arr) roots.push_back(index_of(n));
         } else if (nodes) {
             for (size_t i = 0; i < nodes->arr.size(); ++i) roots.push_back((long)i);
         }
@@ -951,7 +984,7 @@ struct Loader {
                         if (!primitive(prim, model, nm)) return false;
             }
             if (const Json* ch = node.get("children"))
-                for (const Json& c : ch->arr) stack.emplace_back((long)c.num, model);
+                for (const Json& c : ch->arr) stack.emplace_back(index_of(c), model);
         }
         return true;
     }
@@ -971,6 +1004,9 @@ extern "C" int ptw_load_gltf_bytes(ptw_world* world, const void* bytes, size_t s
     } catch (const std::bad_alloc&) {
         if (error && error_size) snprintf(error, error_size, "out of host memory");
         return PT_ERR_OOM;
+    } catch (const std::exception& e) {  // nothing may leave the C ABI as an exception
+        if (error && error_size) snprintf(error, error_size, "glTF import failed: %s", e.what());
+        return PT_ERR_INVALID_ARG;
     }
     if (!ok && error && error_size) snprintf(error, error_size, "%s", l.error.c_str());
     return ok ? PT_OK : PT_ERR_INVALID_ARG;
@@ -986,6 +1022,9 @@ extern "C" int ptw_load_gltf(ptw_world* world, const char* path, char* error, si
     } catch (const std::bad_alloc&) {
         if (error && error_size) snprintf(error, error_size, "out of host memory");
         return PT_ERR_OOM;
+    } catch (const std::exception& e) {  // nothing may leave the C ABI as an exception
+        if (error && error_size) snprintf(error, error_size, "glTF import failed: %s", e.what());
+        return PT_ERR_INVALID_ARG;
     }
     if (!ok && error && error_size) snprintf(error, error_size, "%s", l.error.c_str());
     return ok ? PT_OK : PT_ERR_INVALID_ARG;

@@ -264,3 +264,51 @@ def test_sparse_accessors(tmp_path):
     a = w.attributes_raw()[np.argsort(w.bvh_order())].view(np.float32).reshape(2, 28)
     np.testing.assert_array_equal(a[0, 10:16], [0, 0, 0, 0, 0.25, 0.75])  # uv of vertex 2 from the sparse values
     w.close()
+
+
+def _edit_glb(path, edit):
+    """Rewrite the JSON chunk of a .glb written by write_gltf through edit(doc)."""
+    data = path.read_bytes()
+    jl = struct.unpack("<I", data[12:16])[0]
+    doc = json.loads(data[20:20 + jl])
+    rest = data[20 + jl:]
+    edit(doc)
+    js = json.dumps(doc).encode()
+    js += b" " * (-len(js) % 4)
+    body = struct.pack("<II", len(js), 0x4E4F534A) + js + rest
+    path.write_bytes(struct.pack("<4sII", b"glTF", 2, 12 + len(body)) + body)
+
+
+@pytest.mark.parametrize("field,value,message", [
+    # a count no long can hold, a count far beyond any buffer, a negative count
+    (("accessors", 1, "count"), 1e30, "count out of range"),
+    (("accessors", 1, "count"), 2 ** 40, "count out of range"),
+    (("accessors", 3, "count"), -5, "count out of range"),
+    # a stride whose product with the count wraps 64 bits, and one the format does not allow
+    (("bufferViews", 1, "byteStride"), 2 ** 60, "byteStride"),
+    (("bufferViews", 1, "byteStride"), 6, "byteStride"),
+    # offset + length past the end of the buffer without and with 64-bit wrap-around
+    (("bufferViews", 2, "byteOffset"), 2 ** 62, "out of range"),
+    (("bufferViews", 2, "byteLength"), 2 ** 63 - 1, "out of range"),
+    (("bufferViews", 2, "byteOffset"), -8, "out of range"),
+    # node indices that are not integers a long can hold
+    (("scenes", 0, "nodes"), [1e300], "node out of range"),
+])
+def test_hostile_numbers_are_refused(tmp_path, field, value, message):
+    """Accessor counts, strides, offsets and node indices taken from the file are checked before any
+    allocation or read they would size: a hostile file gets an error, never a crash or a read outside
+    the buffers (found by fuzzing the importer: a count of 1e30 once escaped as an exception)."""
+    path = write_gltf(tmp_path, [{"mesh": 0}], [0], [{}], True)
+    path.write_bytes(path.read_bytes())
+
+    def edit(doc):
+        obj = doc
+        for k in field[:-1]:
+            obj = obj[k]
+        obj[field[-1]] = value
+        if field[-1] == "byteStride":
+            doc["accessors"][1]["count"] = 17  # with a 2^60 stride, 16 x stride wraps to 0
+
+    _edit_glb(path, edit)
+    with pytest.raises(pt.PathTracerError, match=message):
+        pt.World.from_gltf(path)
