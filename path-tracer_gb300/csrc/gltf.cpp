@@ -992,6 +992,19 @@ struct Loader {
 
 }  // namespace
 
+namespace {
+// the message, with every byte outside printable ASCII (an echo of the file's
+// own bytes, e.g. a malformed name) shown as '?', so that callers always
+// receive plain text
+void printable_error(char* error, size_t size, const std::string& msg) {
+    if (!error || !size) return;
+    std::string clean(msg);
+    for (char& c : clean)
+        if ((unsigned char)c < 0x20 || (unsigned char)c > 0x7e) c = '?';
+    snprintf(error, size, "%s", clean.c_str());
+}
+}  // namespace
+
 extern "C" int ptw_load_gltf_bytes(ptw_world* world, const void* bytes, size_t size, char* error,
                                    size_t error_size) {
     if (!world || !bytes) return PT_ERR_INVALID_ARG;
@@ -1008,7 +1021,7 @@ extern "C" int ptw_load_gltf_bytes(ptw_world* world, const void* bytes, size_t s
         if (error && error_size) snprintf(error, error_size, "glTF import failed: %s", e.what());
         return PT_ERR_INVALID_ARG;
     }
-    if (!ok && error && error_size) snprintf(error, error_size, "%s", l.error.c_str());
+    if (!ok) printable_error(error, error_size, l.error);
     return ok ? PT_OK : PT_ERR_INVALID_ARG;
 }
 
@@ -1026,6 +1039,6 @@ extern "C" int ptw_load_gltf(ptw_world* world, const char* path, char* error, si
         if (error && error_size) snprintf(error, error_size, "glTF import failed: %s", e.what());
         return PT_ERR_INVALID_ARG;
     }
-    if (!ok && error && error_size) snprintf(error, error_size, "%s", l.error.c_str());
+    if (!ok) printable_error(error, error_size, l.error);
     return ok ? PT_OK : PT_ERR_INVALID_ARG;
 }

@@ -1551,8 +1551,14 @@ bool read_image(const char* path, std::vector<float>& rgba, uint32_t& w, uint32_
     return decode_image(data, rgba, w, h, err, size_only);
 }
 
+// the message, with every byte outside printable ASCII (an echo of the file's
+// own bytes) shown as '?', so that callers always receive plain text
 void put_error(char* error, size_t size, const std::string& msg) {
-    if (error && size) snprintf(error, size, "%s", msg.c_str());
+    if (!error || !size) return;
+    std::string clean(msg);
+    for (char& c : clean)
+        if ((unsigned char)c < 0x20 || (unsigned char)c > 0x7e) c = '?';
+    snprintf(error, size, "%s", clean.c_str());
 }
 
 }  // namespace

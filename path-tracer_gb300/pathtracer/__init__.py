@@ -63,7 +63,7 @@ class World:
         rc = w._lib.ptw_load_gltf(w._h, str(path).encode(), err, len(err))
         if rc != abi.PT_OK:
             w.close()
-            raise PathTracerError(rc, f"glTF import of {path}: {err.value.decode()}")
+            raise PathTracerError(rc, f"glTF import of {path}: {err.value.decode(errors="replace")}")
         if build:
             w.build()
         return w
@@ -77,7 +77,7 @@ class World:
         rc = w._lib.ptw_load_gltf_bytes(w._h, buf, len(data), err, len(err))
         if rc != abi.PT_OK:
             w.close()
-            raise PathTracerError(rc, f"glTF import: {err.value.decode()}")
+            raise PathTracerError(rc, f"glTF import: {err.value.decode(errors="replace")}")
         if build:
             w.build()
         return w
@@ -113,7 +113,7 @@ class World:
 
     def _check(self, rc: int) -> None:
         if rc != abi.PT_OK:
-            raise PathTracerError(rc, self._lib.ptw_last_error(self._h).decode())
+            raise PathTracerError(rc, self._lib.ptw_last_error(self._h).decode(errors="replace"))
 
     def close(self) -> None:
         if self._h:
@@ -169,7 +169,7 @@ class World:
         err = C.create_string_buffer(512)
         rc = self._lib.ptw_set_skybox_file(self._h, str(path).encode(), err, len(err))
         if rc != abi.PT_OK:
-            raise PathTracerError(rc, f"skybox {path}: {err.value.decode()}")
+            raise PathTracerError(rc, f"skybox {path}: {err.value.decode(errors="replace")}")
 
     def set_skybox_bytes(self, data: bytes) -> None:
         """Skybox from an .hdr / .exr image given as bytes (World::replace_skybox)."""
@@ -177,7 +177,7 @@ class World:
         buf = C.create_string_buffer(bytes(data), len(data))
         rc = self._lib.ptw_set_skybox_bytes(self._h, buf, len(data), err, len(err))
         if rc != abi.PT_OK:
-            raise PathTracerError(rc, f"skybox: {err.value.decode()}")
+            raise PathTracerError(rc, f"skybox: {err.value.decode(errors="replace")}")
 
     def edit_emission_scale(self, scale: float) -> None:
         """World::edit_emission_scale: emissive materials get their initial strength times `scale`."""
@@ -298,11 +298,11 @@ def read_image(path) -> np.ndarray:
     w, h = C.c_uint32(), C.c_uint32()
     rc = lib.ptw_read_image_rgba(str(path).encode(), None, 0, C.byref(w), C.byref(h), err, len(err))
     if rc != abi.PT_OK:
-        raise PathTracerError(rc, f"{path}: {err.value.decode()}")
+        raise PathTracerError(rc, f"{path}: {err.value.decode(errors="replace")}")
     out = np.empty((h.value, w.value, 4), np.float32)
     rc = lib.ptw_read_image_rgba(str(path).encode(), out.ctypes.data, out.size, C.byref(w), C.byref(h), err, len(err))
     if rc != abi.PT_OK:
-        raise PathTracerError(rc, f"{path}: {err.value.decode()}")
+        raise PathTracerError(rc, f"{path}: {err.value.decode(errors="replace")}")
     return out
 
 
@@ -312,7 +312,7 @@ def write_image(path, rgb: np.ndarray) -> None:
     err = C.create_string_buffer(512)
     rc = load().ptw_write_image(str(path).encode(), a.ctypes.data, a.shape[1], a.shape[0], err, len(err))
     if rc != abi.PT_OK:
-        raise PathTracerError(rc, err.value.decode())
+        raise PathTracerError(rc, err.value.decode(errors="replace"))
 
 
 def decode_texture(data: bytes) -> np.ndarray:
@@ -323,11 +323,11 @@ def decode_texture(data: bytes) -> np.ndarray:
     buf = C.create_string_buffer(bytes(data), len(data))
     rc = lib.ptw_decode_texture_rgba8(buf, len(data), None, 0, C.byref(w), C.byref(h), err, len(err))
     if rc != abi.PT_OK:
-        raise PathTracerError(rc, err.value.decode())
+        raise PathTracerError(rc, err.value.decode(errors="replace"))
     out = np.empty((h.value, w.value, 4), np.uint8)
     rc = lib.ptw_decode_texture_rgba8(buf, len(data), out.ctypes.data, out.size, C.byref(w), C.byref(h), err, len(err))
     if rc != abi.PT_OK:
-        raise PathTracerError(rc, err.value.decode())
+        raise PathTracerError(rc, err.value.decode(errors="replace"))
     return out
 
 
@@ -365,7 +365,7 @@ class PathTracer:
 
     def _check(self, rc: int) -> None:
         if rc != abi.PT_OK:
-            raise PathTracerError(rc, self._lib.pt_last_error(self._h).decode())
+            raise PathTracerError(rc, self._lib.pt_last_error(self._h).decode(errors="replace"))
 
     def close(self) -> None:
         if getattr(self, "_h", None):

@@ -65,7 +65,7 @@ class Engine:
 
     def _check(self, rc: int) -> None:
         if rc != abi.PT_OK:
-            raise PathTracerError(rc, self._lib.pte_last_error(self._h).decode())
+            raise PathTracerError(rc, self._lib.pte_last_error(self._h).decode(errors="replace"))
 
     def close(self) -> None:
         if getattr(self, "_h", None):
