@@ -26,6 +26,7 @@
 
 #include "../../include/pt_batch.h"
 #include "../../include/pt_precision.h"
+#include "pt_abi_guard.h"
 #include "pt_links.h"
 #include "pt_wave.cuh"
 #include "pt_wavefront.h"
@@ -1108,9 +1109,24 @@ static void pump_loop(pt_engine* e) {
     }
 }
 
+namespace {
+// inside a catch handler of an engine entry point: the status, with the
+// message kept as the engine's last error under its lock (the engine's
+// thread writes it too)
+int engine_abi_status(pt_engine* e) noexcept {
+    if (!e) return pt_abi_current_status(nullptr);
+    try {
+        std::lock_guard<std::recursive_mutex> lock(e->mu);
+        return pt_abi_current_status(&e->error);
+    } catch (...) {
+        return pt_abi_current_status(nullptr);
+    }
+}
+}  // namespace
+
 extern "C" {
 
-int pte_create(const pt_engine_config* cfg, pt_engine** out) {
+int pte_create(const pt_engine_config* cfg, pt_engine** out) try {
     if (!out) return PT_ERR_INVALID_ARG;
     *out = nullptr;
     pt_engine* e = new pt_engine();
@@ -1175,6 +1191,8 @@ int pte_create(const pt_engine_config* cfg, pt_engine** out) {
     }
     *out = e;
     return PT_OK;
+} catch (...) {
+    return pt_abi_current_status(nullptr);
 }
 
 void pte_destroy(pt_engine* e) {
@@ -1206,7 +1224,7 @@ const char* pte_last_error(const pt_engine* e) {
     return e->error.c_str();
 }
 
-int pte_scene_add(pt_engine* e, const pt_world_updates* u, uint64_t* scene_id) {
+int pte_scene_add(pt_engine* e, const pt_world_updates* u, uint64_t* scene_id) try {
     if (!e || !u || !scene_id) return PT_ERR_INVALID_ARG;
     std::lock_guard<std::recursive_mutex> lock(e->mu);
     if (e->sticky) return e->sticky;
@@ -1331,9 +1349,11 @@ int pte_scene_add(pt_engine* e, const pt_world_updates* u, uint64_t* scene_id) {
     e->stats.scenes_cached = e->scenes.size();
     *scene_id = h;
     return PT_OK;
+} catch (...) {
+    return engine_abi_status(e);
 }
 
-int pte_scene_release(pt_engine* e, uint64_t scene_id) {
+int pte_scene_release(pt_engine* e, uint64_t scene_id) try {
     if (!e) return PT_ERR_INVALID_ARG;
     std::lock_guard<std::recursive_mutex> lock(e->mu);
     if (e->sticky) return e->sticky;
@@ -1341,9 +1361,11 @@ int pte_scene_release(pt_engine* e, uint64_t scene_id) {
     if (it == e->scenes.end()) return e->fail(PT_ERR_INVALID_ARG, "unknown scene");
     it->second->caller_refs -= 1;
     return PT_OK;
+} catch (...) {
+    return engine_abi_status(e);
 }
 
-int pte_submit(pt_engine* e, const pt_job_desc* d, uint64_t* job_id) {
+int pte_submit(pt_engine* e, const pt_job_desc* d, uint64_t* job_id) try {
     if (!e || !d || !job_id) return PT_ERR_INVALID_ARG;
     std::lock_guard<std::recursive_mutex> lock(e->mu);
     if (e->sticky) return e->sticky;
@@ -1412,9 +1434,11 @@ int pte_submit(pt_engine* e, const pt_job_desc* d, uint64_t* job_id) {
     if (rc) return rc;
     *job_id = j.id;
     return pump(e);
+} catch (...) {
+    return engine_abi_status(e);
 }
 
-int pte_poll(pt_engine* e, uint32_t timeout_ms, uint64_t* done, uint32_t capacity, uint32_t* count) {
+int pte_poll(pt_engine* e, uint32_t timeout_ms, uint64_t* done, uint32_t capacity, uint32_t* count) try {
     if (!e || !count || (capacity && !done)) return PT_ERR_INVALID_ARG;
     cudaSetDevice(e->cfg.device);
     *count = 0;
@@ -1434,9 +1458,11 @@ int pte_poll(pt_engine* e, uint32_t timeout_ms, uint64_t* done, uint32_t capacit
         }
         std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
+} catch (...) {
+    return engine_abi_status(e);
 }
 
-int pte_wait_idle(pt_engine* e, uint32_t timeout_ms) {
+int pte_wait_idle(pt_engine* e, uint32_t timeout_ms) try {
     if (!e) return PT_ERR_INVALID_ARG;
     cudaSetDevice(e->cfg.device);
     const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
@@ -1455,9 +1481,11 @@ int pte_wait_idle(pt_engine* e, uint32_t timeout_ms) {
         }
         std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
+} catch (...) {
+    return engine_abi_status(e);
 }
 
-int pte_job_status(pt_engine* e, uint64_t id, int* status, uint32_t* samples_done) {
+int pte_job_status(pt_engine* e, uint64_t id, int* status, uint32_t* samples_done) try {
     if (!e) return PT_ERR_INVALID_ARG;
     std::lock_guard<std::recursive_mutex> lock(e->mu);
     if (e->sticky) return e->sticky;
@@ -1466,9 +1494,11 @@ int pte_job_status(pt_engine* e, uint64_t id, int* status, uint32_t* samples_don
     if (status) *status = it->second.status;
     if (samples_done) *samples_done = it->second.acc ? it->second.acc->samples_done : 0;
     return PT_OK;
+} catch (...) {
+    return engine_abi_status(e);
 }
 
-int pte_job_read(pt_engine* e, uint64_t id, int which, float* host) {
+int pte_job_read(pt_engine* e, uint64_t id, int which, float* host) try {
     if (!e || !host || (which != PT_TILE_IMAGE && which != PT_TILE_ACCUMULATION && which != PT_TILE_COMPENSATION))
         return PT_ERR_INVALID_ARG;
     std::lock_guard<std::recursive_mutex> lock(e->mu);
@@ -1486,9 +1516,11 @@ int pte_job_read(pt_engine* e, uint64_t id, int which, float* host) {
     int rc = e->cuda(cudaMemcpyAsync(host, b.p, (size_t)a.width * a.height * 16, cudaMemcpyDeviceToHost, e->stream), "job readback");
     if (!rc) rc = e->cuda(cudaStreamSynchronize(e->stream), "job readback");
     return rc;
+} catch (...) {
+    return engine_abi_status(e);
 }
 
-int pte_job_release(pt_engine* e, uint64_t id) {
+int pte_job_release(pt_engine* e, uint64_t id) try {
     if (!e) return PT_ERR_INVALID_ARG;
     std::lock_guard<std::recursive_mutex> lock(e->mu);
     if (e->sticky) return e->sticky;
@@ -1506,9 +1538,11 @@ int pte_job_release(pt_engine* e, uint64_t id) {
         }
     }
     return PT_OK;
+} catch (...) {
+    return engine_abi_status(e);
 }
 
-int pte_stats(pt_engine* e, pt_engine_stats* s) {
+int pte_stats(pt_engine* e, pt_engine_stats* s) try {
     if (!e || !s) return PT_ERR_INVALID_ARG;
     std::lock_guard<std::recursive_mutex> lock(e->mu);
     *s = e->stats;
@@ -1524,9 +1558,11 @@ int pte_stats(pt_engine* e, pt_engine_stats* s) {
     s->traversal_threads = e->cfg.traversal_threads;
     s->shade_threads = e->cfg.shade_threads;
     return PT_OK;
+} catch (...) {
+    return engine_abi_status(e);
 }
 
-int pte_autotune(pt_engine* e, const pt_job_desc* jobs, uint32_t count, pt_engine_config* chosen) {
+int pte_autotune(pt_engine* e, const pt_job_desc* jobs, uint32_t count, pt_engine_config* chosen) try {
     if (!e || !jobs || count == 0) return PT_ERR_INVALID_ARG;
     std::lock_guard<std::recursive_mutex> lock(e->mu);
     if (e->sticky) return e->sticky;
@@ -1605,6 +1641,8 @@ int pte_autotune(pt_engine* e, const pt_job_desc* jobs, uint32_t count, pt_engin
     drop_graphs(e);
     if (chosen) *chosen = best;
     return PT_OK;
+} catch (...) {
+    return engine_abi_status(e);
 }
 
 }  // extern "C"

@@ -17,6 +17,7 @@
 
 #include "../../include/pt.h"
 #include "../../include/pt_precision.h"
+#include "pt_abi_guard.h"
 #include "pt_kernels.h"
 #include "pt_wavefront.h"
 
@@ -588,7 +589,7 @@ int trace_impl(pt_ctx* c, uint32_t samples, uint32_t* traced, pt_path_record* ho
 
 extern "C" {
 
-int pt_create(int device, const pt_world_updates* updates, uint32_t tile_width, uint32_t tile_height, pt_ctx** out) {
+int pt_create(int device, const pt_world_updates* updates, uint32_t tile_width, uint32_t tile_height, pt_ctx** out) try {
     if (!out) return PT_ERR_INVALID_ARG;
     *out = nullptr;
     pt_ctx* c = new pt_ctx();
@@ -619,6 +620,8 @@ int pt_create(int device, const pt_world_updates* updates, uint32_t tile_width, 
     c->params.sample_count = 0;
     *out = c;
     return PT_OK;
+} catch (...) {
+    return pt_abi_current_status(nullptr);
 }
 
 void pt_destroy(pt_ctx* c) {
@@ -636,13 +639,15 @@ void pt_destroy(pt_ctx* c) {
     delete c;
 }
 
-int pt_apply_updates(pt_ctx* c, const pt_world_updates* u) {
+int pt_apply_updates(pt_ctx* c, const pt_world_updates* u) try {
     if (!c) return PT_ERR_INVALID_ARG;
     cudaSetDevice(c->device);
     return apply(c, u, false);
+} catch (...) {
+    return pt_abi_status(c);
 }
 
-int pt_set_tile(pt_ctx* c, const uint32_t image_size[2], const uint32_t origin[2], const uint32_t size[2]) {
+int pt_set_tile(pt_ctx* c, const uint32_t image_size[2], const uint32_t origin[2], const uint32_t size[2]) try {
     if (!c || !image_size || !origin || !size) return PT_ERR_INVALID_ARG;
     if (!(origin[0] < image_size[0] && origin[1] < image_size[1]))
         return c->fail(PT_ERR_INVALID_ARG, "tile origin must be within the image");
@@ -657,9 +662,11 @@ int pt_set_tile(pt_ctx* c, const uint32_t image_size[2], const uint32_t origin[2
     c->params.tile_origin[1] = origin[1];
     c->params.sample_count = 0;
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(c);
 }
 
-int pt_set_max_bounces(pt_ctx* c, uint32_t max_bounces) {
+int pt_set_max_bounces(pt_ctx* c, uint32_t max_bounces) try {
     if (!c) return PT_ERR_INVALID_ARG;
     if (max_bounces > PT_MAX_BOUNCES_LIMIT) return c->fail(PT_ERR_INVALID_ARG, "max bounces must be at most 16");
     if (c->params.max_bounces != max_bounces) {
@@ -667,30 +674,38 @@ int pt_set_max_bounces(pt_ctx* c, uint32_t max_bounces) {
         c->params.sample_count = 0;
     }
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(c);
 }
 
 uint32_t pt_max_bounces(const pt_ctx* c) { return c ? c->params.max_bounces : 0; }
 uint32_t pt_sample_count(const pt_ctx* c) { return c ? c->params.sample_count : 0; }
 
-int pt_trace(pt_ctx* c, uint32_t samples, uint32_t* traced) {
+int pt_trace(pt_ctx* c, uint32_t samples, uint32_t* traced) try {
     if (!c) return PT_ERR_INVALID_ARG;
     cudaSetDevice(c->device);
     return trace_impl(c, samples, traced, nullptr, nullptr);
+} catch (...) {
+    return pt_abi_status(c);
 }
 
-int pt_trace_counted(pt_ctx* c, uint32_t samples, uint32_t* traced, uint64_t totals[PT_COUNT_FIELDS]) {
+int pt_trace_counted(pt_ctx* c, uint32_t samples, uint32_t* traced, uint64_t totals[PT_COUNT_FIELDS]) try {
     if (!c || !totals) return PT_ERR_INVALID_ARG;
     cudaSetDevice(c->device);
     return trace_impl(c, samples, traced, nullptr, totals);
+} catch (...) {
+    return pt_abi_status(c);
 }
 
-int pt_trace_recorded(pt_ctx* c, uint32_t samples, uint32_t* traced, pt_path_record* host_records) {
+int pt_trace_recorded(pt_ctx* c, uint32_t samples, uint32_t* traced, pt_path_record* host_records) try {
     if (!c || !host_records) return PT_ERR_INVALID_ARG;
     cudaSetDevice(c->device);
     return trace_impl(c, samples, traced, host_records, nullptr);
+} catch (...) {
+    return pt_abi_status(c);
 }
 
-int pt_read_tile(pt_ctx* c, int which, float* host_rgba) {
+int pt_read_tile(pt_ctx* c, int which, float* host_rgba) try {
     if (!c || !host_rgba || (which != PT_TILE_IMAGE && which != PT_TILE_ACCUMULATION && which != PT_TILE_COMPENSATION))
         return PT_ERR_INVALID_ARG;
     c->touched();
@@ -704,9 +719,11 @@ int pt_read_tile(pt_ctx* c, int which, float* host_rgba) {
                      "tile readback");
     if (!rc) rc = c->cuda(cudaStreamSynchronize(c->stream), "tile readback");
     return rc;
+} catch (...) {
+    return pt_abi_status(c);
 }
 
-int pt_display_tile(pt_ctx* c, uint8_t* host_rgba8) {
+int pt_display_tile(pt_ctx* c, uint8_t* host_rgba8) try {
     if (!c || !host_rgba8) return PT_ERR_INVALID_ARG;
     c->touched();
     cudaSetDevice(c->device);
@@ -718,9 +735,11 @@ int pt_display_tile(pt_ctx* c, uint8_t* host_rgba8) {
     if (!rc) rc = c->cuda(cudaMemcpyAsync(host_rgba8, c->display.p, px * 4, cudaMemcpyDeviceToHost, c->stream), "display readback");
     if (!rc) rc = c->cuda(cudaStreamSynchronize(c->stream), "display readback");
     return rc;
+} catch (...) {
+    return pt_abi_status(c);
 }
 
-int pt_synchronize(pt_ctx* c, uint32_t timeout_ms) {
+int pt_synchronize(pt_ctx* c, uint32_t timeout_ms) try {
     if (!c) return PT_ERR_INVALID_ARG;
     cudaSetDevice(c->device);
     if (timeout_ms == 0) return c->cuda(cudaStreamSynchronize(c->stream), "synchronize");
@@ -732,20 +751,24 @@ int pt_synchronize(pt_ctx* c, uint32_t timeout_ms) {
         if (std::chrono::steady_clock::now() >= deadline) return c->fail(PT_ERR_TIMEOUT, "queued work did not finish in time");
         std::this_thread::sleep_for(std::chrono::microseconds(200));
     }
+} catch (...) {
+    return pt_abi_status(c);
 }
 
 const char* pt_last_error(const pt_ctx* c) { return c ? c->error.c_str() : "null context"; }
 
-int pt_set_kernel(pt_ctx* c, int kernel) {
+int pt_set_kernel(pt_ctx* c, int kernel) try {
     if (!c) return PT_ERR_INVALID_ARG;
     if (kernel != PT_KERNEL_WAVEFRONT && kernel != PT_KERNEL_PLAIN) return c->fail(PT_ERR_INVALID_ARG, "unknown kernel");
     if (kernel == PT_KERNEL_PLAIN && c->precision != PT_PRECISION_FP32)
         return c->fail(PT_ERR_STATE, "the precision form runs on the wavefront kernels");
     c->kernel = kernel;
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(c);
 }
 
-int pt_set_precision(pt_ctx* c, uint32_t flags) {
+int pt_set_precision(pt_ctx* c, uint32_t flags) try {
     if (!c) return PT_ERR_INVALID_ARG;
     c->touched();
     if (flags & ~PT_PRECISION_COMPRESSED) return c->fail(PT_ERR_INVALID_ARG, "unknown precision bits");
@@ -761,25 +784,31 @@ int pt_set_precision(pt_ctx* c, uint32_t flags) {
     }
     c->params.sample_count = 0;
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(c);
 }
 
 uint32_t pt_precision(const pt_ctx* c) { return c ? c->precision : 0u; }
 uint32_t pt_precision_active(const pt_ctx* c) { return c ? c->precision_active : 0u; }
 
-int pt_get_stream(pt_ctx* c, void** stream) {
+int pt_get_stream(pt_ctx* c, void** stream) try {
     if (!c || !stream) return PT_ERR_INVALID_ARG;
     c->touched();
     *stream = (void*)c->stream;
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(c);
 }
 
-int pt_set_profiling(pt_ctx* c, int enabled) {
+int pt_set_profiling(pt_ctx* c, int enabled) try {
     if (!c) return PT_ERR_INVALID_ARG;
     c->profiling = enabled != 0;
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(c);
 }
 
-int pt_get_kernel_times(pt_ctx* c, uint64_t launches[PT_KERNEL_CLASS_COUNT], double ms[PT_KERNEL_CLASS_COUNT]) {
+int pt_get_kernel_times(pt_ctx* c, uint64_t launches[PT_KERNEL_CLASS_COUNT], double ms[PT_KERNEL_CLASS_COUNT]) try {
     if (!c || !launches || !ms) return PT_ERR_INVALID_ARG;
     cudaSetDevice(c->device);
     c->harvest();
@@ -788,9 +817,11 @@ int pt_get_kernel_times(pt_ctx* c, uint64_t launches[PT_KERNEL_CLASS_COUNT], dou
         ms[i] = c->class_ms[i];
     }
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(c);
 }
 
-int pt_reset_kernel_times(pt_ctx* c) {
+int pt_reset_kernel_times(pt_ctx* c) try {
     if (!c) return PT_ERR_INVALID_ARG;
     cudaSetDevice(c->device);
     c->harvest();
@@ -799,11 +830,13 @@ int pt_reset_kernel_times(pt_ctx* c) {
         c->class_ms[i] = 0.0;
     }
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(c);
 }
 
 uint64_t pt_launch_count(const pt_ctx* c) { return c ? c->launch_count : 0; }
 
-int pt_render_fp64(pt_ctx* c, uint32_t sample_first, uint32_t sample_count, double* host_rgb_sums) {
+int pt_render_fp64(pt_ctx* c, uint32_t sample_first, uint32_t sample_count, double* host_rgb_sums) try {
     if (!c || !host_rgb_sums) return PT_ERR_INVALID_ARG;
     c->touched();
     if (sample_first == 0 || sample_count == 0 || sample_count - 1u > 0xffffffffu - sample_first)
@@ -820,10 +853,12 @@ int pt_render_fp64(pt_ctx* c, uint32_t sample_first, uint32_t sample_count, doub
     if (!rc) rc = c->cuda(cudaMemcpyAsync(host_rgb_sums, c->fp64.p, bytes, cudaMemcpyDeviceToHost, c->stream), "FP64 readback");
     if (!rc) rc = c->cuda(cudaStreamSynchronize(c->stream), "FP64 render");
     return rc;
+} catch (...) {
+    return pt_abi_status(c);
 }
 
 int pt_debug_intersect(pt_ctx* c, uint64_t n, const float* origins, const float* directions, const float* t_max,
-                       int32_t* hit, float* hit_t, pt_path_record* records) {
+                       int32_t* hit, float* hit_t, pt_path_record* records) try {
     if (!c || !origins || !directions || !t_max || !hit || !hit_t) return PT_ERR_INVALID_ARG;
     c->touched();
     if (!c->world_ready) return c->fail(PT_ERR_STATE, "no world uploaded");
@@ -858,6 +893,8 @@ int pt_debug_intersect(pt_ctx* c, uint64_t n, const float* origins, const float*
     if (!rc) rc = c->cuda(cudaStreamSynchronize(c->stream), "debug intersect");
     for (DevBuf* b : {&o, &d, &tm, &h, &ht, &rec}) b->release();
     return rc;
+} catch (...) {
+    return pt_abi_status(c);
 }
 
 }  // extern "C"

@@ -10,6 +10,7 @@
 #include <map>
 #include <vector>
 
+#include "pt_abi_guard.h"
 #include "../../include/pt_world.h"
 #include "pt_fmath.h"
 
@@ -266,7 +267,7 @@ struct TextureAtlas {
 
 extern "C" {
 
-int ptw_scene_cornell_box(ptw_world** out) {
+int ptw_scene_cornell_box(ptw_world** out) try {
     if (!out) return PT_ERR_INVALID_ARG;
     ptw_world* w = nullptr;
     ptw_create(&w);
@@ -310,9 +311,11 @@ int ptw_scene_cornell_box(ptw_world** out) {
     }
     *out = w;
     return PT_OK;
+} catch (...) {
+    return pt_abi_current_status(nullptr);
 }
 
-int ptw_scene_cornell_box_textured(uint64_t seed, ptw_world** out) {
+int ptw_scene_cornell_box_textured(uint64_t seed, ptw_world** out) try {
     if (!out) return PT_ERR_INVALID_ARG;
     ptw_world* w = nullptr;
     ptw_create(&w);
@@ -357,10 +360,12 @@ int ptw_scene_cornell_box_textured(uint64_t seed, ptw_world** out) {
     }
     *out = w;
     return PT_OK;
+} catch (...) {
+    return pt_abi_current_status(nullptr);
 }
 
 // sky: vertical gradient plus a Gaussian sun lobe, equirectangular, top row up
-int ptw_set_procedural_skybox(ptw_world* w, uint32_t W, uint32_t H) {
+int ptw_set_procedural_skybox(ptw_world* w, uint32_t W, uint32_t H) try {
     if (!w || W == 0 || H == 0) return PT_ERR_INVALID_ARG;
     std::vector<float> px((size_t)W * H * 4);
     const V3 sun = normalize(V3{-0.45f, 0.64f, -0.62f});
@@ -393,6 +398,8 @@ int ptw_set_procedural_skybox(ptw_world* w, uint32_t W, uint32_t H) {
         }
     }
     return ptw_set_skybox_rgba(w, px.data(), W, H);
+} catch (...) {
+    return pt_abi_current_status(nullptr);  // the world is opaque here: the status alone
 }
 
 void ptw_procedural_defaults(ptw_procedural_params* p) {
@@ -412,7 +419,7 @@ void ptw_procedural_defaults(ptw_procedural_params* p) {
     p->non_opaque = 0;
 }
 
-int ptw_scene_procedural(const ptw_procedural_params* params, ptw_world** out) {
+int ptw_scene_procedural(const ptw_procedural_params* params, ptw_world** out) try {
     if (!params || !out) return PT_ERR_INVALID_ARG;
     const ptw_procedural_params& P = *params;
     if (P.grid_x == 0 || P.grid_z == 0 || P.sphere_subdivision > 7) return PT_ERR_INVALID_ARG;
@@ -538,6 +545,8 @@ int ptw_scene_procedural(const ptw_procedural_params* params, ptw_world** out) {
     }
     *out = w;
     return PT_OK;
+} catch (...) {
+    return pt_abi_current_status(nullptr);
 }
 
 }  // extern "C"

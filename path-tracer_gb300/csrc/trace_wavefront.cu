@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/pt_precision.h"
+#include "pt_abi_guard.h"
 #include "pt_links.h"
 #include "pt_wave.cuh"
 #include "pt_wavefront.h"
@@ -955,7 +956,7 @@ int noalloc_setup(int dev, char* error, size_t size) {
 
 extern "C" int pt_trace_noalloc(const pt_device_world* world, const pt_trace_parameters* params, uint32_t tile_width,
                                 uint32_t tile_height, uint32_t samples, float* accum, float* image, void* stream,
-                                char* error, size_t error_size) {
+                                char* error, size_t error_size) try {
     if (!world || !params || !accum || !image)
         return noalloc_fail(error, error_size, PT_ERR_INVALID_ARG, "world, params, accum and image are required");
     if (!world->geometries || !world->attributes || !world->materials || !world->bvh_nodes || !world->skybox_rgba ||
@@ -1061,4 +1062,8 @@ extern "C" int pt_trace_noalloc(const pt_device_world* world, const pt_trace_par
                               ? ptw::run_group<false, true, true>(g_noalloc_devices[dev].sms, w, f, q, t, g, ptk::Sinks{nullptr, nullptr}, s, untimed)
                               : ptw::run_group<false, false, true>(g_noalloc_devices[dev].sms, w, f, q, t, g, ptk::Sinks{nullptr, nullptr}, s, untimed);
     return noalloc_cuda(error, error_size, e, "trace launch");
+} catch (...) {
+    std::string message;
+    const int rc = pt_abi_current_status(&message);
+    return noalloc_fail(error, error_size, rc, message.c_str());
 }

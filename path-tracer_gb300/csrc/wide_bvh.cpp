@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/pt_precision.h"
+#include "pt_abi_guard.h"
 #include "pt_links.h"
 
 namespace {
@@ -318,7 +319,7 @@ int ptw::build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, uint32_t 
 }
 
 extern "C" int pt_build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, uint32_t max_leaf_triangles,
-                                 pt_wide_node* out, uint64_t capacity, uint64_t* wide_count, uint32_t* wide_depth) {
+                                 pt_wide_node* out, uint64_t capacity, uint64_t* wide_count, uint32_t* wide_depth) try {
     std::vector<pt_wide_node> wide;
     const int rc = collapse(nodes, node_count, max_leaf_triangles, wide, wide_depth);
     if (rc != PT_OK) return rc;
@@ -328,6 +329,8 @@ extern "C" int pt_build_wide_bvh(const pt_bvh_node* nodes, uint64_t node_count, 
     order_all_by_octant(wide);
     std::memcpy(out, wide.data(), wide.size() * sizeof(pt_wide_node));
     return PT_OK;
+} catch (...) {
+    return pt_abi_current_status(nullptr);
 }
 
 namespace {

@@ -15,6 +15,7 @@
 
 #include "../../include/pt_world.h"
 #include "pt_fmath.h"
+#include "pt_abi_guard.h"
 #include "pt_mikktspace.h"
 
 namespace {
@@ -513,10 +514,12 @@ Vec3 tri_normal(Vec3 a, Vec3 b, Vec3 c) { return normalize(cross(b - a, c - a));
 
 extern "C" {
 
-int ptw_create(ptw_world** out) {
+int ptw_create(ptw_world** out) try {
     if (!out) return PT_ERR_INVALID_ARG;
     *out = new ptw_world();
     return PT_OK;
+} catch (...) {
+    return pt_abi_current_status(nullptr);
 }
 
 void ptw_destroy(ptw_world* w) { delete w; }
@@ -550,15 +553,17 @@ void ptw_default_material(pt_material* m) {
     m->specular_weight_tex_layer = -1;
 }
 
-int ptw_add_material(ptw_world* w, const pt_material* m, uint32_t* index) {
+int ptw_add_material(ptw_world* w, const pt_material* m, uint32_t* index) try {
     if (!w || !m) return PT_ERR_INVALID_ARG;
     if (w->built) return w->fail(PT_ERR_STATE, "materials must be added before ptw_build");
     if (index) *index = (uint32_t)w->materials.size();
     w->materials.push_back(*m);
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(w);
 }
 
-int ptw_add_atlas_layer(ptw_world* w, int srgb, const uint8_t* rgba8, int32_t* layer) {
+int ptw_add_atlas_layer(ptw_world* w, int srgb, const uint8_t* rgba8, int32_t* layer) try {
     if (!w || !rgba8) return PT_ERR_INVALID_ARG;
     if (w->built) return w->fail(PT_ERR_STATE, "atlas layers must be added before ptw_build");
     auto& layers = srgb ? w->srgb_layers : w->linear_layers;
@@ -566,10 +571,12 @@ int ptw_add_atlas_layer(ptw_world* w, int srgb, const uint8_t* rgba8, int32_t* l
     layers.emplace_back(rgba8, rgba8 + bytes);
     if (layer) *layer = (int32_t)layers.size() - 1;
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(w);
 }
 
 // triangle intake, world.rs:1152-1331
-int ptw_add_mesh(ptw_world* w, const ptw_mesh* mesh) {
+int ptw_add_mesh(ptw_world* w, const ptw_mesh* mesh) try {
     if (!w || !mesh || !mesh->positions) return PT_ERR_INVALID_ARG;
     if (w->built) return w->fail(PT_ERR_STATE, "meshes must be added before ptw_build");
     if (mesh->material_index >= w->materials.size())
@@ -679,9 +686,11 @@ int ptw_add_mesh(ptw_world* w, const ptw_mesh* mesh) {
         w->in_attrs.push_back(at);
     }
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(w);
 }
 
-int ptw_build(ptw_world* w) {
+int ptw_build(ptw_world* w) try {
     if (!w) return PT_ERR_INVALID_ARG;
     if (w->built) return w->fail(PT_ERR_STATE, "world already built");
     if (w->in_geos.empty()) return w->fail(PT_ERR_INVALID_ARG, "scene has no triangles");
@@ -713,9 +722,11 @@ int ptw_build(ptw_world* w) {
     w->built = true;
     w->full_upload = true;
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(w);
 }
 
-int ptw_set_skybox_rgba(ptw_world* w, const float* rgba, uint32_t width, uint32_t height) {
+int ptw_set_skybox_rgba(ptw_world* w, const float* rgba, uint32_t width, uint32_t height) try {
     if (!w || !rgba || width == 0 || height == 0) return PT_ERR_INVALID_ARG;
     Skybox s = make_skybox(rgba, width, height);
     if (!w->taken_once) {
@@ -727,16 +738,20 @@ int ptw_set_skybox_rgba(ptw_world* w, const float* rgba, uint32_t width, uint32_
         w->pending_skybox = true;
     }
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(w);
 }
 
-int ptw_edit_skybox_average_luminance(ptw_world* w, float luminance) {
+int ptw_edit_skybox_average_luminance(ptw_world* w, float luminance) try {
     if (!w) return PT_ERR_INVALID_ARG;
     w->pending_luminance = true;
     w->next_luminance = std::fmax(luminance, 0.0f);
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(w);
 }
 
-int ptw_set_aspect_ratio(ptw_world* w, float aspect) {
+int ptw_set_aspect_ratio(ptw_world* w, float aspect) try {
     if (!w) return PT_ERR_INVALID_ARG;
     if (!(std::isfinite(aspect) && aspect > 0.0f))
         return w->fail(PT_ERR_INVALID_ARG, "Aspect ratio must be finite and positive.");
@@ -749,9 +764,11 @@ int ptw_set_aspect_ratio(ptw_world* w, float aspect) {
         w->next_camera.aspect_ratio = aspect;
     }
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(w);
 }
 
-int ptw_edit_camera(ptw_world* w, const float* position, const float* yaw, const float* pitch, const float* fov) {
+int ptw_edit_camera(ptw_world* w, const float* position, const float* yaw, const float* pitch, const float* fov) try {
     if (!w) return PT_ERR_INVALID_ARG;
     if (!w->pending_camera) {
         w->next_camera = w->camera;
@@ -765,9 +782,11 @@ int ptw_edit_camera(ptw_world* w, const float* position, const float* yaw, const
     else c.pitch = std::fmin(std::fmax(c.pitch, -half_pi), half_pi);
     if (fov) c.fov = std::fmin(std::fmax(*fov, 0.0f), 3.14159265358979323846f - std::numeric_limits<float>::epsilon());
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(w);
 }
 
-int ptw_edit_material(ptw_world* w, uint32_t index, const pt_material* m) {
+int ptw_edit_material(ptw_world* w, uint32_t index, const pt_material* m) try {
     if (!w || !m) return PT_ERR_INVALID_ARG;
     if (index >= w->materials.size()) return w->fail(PT_ERR_INVALID_ARG, "material index out of range");
     const float* f = reinterpret_cast<const float*>(m);
@@ -781,12 +800,14 @@ int ptw_edit_material(ptw_world* w, uint32_t index, const pt_material* m) {
     else
         w->pending_materials[index] = accepted;
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(w);
 }
 
 // World::edit_emission_scale, world.rs:655-692: every emissive material
 // (emission colour luminance times emission weight above 0) gets its initial
 // emission strength times `scale`, replacing edits of that value
-int ptw_edit_emission_scale(ptw_world* w, float scale) {
+int ptw_edit_emission_scale(ptw_world* w, float scale) try {
     if (!w) return PT_ERR_INVALID_ARG;
     if (!w->built) return w->fail(PT_ERR_STATE, "ptw_build has not run");
     if (std::isnan(scale)) return w->fail(PT_ERR_INVALID_ARG, "scale must not be NaN");
@@ -804,12 +825,14 @@ int ptw_edit_emission_scale(ptw_world* w, float scale) {
             w->pending_materials[i] = edited;
     }
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(w);
 }
 
 float ptw_emission_scale(const ptw_world* w) { return w ? w->emission_scale : 0.0f; }
 
 // World::take_updates, world.rs:790-884
-int ptw_take_updates(ptw_world* w, pt_world_updates* out) {
+int ptw_take_updates(ptw_world* w, pt_world_updates* out) try {
     if (!w || !out) return PT_ERR_INVALID_ARG;
     if (!w->built) return w->fail(PT_ERR_STATE, "ptw_build has not run");
     std::memset(out, 0, sizeof(*out));
@@ -897,6 +920,8 @@ int ptw_take_updates(ptw_world* w, pt_world_updates* out) {
     w->pending_materials.clear();
     w->taken_once = true;
     return PT_OK;
+} catch (...) {
+    return pt_abi_status(w);
 }
 
 uint64_t ptw_triangle_count(const ptw_world* w) { return w ? w->geos.size() : 0; }
@@ -909,15 +934,17 @@ const pt_material* ptw_materials(const ptw_world* w) { return w ? w->materials.d
 const uint32_t* ptw_bvh_order(const ptw_world* w) { return w ? w->order.data() : nullptr; }
 uint32_t ptw_bvh_max_depth(const ptw_world* w) { return w ? w->depth : 0; }
 
-uint64_t ptw_alias_table(const double* weights, uint64_t count, pt_skybox_alias_entry* out) {
+uint64_t ptw_alias_table(const double* weights, uint64_t count, pt_skybox_alias_entry* out) try {
     if (!weights || !out) return 0;
     auto t = alias_table(weights, (size_t)count);
     std::copy(t.begin(), t.end(), out);
     return t.size();
+} catch (...) {
+    return 0;  // an allocation failed: nothing produced
 }
 
 uint64_t ptw_build_bvh(const pt_triangle_geometry* triangles, uint64_t count, pt_bvh_node* nodes_out,
-                       uint32_t* order_out) {
+                       uint32_t* order_out) try {
     if (!triangles || count == 0 || !nodes_out || !order_out) return 0;
     std::vector<pt_triangle_geometry> g(triangles, triangles + count);
     std::vector<pt_bvh_node> nodes;
@@ -926,6 +953,8 @@ uint64_t ptw_build_bvh(const pt_triangle_geometry* triangles, uint64_t count, pt
     std::copy(nodes.begin(), nodes.end(), nodes_out);
     std::copy(order.begin(), order.end(), order_out);
     return nodes.size();
+} catch (...) {
+    return 0;  // an allocation failed: nothing produced
 }
 
 }  // extern "C"
