@@ -1098,8 +1098,13 @@ static void pump_loop(pt_engine* e) {
         {
             std::lock_guard<std::recursive_mutex> g(e->mu);
             if (e->sticky == PT_OK) {
-                int rc = harvest(e, false);
-                if (!rc) rc = pump(e);
+                int rc;
+                try {
+                    rc = harvest(e, false);
+                    if (!rc) rc = pump(e);
+                } catch (...) {  // an exception leaving this thread would end the process
+                    rc = pt_abi_current_status(&e->error);
+                }
                 if (rc) e->sticky = rc;
             }
             idle = e->flights.empty();  // nothing on the GPU and nothing queued by pump()
