@@ -12,6 +12,8 @@
 // child's upper bound fits in 8 bits.  Every decoded box therefore contains
 // its binary node's box, and since the slab test is monotone in the box
 // bounds, a wide box test accepts every ray the binary node's test accepts.
+#include <array>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <system_error>
@@ -184,6 +186,62 @@ struct Work {
 
 namespace {
 
+// Frame origin and outward-rounded 8-bit child boxes of every wide node from
+// its binary children (quantise_axis); nodes are independent, so up to 16
+// host threads share them.  PT_ERR_INVALID_ARG if a child box is not finite
+// or an axis fits no exponent.
+int quantise_all(const pt_bvh_node* nodes, std::vector<pt_wide_node>& wide,
+                 const std::vector<std::array<uint32_t, 8>>& kids_of) {
+    if (kids_of.size() < wide.size()) return PT_ERR_INVALID_ARG;  // every wide node was reached by the walk
+    std::atomic<bool> bad{false};
+    const auto range = [&](size_t lo_k, size_t hi_k) {
+        for (size_t k = lo_k; k < hi_k && !bad.load(std::memory_order_relaxed); ++k) {
+            pt_wide_node& node = wide[k];
+            const int n = node.child_count;
+            float lo[3][8], hi[3][8];
+            for (int i = 0; i < n; ++i) {
+                const pt_bvh_node& c = nodes[kids_of[k][i]];
+                if (!finite_box(c)) {
+                    bad = true;
+                    return;
+                }
+                for (int a = 0; a < 3; ++a) {
+                    lo[a][i] = c.aabb_min[a];
+                    hi[a][i] = c.aabb_max[a];
+                }
+            }
+            for (int a = 0; a < 3; ++a) {
+                float origin = lo[a][0];
+                for (int i = 1; i < n; ++i) origin = std::fmin(origin, lo[a][i]);
+                node.origin[a] = origin;
+                if (!quantise_axis(origin, lo[a], hi[a], n, node.lo[a], node.hi[a], &node.exponent[a])) {
+                    bad = true;
+                    return;
+                }
+            }
+        }
+    };
+    const size_t count = wide.size();
+    unsigned threads = std::thread::hardware_concurrency();
+    threads = threads == 0 ? 1 : (threads > 16 ? 16 : threads);
+    if (count < 4096) threads = 1;
+    const size_t per = (count + threads - 1) / threads;
+    std::vector<std::thread> pool;
+    size_t next = 0;  // first node no thread has taken
+    for (unsigned t = 1; t < threads && next + per < count; ++t) {
+        const size_t lo_k = next, hi_k = lo_k + per;
+        try {
+            pool.emplace_back(range, lo_k, hi_k);
+        } catch (const std::system_error&) {
+            break;  // the calling thread takes the rest
+        }
+        next = hi_k;
+    }
+    range(next, count);
+    for (auto& th : pool) th.join();
+    return bad ? PT_ERR_INVALID_ARG : PT_OK;
+}
+
 // the collapse proper, without the octant placement
 int collapse(const pt_bvh_node* nodes, uint64_t node_count, uint32_t max_leaf_triangles,
              std::vector<pt_wide_node>& wide, uint32_t* wide_depth) {
@@ -222,6 +280,7 @@ int collapse(const pt_bvh_node* nodes, uint64_t node_count, uint32_t max_leaf_tr
     };
     wide.assign(1, pt_wide_node{});
     std::memset(wide.data(), 0, sizeof(pt_wide_node));
+    std::vector<std::array<uint32_t, 8>> kids_of(1);  // binary children of each wide node, in slot order
     std::vector<Work> stack{{0u, 0u, 1u}};
     uint32_t max_depth = 0;
     const auto interior_ok = [&](uint32_t b) {
@@ -262,27 +321,17 @@ int collapse(const pt_bvh_node* nodes, uint64_t node_count, uint32_t max_leaf_tr
             kids[best + 1] = nodes[open].left_first + 1;
             ++n;
         }
-        float lo[3][8], hi[3][8];
-        for (int i = 0; i < n; ++i) {
-            const pt_bvh_node& c = nodes[kids[i]];
-            if (!finite_box(c)) return PT_ERR_INVALID_ARG;
-            if (c.tri_count > 0xffffu) return PT_ERR_INVALID_ARG;
-            for (int a = 0; a < 3; ++a) {
-                lo[a][i] = c.aabb_min[a];
-                hi[a][i] = c.aabb_max[a];
-            }
-        }
+        for (int i = 0; i < n; ++i)
+            if (nodes[kids[i]].tri_count > 0xffffu) return PT_ERR_INVALID_ARG;
         pt_wide_node node;
         std::memset(&node, 0, sizeof node);
         node.child_count = (uint8_t)n;
         node.source_node = wk.bnode;
-        for (int a = 0; a < 3; ++a) {
-            float origin = lo[a][0];
-            for (int i = 1; i < n; ++i) origin = std::fmin(origin, lo[a][i]);
-            node.origin[a] = origin;
-            if (!quantise_axis(origin, lo[a], hi[a], n, node.lo[a], node.hi[a], &node.exponent[a]))
-                return PT_ERR_INVALID_ARG;
-        }
+        // the boxes are quantised after the walk (quantise_all), from these children
+        std::array<uint32_t, 8> slots{};
+        for (int i = 0; i < n; ++i) slots[i] = kids[i];
+        if (kids_of.size() <= wk.wide) kids_of.resize((size_t)wk.wide + 1);
+        kids_of[wk.wide] = slots;
         const uint32_t first_child = (uint32_t)wide.size();
         uint32_t next = first_child;
         for (int i = 0; i < n; ++i) {
@@ -306,7 +355,7 @@ int collapse(const pt_bvh_node* nodes, uint64_t node_count, uint32_t max_leaf_tr
             if (node.tri_count[i] == 0) stack.push_back({kids[i], node.child[i], wk.depth + 1});
     }
     if (wide_depth) *wide_depth = max_depth;
-    return PT_OK;
+    return quantise_all(nodes, wide, kids_of);
 }
 
 }  // namespace
